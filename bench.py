@@ -1,0 +1,316 @@
+#!/usr/bin/env python
+"""Benchmark of the batched modular GCD on GB300 (one JSON line on rank 0).
+
+Workload (default): the mixed batch -- 4096 pairs, operand bit lengths log-uniform in
+[1k, 64k], bits(v) = bits(u)/U(1, 2), 25% coprime, 5% v | u, 70% planted gcds of U[0, 50%] of
+the smaller operand, 32-bit moduli -- seeded synthetic data (workloads.mixed_batch).
+
+A step is the gcd of every pair of the batch.
+  value     GCDs/s with the batch resident on the device: CUDA events on the library's
+            stream around each run (residues, reduction, replay, recovery; all launches),
+            L2 flushed before every step.
+  e2e       GCDs/s through the C ABI with host buffers: mgcd_gcd_batch per step (H2D of the
+            operands, the run, D2H of the digits, conversion to binary gcds).
+  plain     the same pairs one per launch (the reference's method), on a sample.
+Every result is compared bit for bit with GMP mpz_gcd.
+
+--impl reference times the reference's CPU computation of the same batch: GMP mpz_gcd
+(testmodgcd.cpp:441, the -DNO_GPU build) on all host cores.
+"""
+import argparse
+import importlib
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+
+# Algorithmic cost model (int ops per unit of work): Barrett/Montgomery limb step 9,
+# reduction-loop update 257 (two inverses of ~19 quotient steps x 6 ops + 3 modmul + 2 modsub
+# in the reference's formulation), recovery update 124.
+OPS_RESIDUE, OPS_EUCLID, OPS_RECOVERY = 9.0, 257.0, 124.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--pairs", type=int, default=4096)
+    ap.add_argument("--seed", type=int, default=3)
+    ap.add_argument("--plain-sample", type=int, default=64)
+    ap.add_argument("--cpu-reps", type=int, default=10)
+    return ap.parse_args()
+
+
+def dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as td
+        backend = "nccl" if os.environ.get("MGCD_BENCH_BACKEND", "gloo") == "nccl" else "gloo"
+        td.init_process_group(backend=backend)
+        pg = td
+    return rank, local, world, pg
+
+
+def reduce_max(pg, x):
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+class Clocks:
+    """nvidia-smi samples (200 ms) while running."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        rows = [r.split(",") for r in open(self.f.name).read().strip().split("\n") if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.strip() == "Active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(PEAKS_FILE) as f:
+            return json.load(f), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0}, "fallback"
+
+
+def gmp_baseline(po, packed, nthreads, reps):
+    limbs, uo, ul, vo, vl = packed
+    secs, g, goff, glen = po.cpu_gmp_gcd_batch(limbs, uo, ul, vo, vl, nthreads)
+    best = [secs]
+    for _ in range(reps - 1):
+        best.append(po.cpu_gmp_gcd_batch(limbs, uo, ul, vo, vl, nthreads, want_results=False)[0])
+    return best, g, goff, glen
+
+
+def results_equal(mg, g1, o1, n1, g2, o2, n2):
+    for i in range(len(n1)):
+        a = g1[int(o1[i]): int(o1[i]) + int(n1[i])]
+        b = g2[int(o2[i]): int(o2[i]) + int(n2[i])]
+        if int(n1[i]) != int(n2[i]) or not (a == b).all():
+            return False
+    return True
+
+
+def run_reference(args, rank, pg):
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    mg = importlib.import_module("modgcd-onegpu_gb300")
+    wl = importlib.import_module("modgcd-onegpu_gb300.workloads")
+    us, vs, _ = wl.mixed_batch(args.pairs, seed=args.seed)
+    packed = mg.pack_pairs(us, vs)
+    nthreads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        po.cpu_gmp_gcd_batch(*packed, nthreads, want_results=False)
+    times = [po.cpu_gmp_gcd_batch(*packed, nthreads, want_results=False)[0] for _ in range(args.steps)]
+    tot = sum(times)
+    v = args.pairs * args.steps / tot
+    line = {
+        "impl": "reference", "metric": "GCDs/s (mixed 1k-64k-bit batch, bit-exact vs mpz_gcd)",
+        "value": v, "unit": "GCDs/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": "mixed batch: %d pairs, bits log-uniform [1k,64k], 25%% coprime, 5%% v|u, "
+                               "70%% planted gcd U[0,50%%]" % args.pairs, "modulus_bits": 32},
+        "cpu_baseline": {"value": v, "unit": "GCDs/s", "cores": nthreads, "kind": "reference",
+                         "sample": "GMP %s mpz_gcd (the reference's -DNO_GPU path, testmodgcd.cpp:441) over all "
+                                   "%d pairs per step, %d threads" % (po.gmp_version(), args.pairs, nthreads)},
+        "e2e": {"value": v, "unit": "GCDs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, local, world, pg):
+    import torch
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    mg = importlib.import_module("modgcd-onegpu_gb300")
+    wl = importlib.import_module("modgcd-onegpu_gb300.workloads")
+    torch.cuda.set_device(local)
+
+    us, vs, kinds = wl.mixed_batch(args.pairs, seed=args.seed)
+    packed = mg.pack_pairs(us, vs)
+    n = args.pairs
+    nthreads = os.cpu_count() or 1
+    # expected results: GMP mpz_gcd (also the CPU baseline on rank 0)
+    cpu_times, gx, gxo, gxn = gmp_baseline(po, packed, nthreads, args.cpu_reps if rank == 0 else 1)
+
+    dev = mg.Device(local, 32)
+    int_peak = dev.int_peak()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")   # > L2 (129 MB)
+
+    # ---- device-resident throughput
+    dev.batch_upload(*packed)
+    for _ in range(args.warmup):
+        dev.batch_run()
+        dev.batch_sync()
+    g, go, gn, st = dev.batch_download()
+    ok_dev = bool((st == 0).all()) and results_equal(mg, g, go, gn, gx, gxo, gxn)
+    work = dev.batch_work()
+    launches = dev.batch_launches()
+
+    clocks = Clocks(local)
+    barrier(pg)
+    clocks.start()
+    run_ms, dom_ms = [], []
+    wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        dev.batch_run()
+        dev.batch_sync()
+        r, d, dom_t = dev.batch_elapsed_ms()
+        run_ms.append(r)
+        dom_ms.append(d)
+    wall = time.perf_counter() - wall0
+    tot_s = reduce_max(pg, sum(run_ms) / 1e3)
+    clk = clocks.stop()
+
+    # ---- end to end through the C ABI with host buffers
+    barrier(pg)
+    e2e_t = []
+    ok_e2e = True
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        g2, go2, gn2, st2 = dev.gcd_batch_packed(*packed)
+        e2e_t.append(time.perf_counter() - t0)
+        ok_e2e = ok_e2e and bool((st2 == 0).all())
+    ok_e2e = ok_e2e and results_equal(mg, g2, go2, gn2, gx, gxo, gxn)
+    e2e_s = reduce_max(pg, sum(e2e_t))
+    h2d, d2h = dev.batch_transfer_bytes()
+
+    # ---- plain method (one pair per launch) on a sample of the same pairs
+    idx = list(range(0, n, max(1, n // args.plain_sample)))[: args.plain_sample]
+    lat = []
+    ok_plain = True
+    for i in idx:
+        t0 = time.perf_counter()
+        r = dev.gcd(us[i], vs[i])
+        lat.append(time.perf_counter() - t0)
+        ok_plain = ok_plain and r == math.gcd(us[i], vs[i])
+    plain_rate = len(idx) / sum(lat)
+    lat_ms = sorted(1e3 * x for x in lat)
+
+    if rank != 0:
+        return
+    peaks, peaks_kind = measured_peaks()
+    value = n * world * args.steps / tot_s
+    ms_step = 1e3 * tot_s / args.steps
+    ops = OPS_RESIDUE * work["residue_steps"] + OPS_EUCLID * work["euclid_updates"] + \
+        OPS_RECOVERY * work["recovery_updates"]
+    run_s = statistics.mean(run_ms) / 1e3
+    achieved = ops / run_s
+    alg_bytes = work["operand_bytes"]
+    traffic = None
+    try:
+        with open(TRAFFIC_FILE) as f:
+            traffic = json.load(f).get("bytes_per_run")
+    except (OSError, ValueError):
+        pass
+    line = {
+        "metric": "GCDs/s (mixed 1k-64k-bit batch, bit-exact vs mpz_gcd)",
+        "value": value, "unit": "GCDs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32", "data": "synthetic",
+        "config": {"workload": "mixed batch: %d pairs, bits log-uniform [1k,64k], bits(v)=bits(u)/U(1,2), "
+                               "25%% coprime, 5%% v|u, 70%% planted gcd U[0,50%%] of the smaller" % n,
+                   "modulus_bits": 32, "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "flushed before every step (256 MB write)"},
+        "bit_exact": ok_dev and ok_e2e and ok_plain,
+        "e2e": {"value": n * world * args.steps / e2e_s, "unit": "GCDs/s",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "plain": {"value": plain_rate, "unit": "GCDs/s", "sample_pairs": len(idx),
+                  "p50_ms": lat_ms[len(lat_ms) // 2], "p99_ms": lat_ms[min(len(lat_ms) - 1, int(0.99 * len(lat_ms)))],
+                  "batched_over_plain": value / world / plain_rate},
+        "batch_latency_ms": {"p50": statistics.median(run_ms), "max": max(run_ms)},
+        "roofline": {"bound": "int", "achieved": achieved / 1e9, "peak": int_peak / 1e9, "unit": "Gop/s",
+                     "frac": achieved / int_peak, "traffic": traffic,
+                     "kernel": "all launches of one step (%d persistent bucket kernels)" % launches,
+                     "model": "ops = 9*residue_steps + 257*euclid_updates + 124*recovery_updates",
+                     "peak_source": "in-repo IMAD microbenchmark (mgcd_int_peak), measured live",
+                     "hbm": {"achieved_gbs": alg_bytes / run_s / 1e9, "peak_gbs": peaks.get("hbm_gbs"),
+                             "frac": alg_bytes / run_s / 1e9 / peaks.get("hbm_gbs", 6800.0),
+                             "peak_source": peaks_kind}},
+        "work": work,
+        "dominant_kernel_ms": statistics.mean(dom_ms), "dominant_kernel_threads": dom_t,
+        "cpu_baseline": {"value": n / min(cpu_times), "unit": "GCDs/s", "cores": nthreads, "kind": "reference",
+                         "sample": "GMP %s mpz_gcd over the same %d pairs, best of %d, %d threads" %
+                                   (po.gmp_version(), n, len(cpu_times), nthreads)},
+        "gpu_launches": launches * args.steps,
+        "clocks": clk,
+        "wall_s_timed": wall,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, local, world, pg = dist()
+    if args.impl == "reference":
+        run_reference(args, rank, pg)
+    else:
+        run_ours(args, rank, local, world, pg)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

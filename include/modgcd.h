@@ -1,0 +1,142 @@
+/*  modgcd.h -- C ABI of the GB300 modular integer GCD library (libmodgcd.so).
+
+    Weber's modular integer GCD on one GPU.  Operands and results cross this boundary as
+    little-endian arrays of 32-bit limbs (the layout the reference stages with
+    mpz_export(buf, &n, -1, sizeof(uint32_t), 0, 0, x), GmpCudaDevice-gcd.cu:71-73), plain
+    pointers and sizes, and every entry point returns a status code (no exceptions cross
+    the ABI).  The C++ drop-in GmpCuda::GmpCudaDevice (GmpCuda.h) is implemented on top of
+    these calls.
+
+    Reference interfaces replaced (paths within mountunion/ModGCD-OneGPU):
+      mgcd_device_count / mgcd_set_device   GmpCudaDevice::setDevice      GmpCudaDevice.cu:96-103
+      mgcd_create / mgcd_destroy            GmpCudaDevice(), ~GmpCudaDevice  GmpCudaDevice.cu:107-144
+      mgcd_max_grid_size                    GmpCudaDevice::getMaxGridSize GmpCuda.h:118
+      mgcd_moduli_needed                    numModuliNeededFor           GmpCudaDevice-gcd.cu:49-55
+      mgcd_gcd_digits                       GmpCudaDevice::gcd up to the kernel's pair_t result
+                                                                          GmpCudaDevice-gcd.cu:59-114
+      mgcd_gcd                              GmpCudaDevice::gcd            GmpCudaDevice-gcd.cu:59-132
+      mgcd_moduli / mgcd_gen_moduli         GmpCuda::moduli[] / createModuli GmpCuda.h:126,
+                                                                          createModuli.cpp:104-179
+      mgcd_batch_* , mgcd_serve_*           no counterpart (batching and serving are new)
+*/
+#ifndef MODGCD_H
+#define MODGCD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The reference's std::runtime_error messages map to these
+   (GmpCudaDevice-gcd.cu:78, 82, 107-109); mgcd_status_string() returns the same text. */
+#define MGCD_OK                    0
+#define MGCD_ERR_INVALID_ARG       1
+#define MGCD_ERR_NO_DEVICE         2   /* "Invalid device number." */
+#define MGCD_ERR_CUDA              3
+#define MGCD_ERR_NOT_ENOUGH_MODULI 4   /* "Not enough moduli available for given input." */
+#define MGCD_ERR_GRID              5   /* "Cannot allocate enough threads to support computation." */
+#define MGCD_ERR_REDUX             6   /* "Ran out of moduli in the reduction loop." */
+#define MGCD_ERR_RECOVERY          7   /* "Ran out of moduli in the recovery loop." */
+#define MGCD_ERR_KERNEL            8   /* "Unknown error in the gcd kernel." */
+#define MGCD_ERR_TIMEOUT           9   /* a bounded device-side wait expired */
+#define MGCD_ERR_CAPACITY         10   /* caller's output buffer is too small */
+#define MGCD_ERR_BUDGET           11   /* serving: request larger than the admission budget */
+#define MGCD_ERR_BUSY             12   /* serving: queue full, retry later */
+
+/* One signed mixed-radix digit: the reference's pair_t (GmpCuda.h:112). */
+typedef struct mgcd_pair {
+  uint32_t modulus;
+  int32_t value;
+} mgcd_pair;
+
+typedef struct mgcd_context mgcd_context;
+
+const char *mgcd_status_string(int status);
+
+/* Number of CUDA devices (0 when none is usable). */
+int mgcd_device_count(int *count);
+
+/* Checks devNo like GmpCudaDevice::setDevice and makes it current for this host thread.
+   MGCD_ERR_NO_DEVICE for an invalid number. */
+int mgcd_set_device(int devNo);
+
+/* Creates a context on device `device` (-1: the current device) for modulus width L
+   (22, 27 or 32; the reference fixes L = 32 at GmpCuda.h:121).  Builds the L-bit moduli
+   table (createModuli order) and uploads it with its Montgomery constants. */
+int mgcd_create(int device, int L, mgcd_context **ctx);
+int mgcd_destroy(mgcd_context *ctx);
+
+/* Largest number of 256-modulus groups one pair may use (the reference's grid cap). */
+int mgcd_max_grid_size(const mgcd_context *ctx, int *out);
+/* Number of moduli in the context's table (the reference's NUM_MODULI). */
+int mgcd_num_moduli(const mgcd_context *ctx, size_t *out);
+/* Copies the first n moduli of the context's table. */
+int mgcd_moduli(const mgcd_context *ctx, uint32_t *out, size_t n);
+/* Moduli the reference would use for an operand of `bits` bits at width L. */
+int mgcd_moduli_needed(int L, size_t bits);
+/* The first `count` usable L-bit primes in descending order, as createModuli prints
+   them.  Returns the number written. */
+size_t mgcd_gen_moduli(int L, uint32_t *out, size_t count);
+
+/* gcd of one pair, as the signed mixed-radix digits the reference kernel returns
+   (buf[1..count) of GmpCudaDevice-gcd.cu:113-116): |g| = d[n-1], then g = g*d[i].modulus +
+   d[i].value for i = n-2..0.  u and v need not be ordered; both must be nonzero.
+   *count receives the digit count (<= cap). */
+int mgcd_gcd_digits(mgcd_context *ctx, const uint32_t *u, size_t uSz, const uint32_t *v, size_t vSz,
+                    mgcd_pair *digits, size_t cap, size_t *count);
+
+/* gcd of one pair as little-endian 32-bit limbs: g = gcd(u, v) >= 0 (gcd(x, 0) = x,
+   gcd(0, 0) = 0).  g_cap >= min(uSz, vSz) (or >= the nonzero operand's size) always
+   suffices; *g_len receives the limb count (0 for g = 0). */
+int mgcd_gcd(mgcd_context *ctx, const uint32_t *u, size_t uSz, const uint32_t *v, size_t vSz,
+             uint32_t *g, size_t g_cap, size_t *g_len);
+
+/* ----------------------------------------------------------------------- batches ----
+   Batch layout: all operand limbs in one array; pair i has u at limbs[u_off[i] ..
+   u_off[i]+u_len[i]) and v at limbs[v_off[i] .. +v_len[i]).  Results: g of pair i at
+   g[g_off[i] ..] with capacity g_cap[i] limbs, length in g_len[i], per-pair status in
+   status[i] (MGCD_OK or an error code).  The call returns MGCD_OK when every pair
+   succeeded, else the first failing pair's code. */
+int mgcd_gcd_batch(mgcd_context *ctx, size_t npairs, const uint32_t *limbs,
+                   const uint64_t *u_off, const uint32_t *u_len,
+                   const uint64_t *v_off, const uint32_t *v_len,
+                   uint32_t *g, const uint64_t *g_off, const uint32_t *g_cap, uint32_t *g_len,
+                   int32_t *status);
+
+/* The same in three steps, so that the device part can be timed and replayed with inputs
+   resident on the device:
+     mgcd_batch_upload   validates and orders the pairs on the host and copies the batch
+                         to the device (the plan stays valid until the next upload);
+     mgcd_batch_run      runs the GPU work only (queue reset + persistent kernels) on the
+                         context's stream, asynchronously; mgcd_batch_sync waits;
+     mgcd_batch_download copies the digits back and converts them to binary. */
+int mgcd_batch_upload(mgcd_context *ctx, size_t npairs, const uint32_t *limbs,
+                      const uint64_t *u_off, const uint32_t *u_len,
+                      const uint64_t *v_off, const uint32_t *v_len);
+int mgcd_batch_run(mgcd_context *ctx);
+int mgcd_batch_sync(mgcd_context *ctx);
+int mgcd_batch_download(mgcd_context *ctx, uint32_t *g, const uint64_t *g_off, const uint32_t *g_cap,
+                        uint32_t *g_len, int32_t *status);
+/* Kernel launches the last mgcd_batch_run issued. */
+int mgcd_batch_launches(const mgcd_context *ctx, int *launches);
+/* Device time of the last mgcd_batch_run (CUDA events on the context's stream around
+   the run's GPU work), after mgcd_batch_sync.  Also the time of the dominant launch (the
+   bucket kernel with the most work). */
+int mgcd_batch_elapsed_ms(const mgcd_context *ctx, float *run_ms, float *dominant_ms, int *dominant_threads);
+/* Bytes the last upload copied host->device and the last download device->host. */
+int mgcd_batch_transfer_bytes(const mgcd_context *ctx, uint64_t *h2d, uint64_t *d2h);
+/* Integer-pipe throughput of this GPU measured by a microbenchmark (independent 32-bit
+   IMAD chains on every SM): instructions per second. */
+int mgcd_int_peak(mgcd_context *ctx, double *int_ops_per_s);
+/* Total work of the uploaded batch by the algorithmic cost model (see DESIGN): residue
+   limb steps, reduction-loop updates and recovery updates, after a run completed. */
+int mgcd_batch_work(const mgcd_context *ctx, double *residue_steps, double *euclid_updates,
+                    double *recovery_updates, double *operand_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MODGCD_H */

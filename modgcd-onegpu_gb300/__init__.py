@@ -1,0 +1,303 @@
+"""GB300 modular integer GCD -- Python binding of the C ABI (include/modgcd.h, libmodgcd.so).
+
+Mirrors the reference's host object GmpCuda::GmpCudaDevice (GmpCuda.h:87-119):
+
+    Device.set_device(0)          GmpCudaDevice::setDevice     (GmpCudaDevice.cu:96-103)
+    dev = Device()                GmpCudaDevice()              (GmpCudaDevice.cu:107-137)
+    dev.gcd(u, v)                 GmpCudaDevice::gcd           (GmpCudaDevice-gcd.cu:57-132)
+    dev.max_grid_size             getMaxGridSize               (GmpCuda.h:118)
+
+plus batches (``gcd_batch`` and the upload/run/download steps).  Errors raise
+``GcdError`` with the reference's messages.  Every computation runs on the GPU through
+libmodgcd.so; there is no CPU path, and importing fails loudly if the library is missing.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_DIR = os.path.join(HERE, "lib")
+LIB_PATH = os.path.join(LIB_DIR, "libmodgcd.so")
+
+MGCD_OK = 0
+MGCD_ERR_NO_DEVICE = 2
+STATUS_NAMES = {
+    0: "MGCD_OK", 1: "MGCD_ERR_INVALID_ARG", 2: "MGCD_ERR_NO_DEVICE", 3: "MGCD_ERR_CUDA",
+    4: "MGCD_ERR_NOT_ENOUGH_MODULI", 5: "MGCD_ERR_GRID", 6: "MGCD_ERR_REDUX", 7: "MGCD_ERR_RECOVERY",
+    8: "MGCD_ERR_KERNEL", 9: "MGCD_ERR_TIMEOUT", 10: "MGCD_ERR_CAPACITY", 11: "MGCD_ERR_BUDGET",
+    12: "MGCD_ERR_BUSY",
+}
+
+# Every function declared in include/modgcd.h, with its ctypes signature.
+_c = ctypes
+_P = _c.c_void_p
+SIGNATURES = {
+    "mgcd_status_string": (_c.c_char_p, [_c.c_int]),
+    "mgcd_device_count": (_c.c_int, [_c.POINTER(_c.c_int)]),
+    "mgcd_set_device": (_c.c_int, [_c.c_int]),
+    "mgcd_create": (_c.c_int, [_c.c_int, _c.c_int, _c.POINTER(_P)]),
+    "mgcd_destroy": (_c.c_int, [_P]),
+    "mgcd_max_grid_size": (_c.c_int, [_P, _c.POINTER(_c.c_int)]),
+    "mgcd_num_moduli": (_c.c_int, [_P, _c.POINTER(_c.c_size_t)]),
+    "mgcd_moduli": (_c.c_int, [_P, _P, _c.c_size_t]),
+    "mgcd_moduli_needed": (_c.c_int, [_c.c_int, _c.c_size_t]),
+    "mgcd_gen_moduli": (_c.c_size_t, [_c.c_int, _P, _c.c_size_t]),
+    "mgcd_gcd_digits": (_c.c_int, [_P, _P, _c.c_size_t, _P, _c.c_size_t, _P, _c.c_size_t,
+                                   _c.POINTER(_c.c_size_t)]),
+    "mgcd_gcd": (_c.c_int, [_P, _P, _c.c_size_t, _P, _c.c_size_t, _P, _c.c_size_t, _c.POINTER(_c.c_size_t)]),
+    "mgcd_gcd_batch": (_c.c_int, [_P, _c.c_size_t, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "mgcd_batch_upload": (_c.c_int, [_P, _c.c_size_t, _P, _P, _P, _P, _P]),
+    "mgcd_batch_run": (_c.c_int, [_P]),
+    "mgcd_batch_sync": (_c.c_int, [_P]),
+    "mgcd_batch_download": (_c.c_int, [_P, _P, _P, _P, _P, _P]),
+    "mgcd_batch_launches": (_c.c_int, [_P, _c.POINTER(_c.c_int)]),
+    "mgcd_batch_work": (_c.c_int, [_P, _c.POINTER(_c.c_double), _c.POINTER(_c.c_double),
+                                   _c.POINTER(_c.c_double), _c.POINTER(_c.c_double)]),
+    "mgcd_batch_elapsed_ms": (_c.c_int, [_P, _c.POINTER(_c.c_float), _c.POINTER(_c.c_float),
+                                         _c.POINTER(_c.c_int)]),
+    "mgcd_batch_transfer_bytes": (_c.c_int, [_P, _c.POINTER(_c.c_uint64), _c.POINTER(_c.c_uint64)]),
+    "mgcd_int_peak": (_c.c_int, [_P, _c.POINTER(_c.c_double)]),
+}
+
+_lib = None
+
+
+class GcdError(RuntimeError):
+    """A failed call; ``status`` is the MGCD_* code, the message the reference's text."""
+
+    def __init__(self, status, msg):
+        super().__init__(msg)
+        self.status = status
+
+
+def load():
+    """Loads libmodgcd.so (built in-tree by build.py) and declares its signatures."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libmodgcd.so is not built (%s): run modgcd-onegpu_gb300/build.py" % LIB_PATH)
+        lib = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def status_string(code):
+    return load().mgcd_status_string(int(code)).decode()
+
+
+def _check(code):
+    if code != MGCD_OK:
+        raise GcdError(code, status_string(code))
+
+
+def _ptr(a):
+    return a.ctypes.data if a is not None and a.size else None
+
+
+# ------------------------------------------------------------------ integers <-> limbs ----
+
+def to_limbs(x):
+    """|x| as little-endian uint32 limbs (mpz_export(..., -1, 4, 0, 0, x)); 0 -> empty."""
+    x = abs(int(x))
+    if x == 0:
+        return np.zeros(0, dtype=np.uint32)
+    n = (x.bit_length() + 31) // 32
+    return np.frombuffer(x.to_bytes(4 * n, "little"), dtype="<u4").astype(np.uint32)
+
+
+def from_limbs(a):
+    return int.from_bytes(np.ascontiguousarray(a, dtype="<u4").tobytes(), "little")
+
+
+def pack_pairs(us, vs):
+    """Packs operand pairs into the batch layout: (limbs, u_off, u_len, v_off, v_len)."""
+    parts, uo, ul, vo, vl = [], [], [], [], []
+    off = 0
+    for u, v in zip(us, vs):
+        a, b = to_limbs(u), to_limbs(v)
+        uo.append(off); ul.append(len(a)); parts.append(a); off += len(a)
+        vo.append(off); vl.append(len(b)); parts.append(b); off += len(b)
+    limbs = np.concatenate(parts) if parts else np.zeros(0, dtype=np.uint32)
+    return (np.ascontiguousarray(limbs, dtype=np.uint32), np.array(uo, dtype=np.uint64),
+            np.array(ul, dtype=np.uint32), np.array(vo, dtype=np.uint64), np.array(vl, dtype=np.uint32))
+
+
+def result_layout(u_len, v_len):
+    """Output capacity per pair (max operand size + 1) and offsets."""
+    cap = (np.maximum(u_len, v_len).astype(np.uint64) + 1).astype(np.uint32)
+    off = np.zeros(len(cap), dtype=np.uint64)
+    if len(cap):
+        off[1:] = np.cumsum(cap[:-1], dtype=np.uint64)
+    return off, cap, int(cap.sum(dtype=np.uint64))
+
+
+def moduli_needed(bits, L=32):
+    return load().mgcd_moduli_needed(int(L), int(bits))
+
+
+def gen_moduli(L, count):
+    out = np.zeros(count, dtype=np.uint32)
+    n = load().mgcd_gen_moduli(int(L), out.ctypes.data, count)
+    return out[:n]
+
+
+def device_count():
+    n = ctypes.c_int()
+    _check(load().mgcd_device_count(ctypes.byref(n)))
+    return n.value
+
+
+class Device:
+    """One context (moduli table resident on the GPU) -- GmpCuda::GmpCudaDevice."""
+
+    @staticmethod
+    def set_device(dev_no=0):
+        rc = load().mgcd_set_device(int(dev_no))
+        if rc == MGCD_ERR_NO_DEVICE:
+            raise GcdError(rc, "Invalid device number.")
+        _check(rc)
+
+    def __init__(self, device=-1, L=32):
+        self._lib = load()
+        self.L = L
+        h = ctypes.c_void_p()
+        _check(self._lib.mgcd_create(int(device), int(L), ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.mgcd_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def max_grid_size(self):
+        n = ctypes.c_int()
+        _check(self._lib.mgcd_max_grid_size(self._h, ctypes.byref(n)))
+        return n.value
+
+    @property
+    def num_moduli(self):
+        n = ctypes.c_size_t()
+        _check(self._lib.mgcd_num_moduli(self._h, ctypes.byref(n)))
+        return n.value
+
+    def moduli(self, n):
+        out = np.zeros(n, dtype=np.uint32)
+        _check(self._lib.mgcd_moduli(self._h, out.ctypes.data, n))
+        return out
+
+    def gcd(self, u, v):
+        """gcd(u, v) of two Python integers (signs ignored)."""
+        a, b = to_limbs(u), to_limbs(v)
+        cap = max(len(a), len(b)) + 1
+        g = np.zeros(cap, dtype=np.uint32)
+        n = ctypes.c_size_t()
+        _check(self._lib.mgcd_gcd(self._h, _ptr(a), len(a), _ptr(b), len(b), g.ctypes.data, cap, ctypes.byref(n)))
+        return from_limbs(g[: n.value])
+
+    def gcd_digits(self, u, v):
+        """The signed mixed-radix digits [(modulus, value), ...] the kernel returns."""
+        a, b = to_limbs(u), to_limbs(v)
+        cap = moduli_needed(max(abs(u), abs(v)).bit_length(), self.L) + 2
+        d = np.zeros(cap, dtype=[("modulus", "<u4"), ("value", "<i4")])
+        n = ctypes.c_size_t()
+        _check(self._lib.mgcd_gcd_digits(self._h, _ptr(a), len(a), _ptr(b), len(b), d.ctypes.data, cap,
+                                         ctypes.byref(n)))
+        return [(int(m), int(x)) for m, x in d[: n.value]]
+
+    # ------------------------------------------------------------------ batches ----
+    def gcd_batch(self, us, vs, return_status=False):
+        """[gcd(u, v) for u, v in zip(us, vs)] in one batched run."""
+        packed = pack_pairs(us, vs)
+        g, g_off, g_len, st = self.gcd_batch_packed(*packed)
+        res = [from_limbs(g[int(o): int(o) + int(n)]) for o, n in zip(g_off, g_len)]
+        if return_status:
+            return res, st
+        bad = np.nonzero(st != MGCD_OK)[0]
+        if len(bad):
+            raise GcdError(int(st[bad[0]]), status_string(int(st[bad[0]])))
+        return res
+
+    def gcd_batch_packed(self, limbs, u_off, u_len, v_off, v_len):
+        n = len(u_off)
+        g_off, g_cap, tot = result_layout(u_len, v_len)
+        g = np.zeros(max(tot, 1), dtype=np.uint32)
+        g_len = np.zeros(n, dtype=np.uint32)
+        st = np.zeros(n, dtype=np.int32)
+        self._lib.mgcd_gcd_batch(self._h, n, _ptr(limbs), _ptr(u_off), _ptr(u_len), _ptr(v_off), _ptr(v_len),
+                                 g.ctypes.data, _ptr(g_off), _ptr(g_cap), _ptr(g_len), _ptr(st))
+        return g, g_off, g_len, st
+
+    def batch_upload(self, limbs, u_off, u_len, v_off, v_len):
+        self._batch_layout = (len(u_off),) + result_layout(u_len, v_len)
+        _check(self._lib.mgcd_batch_upload(self._h, len(u_off), _ptr(limbs), _ptr(u_off), _ptr(u_len),
+                                           _ptr(v_off), _ptr(v_len)))
+
+    def batch_run(self):
+        _check(self._lib.mgcd_batch_run(self._h))
+
+    def batch_sync(self):
+        _check(self._lib.mgcd_batch_sync(self._h))
+
+    def batch_download(self):
+        n, g_off, g_cap, tot = self._batch_layout
+        g = np.zeros(max(tot, 1), dtype=np.uint32)
+        g_len = np.zeros(n, dtype=np.uint32)
+        st = np.zeros(n, dtype=np.int32)
+        self._lib.mgcd_batch_download(self._h, g.ctypes.data, _ptr(g_off), _ptr(g_cap), _ptr(g_len), _ptr(st))
+        return g, g_off, g_len, st
+
+    def batch_launches(self):
+        n = ctypes.c_int()
+        _check(self._lib.mgcd_batch_launches(self._h, ctypes.byref(n)))
+        return n.value
+
+    def batch_elapsed_ms(self):
+        """(run_ms, dominant_kernel_ms, dominant_threads) of the last run, by CUDA events."""
+        r, d, t = ctypes.c_float(), ctypes.c_float(), ctypes.c_int()
+        _check(self._lib.mgcd_batch_elapsed_ms(self._h, ctypes.byref(r), ctypes.byref(d), ctypes.byref(t)))
+        return r.value, d.value, t.value
+
+    def batch_transfer_bytes(self):
+        h, d = ctypes.c_uint64(), ctypes.c_uint64()
+        _check(self._lib.mgcd_batch_transfer_bytes(self._h, ctypes.byref(h), ctypes.byref(d)))
+        return h.value, d.value
+
+    def int_peak(self):
+        """Measured 32-bit IMAD throughput of the GPU (instructions/s)."""
+        x = ctypes.c_double()
+        _check(self._lib.mgcd_int_peak(self._h, ctypes.byref(x)))
+        return x.value
+
+    def batch_work(self):
+        r, e, m, b = (ctypes.c_double() for _ in range(4))
+        _check(self._lib.mgcd_batch_work(self._h, ctypes.byref(r), ctypes.byref(e), ctypes.byref(m),
+                                         ctypes.byref(b)))
+        return {"residue_steps": r.value, "euclid_updates": e.value, "recovery_updates": m.value,
+                "operand_bytes": b.value}
+
+
+def build(verbose=False):
+    """Compiles libmodgcd.so / libGmpCuda.so in-tree (nvcc for sm_103a)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_mgcd_build", os.path.join(HERE, "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(verbose=verbose)

@@ -1,0 +1,189 @@
+// mgcd_device.cuh -- device arithmetic of the modular GCD kernels (sm_103a).
+//
+// Per-modulus arithmetic is done in Montgomery form with R = 2^32 (REDC), and modular
+// inverses by the extended Euclidean algorithm with float-reciprocal quotient estimates
+// followed by an exact integer correction.  Everything here is bit-exact integer math;
+// floats only ever produce a quotient estimate that is corrected, and every inverse is
+// checked (x * x^-1 == 1) before it is used.
+#pragma once
+#include <cstdint>
+
+namespace mgcd {
+
+// Per-modulus constants, one 16-byte record per table entry.
+//   q    : the prime modulus (table order = createModuli order, descending)
+//   qinv : -q^{-1} mod 2^32 (Montgomery)
+//   r2   : 2^64 mod q
+struct __align__(16) ModConst {
+  uint32_t q, qinv, r2, pad;
+};
+
+// State of one modulus during the reduction loop: t = u_q / v_q mod q, or a marker.
+constexpr uint32_t T_INF = 0xFFFFFFFFu;      // v == 0 (mod q), u != 0
+constexpr uint32_t T_DEGEN = 0xFFFFFFFEu;    // u == v == 0 (mod q): q divides both
+constexpr uint32_t T_RETIRED = 0xFFFFFFFDu;  // q was used as a pivot
+constexpr uint32_t T_MARK = T_RETIRED;       // t >= T_MARK: not a finite ratio
+constexpr uint32_t U_RETIRED = 0xFFFFFFFFu;  // recovery: modulus consumed by a digit
+constexpr int32_t MOD_INFINITY = INT32_MIN;  // reference MOD_INFINITY (GmpCudaDevice-getGcdKernel.cu:46)
+constexpr uint32_t KEY_INF_HI = 0x80000000u; // |MOD_INFINITY| as the key's high word
+
+// T * 2^-32 mod q for T < q * 2^32; result in [0, q).
+__device__ __forceinline__ uint32_t redc(uint64_t T, uint32_t q, uint32_t qinv)
+{
+  const uint32_t lo = (uint32_t)T, hi = (uint32_t)(T >> 32);
+  const uint32_t m = lo * qinv;                   // T + m*q == 0 (mod 2^32)
+  const uint32_t mh = __umulhi(m, q);
+  const uint64_t t = (uint64_t)hi + mh + (lo != 0u);   // (T + m*q) / 2^32 < 2q
+  return (uint32_t)(t >= q ? t - q : t);
+}
+
+// a * b * 2^-32 mod q, a, b < q.
+__device__ __forceinline__ uint32_t mont_mul(uint32_t a, uint32_t b, uint32_t q, uint32_t qinv)
+{
+  return redc((uint64_t)a * b, q, qinv);
+}
+
+__device__ __forceinline__ uint32_t mod_sub(uint32_t a, uint32_t b, uint32_t q)
+{
+  return a - b + ((a < b) ? q : 0u);
+}
+
+// Symmetric residue with the reference's boundary (toSigned, GmpCudaDevice-getGcdKernel.cu:273-281):
+// x >= q/2 maps to x - q.
+__device__ __forceinline__ int32_t to_signed(uint32_t x, uint32_t q)
+{
+  return (x >= (q >> 1)) ? (int32_t)(x - q) : (int32_t)x;
+}
+
+// fromSigned (GmpCudaDevice-getGcdKernel.cu:264-271) for |x| < q.
+__device__ __forceinline__ uint32_t from_signed(int32_t x, uint32_t q)
+{
+  return (uint32_t)x + ((x < 0) ? q : 0u);
+}
+
+__device__ __forceinline__ float rcp_approx(float y)
+{
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(y));
+  return r;
+}
+
+// Exact inverse by integer-only extended Euclid (64-bit division); the fallback that
+// runs only if the fast routine's self-check ever fails.
+__device__ __noinline__ uint32_t inv_mod_slow(uint32_t x, uint32_t q)
+{
+  int64_t r0 = q, r1 = x, s0 = 0, s1 = 1;
+  while (r1 != 0) {
+    const int64_t Q = r0 / r1;
+    int64_t t = r0 - Q * r1; r0 = r1; r1 = t;
+    t = s0 - Q * s1; s0 = s1; s1 = t;
+  }
+  return (uint32_t)(s0 < 0 ? s0 + q : s0);
+}
+
+// x^{-1} mod q for 0 < x < q, q an odd prime < 2^32.
+//
+// Extended Euclid on (r0, r1) = (q, x) tracking the unsigned cofactor s with
+// s_k * x == (-1)^k * r1_k (mod q); at r1 = 1 the inverse is s or q - s by parity.
+// Quotients come from a float reciprocal estimate biased low so that the estimate is
+// the true quotient or one less, then one exact integer correction step:
+//   phase A (r1 >= 2^22): operands rounded up to float, quotient < 2^10, error < 2^-10;
+//   phase B (r0 >= 2^22 > r1): one exact integer division at the transition;
+//   phase C (r0, r1 < 2^22): operands exact in float, remainders exact by FMA, quotient
+//            read from the float's mantissa (x + 2^23 trick), no conversion instruction.
+// The bounds assume rcp.approx.ftz.f32's documented error (1 ulp).  The result is then
+// checked (x * inv == 1 mod q) and recomputed by the integer-only routine if it is wrong,
+// so no float error can reach a result.
+__device__ __forceinline__ uint32_t inv_mod(uint32_t x, uint32_t q, uint32_t qinv)
+{
+  uint32_t r0 = q, r1 = x, s0 = 0, s1 = 1, par = 0;
+  while (r1 >= (1u << 22)) {
+    const float f1 = __uint2float_ru(r1);
+    const float est = __fmaf_rz(__uint2float_ru(r0), rcp_approx(f1), -0x1p-9f);
+    uint32_t Q = __float2uint_rz(est);
+    uint32_t r = r0 - Q * r1;
+    if (r >= r1) { r -= r1; Q += 1; }
+    const uint32_t s = s0 + Q * s1;
+    r0 = r1; r1 = r; s0 = s1; s1 = s; par ^= 1u;
+  }
+  if (r1 > 1u) {
+    if (r0 >= (1u << 22)) {
+      const uint32_t Q = r0 / r1;
+      const uint32_t r = r0 - Q * r1;
+      const uint32_t s = s0 + Q * s1;
+      r0 = r1; r1 = r; s0 = s1; s1 = s; par ^= 1u;
+    }
+    float f0 = (float)r0, f1 = (float)r1;
+    int guard = 64;
+    while (f1 > 1.0f && --guard) {
+      const float rc = rcp_approx(f1);
+      float qm = __fmaf_rz(f0, rc, 8388607.5f);     // 2^23 + floor(f0*rc - 1/2)
+      const float qf = qm - 8388608.0f;
+      float rem = __fmaf_rn(-qf, f1, f0);          // exact: an integer below 2^24
+      if (rem >= f1) { rem -= f1; qm += 1.0f; }
+      const uint32_t Q = __float_as_uint(qm) - 0x4B000000u;
+      const uint32_t s = s0 + Q * s1;
+      f0 = f1; f1 = rem; s0 = s1; s1 = s; par ^= 1u;
+    }
+  }
+  const uint32_t inv = par ? q - s1 : s1;
+  // inv * x == 1 (mod q)  <=>  redc(inv * x) == redc(1)
+  if (redc((uint64_t)inv * x, q, qinv) != redc(1ull, q, qinv))
+    return inv_mod_slow(x, q);
+  return inv;
+}
+
+// Key of the reduction loop's pivot choice (postMinPair, GmpCudaDevice-getGcdKernel.cu:152-154):
+// high word |value| (0x80000000 for MOD_INFINITY), low word modulus - (value >= 0).
+__device__ __forceinline__ void t_key(uint32_t t, uint32_t q, uint32_t& hi, uint32_t& lo)
+{
+  if (t >= T_MARK) { hi = KEY_INF_HI; lo = q; return; }
+  const bool neg = t >= (q >> 1);
+  hi = neg ? q - t : t;
+  lo = neg ? q : q - 1u;
+}
+
+__device__ __forceinline__ bool key_less(uint32_t h1, uint32_t l1, uint32_t h2, uint32_t l2)
+{
+  return h1 < h2 || (h1 == h2 && l1 < l2);
+}
+
+// (p, b) from a key (collectMinPair, GmpCudaDevice-getGcdKernel.cu:214-219).
+__device__ __forceinline__ void key_pair(uint32_t hi, uint32_t lo, uint32_t& p, int32_t& b)
+{
+  p = lo | 1u;
+  b = (lo & 1u) ? (int32_t)(0u - hi) : (int32_t)hi;
+}
+
+// Lexicographic (hi, lo) minimum over the warp, result in every lane.
+__device__ __forceinline__ void warp_min_key(uint32_t& hi, uint32_t& lo)
+{
+  const uint32_t mh = __reduce_min_sync(0xFFFFFFFFu, hi);
+  const uint32_t ml = __reduce_min_sync(0xFFFFFFFFu, hi == mh ? lo : 0xFFFFFFFFu);
+  hi = mh;
+  lo = ml;
+}
+
+// One reduction-loop update of a modulus state t for pivot (p, b):
+//   t' = p / (t - b)  (mod q)   since t' = u'/v' = v / ((u - b v)/p)
+// with t = INF -> 0 (v was 0: u' = 0, v' = u/p), t == b -> INF (v' = 0), degenerate and
+// retired states fixed; the pivot's own modulus retires.
+__device__ __forceinline__ uint32_t t_update(uint32_t t, uint32_t q, uint32_t qinv, uint32_t p, int32_t b)
+{
+  if (t >= T_MARK) return (t == T_INF) ? 0u : t;
+  if (q == p) return T_RETIRED;
+  const uint32_t pm = (p > q) ? p - q : p;
+  const uint32_t d = mod_sub(t, from_signed(b, q), q);
+  if (d == 0u) return T_INF;
+  // redc(d) = d/R, inv = R/d, mont_mul(pm, R/d) = pm/d
+  return mont_mul(pm, inv_mod(redc((uint64_t)d, q, qinv), q, qinv), q, qinv);
+}
+
+// Initial state t = u/v mod q from the residues.
+__device__ __forceinline__ uint32_t t_init(uint32_t u, uint32_t v, uint32_t q, uint32_t qinv)
+{
+  if (v == 0u) return (u == 0u) ? T_DEGEN : T_INF;
+  return mont_mul(u, inv_mod(redc((uint64_t)v, q, qinv), q, qinv), q, qinv);
+}
+
+}  // namespace mgcd

@@ -1,0 +1,83 @@
+// mgcd_internal.h -- types shared by the host orchestration and the kernels.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/modgcd.h"
+
+namespace mgcd {
+
+struct ModConst;
+
+// One gcd job.  u is the larger operand (u >= v > 0); both are little-endian 32-bit limbs
+// in the batch's limb array, with no leading zero limbs.
+struct PairDesc {
+  uint64_t u_off, v_off;
+  uint32_t u_len, v_len;
+  uint32_t nq;       // moduli used (multiple of 256)
+  uint32_t out_off;  // first digit slot in the digit array; nq + 1 slots are reserved
+};
+
+// Per-pair results written by the kernels.
+enum : int32_t {
+  ST_OK = 0,
+  ST_REDUX = 1,      // ran out of moduli in the reduction loop
+  ST_RECOVERY = 2,   // ran out of moduli in the recovery loop
+  ST_TIMEOUT = 3,    // a bounded cross-CTA wait expired
+  ST_PENDING = -1
+};
+
+struct BatchArgs {
+  const uint32_t* limbs;
+  const PairDesc* pairs;
+  const uint32_t* order;     // processing order (indices into pairs)
+  uint32_t npairs;
+  const ModConst* mods;
+  int L;
+  uint32_t* queue;           // work counter, zero before launch
+  uint32_t* scratch;         // per-CTA scratch: u0[nq_max], v0[nq_max], hist[2*nq_max]
+  size_t scratch_words;      // words per CTA
+  uint32_t nq_max;
+  mgcd_pair* digits;
+  uint32_t* count;           // digits per pair
+  uint32_t* iters;           // reduction iterations per pair (work accounting)
+  int32_t* status;
+};
+
+// State of the cross-CTA reduction used by a single pair spread over a cooperative grid.
+struct GridSync {
+  unsigned long long slot[3];
+  unsigned int arrive;
+  unsigned int error;
+  unsigned long long timeout_ns;
+};
+
+struct GridArgs {
+  const uint32_t* limbs;
+  PairDesc pair;
+  const ModConst* mods;
+  int L;
+  uint32_t* scratch;         // u0[nq], v0[nq], hist[2*nq]
+  GridSync* sync;
+  uint32_t per_cta;          // moduli owned by each CTA (contiguous ranges)
+  mgcd_pair* digits;
+  uint32_t* count;
+  uint32_t* iters;
+  int32_t* status;
+};
+
+// Launch helpers (mgcd_kernels.cu).
+size_t batch_smem_bytes(int threads, uint32_t nq_max);
+cudaError_t batch_max_blocks_per_sm(int threads, size_t smem, int* blocks);
+cudaError_t launch_batch(const BatchArgs& a, int threads, int grid, size_t smem, cudaStream_t s);
+
+size_t grid_smem_bytes(uint32_t per_cta);
+cudaError_t grid_max_blocks_per_sm(size_t smem, int* blocks);
+constexpr int GRID_THREADS = 1024;
+cudaError_t launch_grid(const GridArgs& a, int grid, size_t smem, cudaStream_t s);
+
+// 256-thread blocks, 8 IMADs per thread per iteration.
+cudaError_t launch_int_peak(uint32_t* out, int blocks, int iters, cudaStream_t s);
+
+}  // namespace mgcd

@@ -198,7 +198,7 @@ def cpu_gmp_gcd_batch(limbs, u_off, u_len, v_off, v_len, nthreads: int, want_res
     v_off = np.ascontiguousarray(v_off, dtype=np.uint64)
     u_len = np.ascontiguousarray(u_len, dtype=np.uint32)
     v_len = np.ascontiguousarray(v_len, dtype=np.uint32)
-    g_cap = np.maximum(np.minimum(u_len, v_len), 1).astype(np.uint32)
+    g_cap = np.maximum(np.maximum(u_len, v_len), 1).astype(np.uint32)
     g_off = np.zeros(n, dtype=np.uint64)
     if n:
         g_off[1:] = np.cumsum(g_cap[:-1], dtype=np.uint64)

@@ -1,0 +1,142 @@
+"""GPU parity: the CUDA path against the oracle, bit for bit.
+
+Final results against GMP mpz_gcd / Python's exact gcd; the digit list (the kernel's
+pair_t output) against the restated reference algorithm, element by element."""
+import hashlib
+import math
+import os
+import random
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden_pairs
+
+pytestmark = pytest.mark.gpu
+
+
+def rand_pair(rng, nbits, gbits, vbits=None):
+    g = rng.getrandbits(gbits) | (1 << (gbits - 1)) if gbits > 0 else 1
+    a = rng.getrandbits(max(nbits - gbits, 1)) | 1
+    b = rng.getrandbits(max((vbits or nbits) - gbits, 1)) | 1
+    return g * a, g * b
+
+
+@pytest.mark.parametrize("case_idx", range(8))
+def test_golden_reference_inputs(device, golden, case_idx):
+    """The reference driver's own inputs: gcd exact, digits identical to the oracle's."""
+    case = golden["cases"][case_idx]
+    pairs = golden_pairs(case)
+    for (u, v), exp in zip(pairs, case["pairs"]):
+        g = int(exp["gcd_hex"], 16)
+        assert device.gcd(u, v) == g
+        dig = device.gcd_digits(u, v)
+        assert len(dig) == exp["digits"]
+        assert hashlib.sha1(repr(dig).encode()).hexdigest() == exp["digits_sha1"]
+    res = device.gcd_batch([u for u, _ in pairs], [v for _, v in pairs])
+    assert res == [int(e["gcd_hex"], 16) for e in case["pairs"]]
+
+
+def test_digits_match_oracle_random(device, oracle):
+    rng = random.Random(11)
+    mod32 = oracle.gen_moduli(32, 4096)
+    for nbits, gbits in [(64, 1), (300, 50), (1000, 1), (2048, 700), (4096, 1024), (8000, 4000)]:
+        for _ in range(3):
+            u, v = rand_pair(rng, nbits, gbits)
+            uu, vv = max(u, v), min(u, v)
+            nq = oracle.num_moduli_needed(uu.bit_length(), 32)
+            st, dig, tr, it = oracle.modgcd(uu, vv, 32, mod32, nq)
+            assert st == 0
+            assert device.gcd_digits(u, v) == dig
+            assert device.gcd(u, v) == math.gcd(u, v)
+
+
+def test_batch_mixed_sizes(device):
+    rng = random.Random(12)
+    us, vs = [], []
+    for _ in range(300):
+        nb = int(2 ** rng.uniform(6, 14.5))
+        gb = rng.randint(0, nb // 2)
+        u, v = rand_pair(rng, nb, gb, vbits=max(gb + 1, int(nb / rng.uniform(1, 2))))
+        us.append(u)
+        vs.append(v)
+    res = device.gcd_batch(us, vs)
+    assert res == [math.gcd(u, v) for u, v in zip(us, vs)]
+
+
+def test_edge_cases(device):
+    rng = random.Random(13)
+    x = rng.getrandbits(5000) | 1
+    q0 = 4294967291
+    cases = [(x, x), (x * 987654321, x), (x, x * 3), (x << 64, x), (1, 1), (1, 2), (2, 1),
+             (0xFFFFFFFF, 0xFFFFFFFB), (2 ** 32, 2 ** 31), (q0 * x, q0 * 7), (q0 ** 3, q0 ** 2 * 5),
+             (x, 0), (0, x), (0, 0), (2 ** 4000, 2 ** 3999 * 3)]
+    for u, v in cases:
+        assert device.gcd(u, v) == math.gcd(u, v), (u.bit_length(), v.bit_length())
+    res = device.gcd_batch([u for u, _ in cases], [v for _, v in cases])
+    assert res == [math.gcd(u, v) for u, v in cases]
+
+
+def test_order_and_leading_zero_limbs(device, mgcd):
+    rng = random.Random(14)
+    u, v = rand_pair(rng, 3000, 500)
+    a, b = mgcd.to_limbs(u), mgcd.to_limbs(v)
+    z = np.zeros(2, dtype=np.uint32)
+    # pair 0: (v, u) with two zero limbs above v's top limb; pair 1: (u, v) sharing the limbs
+    limbs = np.concatenate([b, z, a]).astype(np.uint32)
+    uo = np.array([0, len(b) + 2], dtype=np.uint64)
+    ul = np.array([len(b) + 2, len(a)], dtype=np.uint32)
+    vo = np.array([len(b) + 2, 0], dtype=np.uint64)
+    vl = np.array([len(a), len(b)], dtype=np.uint32)
+    g, g_off, g_len, st = device.gcd_batch_packed(limbs, uo, ul, vo, vl)
+    assert list(st) == [0, 0]
+    for i in range(2):
+        assert mgcd.from_limbs(g[int(g_off[i]): int(g_off[i]) + int(g_len[i])]) == math.gcd(u, v)
+
+
+@pytest.mark.parametrize("L", [22, 27])
+def test_other_modulus_widths(mgcd, oracle, L):
+    rng = random.Random(15 + L)
+    with mgcd.Device(0, L) as dev:
+        mods = oracle.gen_moduli(L, 8192)
+        us, vs = [], []
+        for nbits, gbits in [(100, 1), (1000, 300), (4096, 1024), (10000, 2500)]:
+            u, v = rand_pair(rng, nbits, gbits)
+            uu, vv = max(u, v), min(u, v)
+            nq = oracle.num_moduli_needed(uu.bit_length(), L)
+            st, dig, _, _ = oracle.modgcd(uu, vv, L, mods, nq)
+            assert st == 0
+            assert dev.gcd_digits(u, v) == dig
+            us.append(u)
+            vs.append(v)
+        assert dev.gcd_batch(us, vs) == [math.gcd(a, b) for a, b in zip(us, vs)]
+
+
+def test_large_pairs_cooperative_grid(device):
+    """Pairs too large for one CTA run on the cooperative grid (plain path above 2,048
+    moduli, batch path above 16,384)."""
+    rng = random.Random(16)
+    u, v = rand_pair(rng, 65536, 16384)
+    assert device.gcd(u, v) == math.gcd(u, v)                       # plain, grid mode
+    u2, v2 = rand_pair(rng, 262144, 65536)
+    assert device.gcd_batch([u2, u], [v2, v]) == [math.gcd(u2, v2), math.gcd(u, v)]
+
+
+def test_not_enough_moduli(mgcd):
+    with mgcd.Device(0, 22) as dev:
+        x = (1 << 1_300_000) + 1
+        with pytest.raises(mgcd.GcdError) as e:
+            dev.gcd(x, x - 2)
+        assert str(e.value) == "Not enough moduli available for given input."
+
+
+def test_cpp_dropin_driver(mgcd):
+    exe = os.path.join(mgcd.LIB_DIR, "testmodgcd_gb300")
+    for f in ("ref_1024-1.txt", "ref_10240-2048.txt", "ref_16384-4096.txt"):
+        for extra in ([], ["--batch"]):
+            r = subprocess.run([exe, "file", os.path.join(GOLDEN, f)] + extra, capture_output=True, text=True)
+            assert r.returncode == 0, r.stdout + r.stderr
+            assert '"mismatches": 0, "errors": 0' in r.stdout
+    r = subprocess.run([exe, "rand", "5000", "1200", "6", "42"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr

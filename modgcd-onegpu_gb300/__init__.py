@@ -58,6 +58,7 @@ SIGNATURES = {
                                          _c.POINTER(_c.c_int)]),
     "mgcd_batch_transfer_bytes": (_c.c_int, [_P, _c.POINTER(_c.c_uint64), _c.POINTER(_c.c_uint64)]),
     "mgcd_int_peak": (_c.c_int, [_P, _c.POINTER(_c.c_double)]),
+    "mgcd_gcd_digits_noalloc": (_c.c_int, [_P, _c.c_size_t, _c.c_size_t, _P, _c.c_size_t, _P, _P, _P]),
 }
 
 _lib = None

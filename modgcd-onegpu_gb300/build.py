@@ -63,7 +63,7 @@ def build(verbose=False, force=False):
     hdrs = _headers()
     cuda_inc = "-I" + os.path.join(CUDA_HOME, "include")
     units = []
-    for f in ("mgcd_kernels.cu",):
+    for f in ("mgcd_kernels.cu", "mgcd_noalloc.cu"):
         src = os.path.join(CSRC, f)
         obj = os.path.join(BUILD, f + ".o")
         cmd = [NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-v",

@@ -70,7 +70,7 @@ __device__ __forceinline__ float rcp_approx(float y)
 
 // Exact inverse by integer-only extended Euclid (64-bit division); the fallback that
 // runs only if the fast routine's self-check ever fails.
-__device__ __noinline__ uint32_t inv_mod_slow(uint32_t x, uint32_t q)
+static __device__ __noinline__ uint32_t inv_mod_slow(uint32_t x, uint32_t q)
 {
   int64_t r0 = q, r1 = x, s0 = 0, s1 = 1;
   while (r1 != 0) {

@@ -1,0 +1,271 @@
+// mgcd_pair.cuh -- the per-pair gcd body shared by the kernels (CTA scope or cooperative
+// grid): reductions, residues, the reduction loop, replay and recovery.
+// See mgcd_kernels.cu for the stage overview.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "mgcd_device.cuh"
+#include "mgcd_internal.h"
+
+namespace mgcd {
+
+constexpr int CHUNK = 1024;  // operand limbs staged per residue pass
+
+struct RedSmem {
+  unsigned long long key[2][32];  // per-warp minima, double-buffered by parity
+  unsigned long long bcast;       // grid mode: the grid-wide result
+  uint32_t bad;                   // grid mode: a bounded wait expired
+};
+
+static __device__ __forceinline__ unsigned long long globaltimer_ns()
+{
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+static __device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p)
+{
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+static __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p)
+{
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Lexicographic (hi, lo) minimum over the CTA; every thread gets the result.
+// One __syncthreads; the two slot buffers alternate so the next call cannot overwrite
+// slots still being read.
+template <int T>
+__device__ __forceinline__ void block_min_key(uint32_t& hi, uint32_t& lo, RedSmem& rs, uint32_t& parity)
+{
+  constexpr int NW = T / 32;
+  warp_min_key(hi, lo);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) rs.key[parity][w] = ((unsigned long long)hi << 32) | lo;
+  __syncthreads();
+  const unsigned long long k = (lane < NW) ? rs.key[parity][lane] : ~0ull;
+  hi = (uint32_t)(k >> 32);
+  lo = (uint32_t)k;
+  warp_min_key(hi, lo);
+  parity ^= 1u;
+}
+
+// Minimum over the CTA and, in grid mode, over all CTAs of the cooperative grid.
+// Grid exchange: thread 0 of every CTA folds its minimum into slot[epoch % 3] with an
+// atomic min, then arrives on a monotonic counter and waits (bounded by timeout_ns) until
+// all CTAs of this epoch arrived.  CTA 0 clears the slot of epoch + 1 before arriving:
+// every CTA has finished reading that slot (epoch - 2) once CTA 0 is past epoch - 1.
+// Returns false if the wait expired (the grid then unwinds; the host sees ST_TIMEOUT).
+template <int T, bool GRID>
+__device__ __forceinline__ bool reduce_min(uint32_t& hi, uint32_t& lo, RedSmem& rs, uint32_t& parity,
+                                           GridSync* gs, uint32_t& epoch)
+{
+  block_min_key<T>(hi, lo, rs, parity);
+  if constexpr (!GRID) {
+    return true;
+  } else {
+    if (threadIdx.x == 0) {
+      const uint32_t s = epoch % 3u;
+      atomicMin(&gs->slot[s], ((unsigned long long)hi << 32) | lo);
+      if (blockIdx.x == 0) gs->slot[(epoch + 1u) % 3u] = ~0ull;
+      __threadfence();
+      atomicAdd(&gs->arrive, 1u);
+      const unsigned int target = (epoch + 1u) * gridDim.x;
+      const unsigned long long t0 = globaltimer_ns();
+      uint32_t bad = 0;
+      while (ld_acquire_u32(&gs->arrive) < target) {
+        if (*(volatile unsigned int*)&gs->error) { bad = 1; break; }
+        if (globaltimer_ns() - t0 > gs->timeout_ns) { atomicExch(&gs->error, 1u); bad = 1; break; }
+      }
+      rs.bcast = bad ? ~0ull : ld_relaxed_u64(&gs->slot[s]);
+      rs.bad = bad;
+    }
+    __syncthreads();
+    const unsigned long long k = rs.bcast;
+    const bool ok = rs.bad == 0;
+    hi = (uint32_t)(k >> 32);
+    lo = (uint32_t)k;
+    epoch += 1u;
+    return ok;
+  }
+}
+
+// x mod q_j for the nloc moduli mods[0..nloc), into acc[] (shared).  Limbs are staged
+// most-significant tile first; Horner in Montgomery form keeps z = y * 2^-32 where y is the
+// residue of the limbs consumed so far: z' = REDC(z * (2^64 mod q) + limb).
+template <int T>
+__device__ void residues(const uint32_t* __restrict__ x, uint32_t n, const ModConst* __restrict__ mods,
+                         uint32_t nloc, uint32_t* __restrict__ acc, uint32_t* __restrict__ chunk)
+{
+  for (uint32_t j = threadIdx.x; j < nloc; j += T) acc[j] = 0u;
+  for (int hi = (int)n; hi > 0; hi -= CHUNK) {
+    const int lo = hi > CHUNK ? hi - CHUNK : 0;
+    __syncthreads();
+    for (int i = lo + (int)threadIdx.x; i < hi; i += T) chunk[i - lo] = __ldg(x + i);
+    __syncthreads();
+    const int len = hi - lo;
+    for (uint32_t j = threadIdx.x; j < nloc; j += T) {
+      const ModConst c = mods[j];
+      uint32_t z = acc[j];
+      for (int i = len - 1; i >= 0; --i) z = redc((uint64_t)z * c.r2 + chunk[i], c.q, c.qinv);
+      acc[j] = z;
+    }
+  }
+  __syncthreads();
+  for (uint32_t j = threadIdx.x; j < nloc; j += T) {
+    const ModConst c = mods[j];
+    acc[j] = redc((uint64_t)acc[j] * c.r2, c.q, c.qinv);
+  }
+  __syncthreads();
+}
+
+// The whole gcd of one pair by this CTA (GRID = false) or by the cooperative grid, the
+// calling CTA owning global moduli [j0, j0 + nloc).
+//   st, acc2   shared arrays of nloc words; chunk: CHUNK words
+//   u0g, v0g   this CTA's initial residues (global scratch, nloc words each)
+//   hist       (p, b) history, one entry per reduction iteration (global scratch, nq entries)
+template <int T, bool GRID>
+__device__ void run_pair(const uint32_t* __restrict__ limbs, const PairDesc& d, const ModConst* __restrict__ mods,
+                         int L, uint32_t j0, uint32_t nloc, uint32_t* st, uint32_t* acc2, uint32_t* chunk,
+                         RedSmem& rs, uint32_t* u0g, uint32_t* v0g, int2* hist, GridSync* gs,
+                         mgcd_pair* digits, uint32_t* count, uint32_t* iters_out, int32_t* status)
+{
+  const bool writer = threadIdx.x == 0 && (!GRID || blockIdx.x == 0);
+  const ModConst* __restrict__ my = mods + j0;
+  uint32_t parity = 0, epoch = 0;
+
+  // ---- MGCD2: residues
+  residues<T>(limbs + d.u_off, d.u_len, my, nloc, st, chunk);
+  residues<T>(limbs + d.v_off, d.v_len, my, nloc, acc2, chunk);
+
+  uint32_t kh = 0xFFFFFFFFu, kl = 0xFFFFFFFFu;
+  for (uint32_t j = threadIdx.x; j < nloc; j += T) {
+    const ModConst c = my[j];
+    const uint32_t u = st[j], v = acc2[j];
+    u0g[j] = u;
+    v0g[j] = v;
+    const uint32_t t = t_init(u, v, c.q, c.qinv);
+    st[j] = t;
+    uint32_t h, l;
+    t_key(t, c.q, h, l);
+    if (key_less(h, l, kh, kl)) { kh = h; kl = l; }
+  }
+  if (!reduce_min<T, GRID>(kh, kl, rs, parity, gs, epoch)) {
+    if (writer) *status = ST_TIMEOUT;
+    return;
+  }
+  uint32_t p;
+  int32_t b;
+  key_pair(kh, kl, p, b);
+
+  // ---- MGCD3: reduction loop (GmpCudaDevice-getGcdKernel.cu:365-402)
+  int remaining = (int)d.nq;
+  int ubits = ((int)d.u_len + 1) * 32, vbits = ((int)d.v_len + 1) * 32;
+  uint32_t iters = 0;
+  while (b != MOD_INFINITY) {
+    if (writer) hist[iters] = make_int2((int)p, b);
+    ++iters;
+    kh = 0xFFFFFFFFu;
+    kl = 0xFFFFFFFFu;
+    for (uint32_t j = threadIdx.x; j < nloc; j += T) {
+      const ModConst c = my[j];
+      const uint32_t t = t_update(st[j], c.q, c.qinv, p, b);
+      st[j] = t;
+      uint32_t h, l;
+      t_key(t, c.q, h, l);
+      if (key_less(h, l, kh, kl)) { kh = h; kl = l; }
+    }
+    remaining -= 1;
+    const uint32_t absb = b < 0 ? 0u - (uint32_t)b : (uint32_t)b;
+    const int tbits = ubits - (L - 1) + __ffs((int)absb);
+    ubits = vbits;
+    vbits = tbits;
+    if (remaining * (L - 2) <= ubits) {
+      if (writer) { *status = ST_REDUX; *count = 0; }
+      return;
+    }
+    if (!reduce_min<T, GRID>(kh, kl, rs, parity, gs, epoch)) {
+      if (writer) *status = ST_TIMEOUT;
+      return;
+    }
+    key_pair(kh, kl, p, b);
+  }
+  if (writer) *iters_out = iters;
+  if constexpr (GRID) __threadfence();
+  __syncthreads();
+
+  // ---- replay: u mod q of the surviving moduli from (u0, v0) and the (p, b) history.
+  // Invariant (U, V) = s * (u_i, v_i) mod q; each step (U, V, s) <- (V p, U - b V, s p) / R.
+  for (uint32_t j = threadIdx.x; j < nloc; j += T) {
+    if (st[j] == T_RETIRED) { st[j] = U_RETIRED; continue; }
+    const ModConst c = my[j];
+    const uint32_t q = c.q, qi = c.qinv;
+    uint32_t U = u0g[j], V = v0g[j], s = 1u;
+    for (uint32_t i = 0; i < iters; ++i) {
+      const int2 h = hist[i];
+      const uint32_t pp = (uint32_t)h.x;
+      const uint32_t pm = pp > q ? pp - q : pp;
+      const uint32_t bn = from_signed(-h.y, q);                 // -b mod q
+      const uint32_t U2 = mont_mul(V, pm, q, qi);
+      const uint32_t V2 = redc((uint64_t)bn * V + U, q, qi);
+      s = mont_mul(s, pm, q, qi);
+      U = U2;
+      V = V2;
+    }
+    st[j] = mont_mul(U, inv_mod(redc((uint64_t)s, q, qi), q, qi), q, qi);   // U / s
+  }
+
+  // ---- MGCD4: recovery (GmpCudaDevice-getGcdKernel.cu:404-443)
+  kh = 0xFFFFFFFFu;
+  kl = 0u;
+  for (uint32_t j = threadIdx.x; j < nloc; j += T) {
+    const uint32_t u = st[j];
+    if (u != U_RETIRED && u != 0u) { kh = j0 + j; kl = (uint32_t)to_signed(u, my[j].q); break; }
+  }
+  if (!reduce_min<T, GRID>(kh, kl, rs, parity, gs, epoch)) {
+    if (writer) *status = ST_TIMEOUT;
+    return;
+  }
+  uint32_t ndig = 0;
+  int32_t g;
+  if (kh == 0xFFFFFFFFu) { p = mods[0].q; g = 0; } else { p = mods[kh].q; g = (int32_t)kl; }
+  do {
+    kh = 0xFFFFFFFFu;
+    kl = 0u;
+    for (uint32_t j = threadIdx.x; j < nloc; j += T) {
+      uint32_t u = st[j];
+      if (u == U_RETIRED) continue;
+      const ModConst c = my[j];
+      const uint32_t q = c.q, qi = c.qinv;
+      if (q == p) { st[j] = U_RETIRED; continue; }
+      const uint32_t pm = p > q ? p - q : p;
+      u = mont_mul(mod_sub(u, from_signed(g, q), q), inv_mod(redc((uint64_t)pm, q, qi), q, qi), q, qi);
+      st[j] = u;
+      if (u != 0u && kh == 0xFFFFFFFFu) { kh = j0 + j; kl = (uint32_t)to_signed(u, q); }
+    }
+    if (writer) digits[d.out_off + ndig] = mgcd_pair{p, g};
+    ++ndig;
+    remaining -= 1;
+    if (remaining <= 0) break;
+    if (!reduce_min<T, GRID>(kh, kl, rs, parity, gs, epoch)) {
+      if (writer) *status = ST_TIMEOUT;
+      return;
+    }
+    if (kh == 0xFFFFFFFFu) { p = mods[0].q; g = 0; } else { p = mods[kh].q; g = (int32_t)kl; }
+  } while (g != 0);
+  if (writer) {
+    *status = (g != 0) ? ST_RECOVERY : ST_OK;
+    *count = ndig;
+  }
+  __syncthreads();
+}
+
+
+}  // namespace mgcd

@@ -119,6 +119,14 @@ int mgcd_batch_run(mgcd_context *ctx);
 int mgcd_batch_sync(mgcd_context *ctx);
 int mgcd_batch_download(mgcd_context *ctx, uint32_t *g, const uint64_t *g_off, const uint32_t *g_cap,
                         uint32_t *g_len, int32_t *status);
+/* Batches may use fewer moduli per pair than the reference's count (less work per
+   reduction iteration): scale in [0.5, 1], 1 = the reference's count (default).  Every
+   result is certified on the device (the surviving moduli must bound both operands); a pair
+   that cannot be certified is rerun with the reference's count, so results do not change.
+   Single-pair calls always use the reference's count. */
+int mgcd_set_nq_scale(mgcd_context *ctx, float scale);
+/* Pairs the last run had to rerun with the reference's moduli count. */
+int mgcd_batch_retried(const mgcd_context *ctx, int *pairs);
 /* Kernel launches the last mgcd_batch_run issued. */
 int mgcd_batch_launches(const mgcd_context *ctx, int *launches);
 /* Device time of the last mgcd_batch_run (CUDA events on the context's stream around

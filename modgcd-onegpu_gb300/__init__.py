@@ -59,6 +59,8 @@ SIGNATURES = {
     "mgcd_batch_transfer_bytes": (_c.c_int, [_P, _c.POINTER(_c.c_uint64), _c.POINTER(_c.c_uint64)]),
     "mgcd_int_peak": (_c.c_int, [_P, _c.POINTER(_c.c_double)]),
     "mgcd_gcd_digits_noalloc": (_c.c_int, [_P, _c.c_size_t, _c.c_size_t, _P, _c.c_size_t, _P, _P, _P]),
+    "mgcd_set_nq_scale": (_c.c_int, [_P, _c.c_float]),
+    "mgcd_batch_retried": (_c.c_int, [_P, _c.POINTER(_c.c_int)]),
 }
 
 _lib = None
@@ -264,6 +266,15 @@ class Device:
         st = np.zeros(n, dtype=np.int32)
         self._lib.mgcd_batch_download(self._h, g.ctypes.data, _ptr(g_off), _ptr(g_cap), _ptr(g_len), _ptr(st))
         return g, g_off, g_len, st
+
+    def set_nq_scale(self, scale):
+        """Fraction of the reference moduli count batches use (results are certified)."""
+        _check(self._lib.mgcd_set_nq_scale(self._h, float(scale)))
+
+    def batch_retried(self):
+        n = ctypes.c_int()
+        _check(self._lib.mgcd_batch_retried(self._h, ctypes.byref(n)))
+        return n.value
 
     def batch_launches(self):
         n = ctypes.c_int()

@@ -15,6 +15,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <thread>
@@ -99,6 +100,7 @@ int to_status(int32_t st)
     case ST_REDUX: return MGCD_ERR_REDUX;
     case ST_RECOVERY: return MGCD_ERR_RECOVERY;
     case ST_TIMEOUT: return MGCD_ERR_TIMEOUT;
+    case ST_INSUFFICIENT: return MGCD_ERR_REDUX;
     default: return MGCD_ERR_KERNEL;
   }
 }
@@ -144,6 +146,11 @@ struct mgcd_context {
   int launches = 0;
   bool ran = false;
   double work[4] = {0, 0, 0, 0};
+  float nq_scale = 1.0f;               // batches: fraction of the reference moduli count
+  std::vector<uint32_t> ref_nq, eff_nq; // per GPU pair: reference count, count of the final run
+  int retried = 0;
+  bool synced = false;
+  DevBuf d_retry;
   // timing: the whole run on `stream`, and each bucket launch on its stream
   cudaEvent_t t_run0 = nullptr, t_run1 = nullptr, t_b0[NSTREAMS] = {}, t_b1[NSTREAMS] = {};
   uint64_t h2d_bytes = 0, d2h_bytes = 0;
@@ -255,7 +262,7 @@ int mgcd_destroy(mgcd_context* c)
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (DevBuf* b : {&c->mods, &c->d_limbs, &c->d_pairs, &c->d_order, &c->d_digits, &c->d_count, &c->d_iters,
-                    &c->d_status, &c->d_queue, &c->d_scratch, &c->d_gsync})
+                    &c->d_status, &c->d_queue, &c->d_scratch, &c->d_gsync, &c->d_retry})
     b->release();
   for (HostBuf* b : {&c->h_count, &c->h_iters, &c->h_status, &c->h_digits, &c->h_gsync}) b->release();
   for (int i = 0; i < NSTREAMS; ++i) {
@@ -295,6 +302,9 @@ int mgcd_moduli(const mgcd_context* c, uint32_t* out, size_t n)
 
 // ------------------------------------------------------------------------- batch ----
 
+static int schedule(mgcd_context* c, const std::vector<PairDesc>& descs, const std::vector<uint32_t>& subset,
+                    bool plain, std::vector<Bucket>& buckets, std::vector<uint32_t>& grid_pairs, size_t& scratch);
+
 static int plan_batch(mgcd_context* c, size_t np, const uint32_t* limbs, const uint64_t* u_off,
                       const uint32_t* u_len, const uint64_t* v_off, const uint32_t* v_len, bool plain)
 {
@@ -307,6 +317,7 @@ static int plan_batch(mgcd_context* c, size_t np, const uint32_t* limbs, const u
   c->slot.assign(np, -1);
   c->trivial.assign(np, {});
   c->descs.clear();
+  c->ref_nq.clear();
   c->grid_pairs.clear();
   c->buckets.clear();
   uint64_t limb_end = 0;
@@ -330,63 +341,34 @@ static int plan_batch(mgcd_context* c, size_t np, const uint32_t* limbs, const u
     }
     const uint32_t top = limbs[d.u_off + d.u_len - 1];
     const size_t ubits = (size_t)(d.u_len - 1) * 32 + (32 - __builtin_clz(top));
-    const int nq = moduli_needed(c->L, ubits);
-    if ((size_t)nq > c->moduli.size()) {
+    const int ref_nq = moduli_needed(c->L, ubits);
+    if ((size_t)ref_nq > c->moduli.size()) {
       c->status[i] = MGCD_ERR_NOT_ENOUGH_MODULI;
       continue;
     }
+    // Batches may use fewer moduli than the reference formula (less work per iteration);
+    // a pair whose result cannot then be certified is rerun with the reference count.
+    int nq = ref_nq;
+    if (!plain && c->nq_scale < 1.0f)
+      nq = std::min(ref_nq, std::max(256, ((int)std::ceil(c->nq_scale * ref_nq) + 255) / 256 * 256));
     d.nq = (uint32_t)nq;
     d.out_off = out_off;
-    out_off += (uint32_t)nq + 1;
+    out_off += (uint32_t)ref_nq + 1;
     c->slot[i] = (int)c->descs.size();
     c->descs.push_back(d);
+    c->ref_nq.push_back((uint32_t)ref_nq);
   }
   c->ndig = out_off;
   const size_t ng = c->descs.size();
-
-  // Partition: CTA buckets (by CTA size) and cooperative-grid pairs.
-  const uint32_t plain_cta_max = (uint32_t)env_int("MGCD_PLAIN_CTA_MAX", 2048);
-  std::vector<uint32_t> byb[NSTREAMS];
-  for (uint32_t k = 0; k < ng; ++k) {
-    const uint32_t nq = c->descs[k].nq;
-    if (plain) {
-      if (nq <= plain_cta_max) byb[2].push_back(k); else c->grid_pairs.push_back(k);
-    } else if (nq > CTA_MAX_NQ) {
-      c->grid_pairs.push_back(k);
-    } else {
-      byb[nq <= 1024 ? 0 : nq <= 4096 ? 1 : 2].push_back(k);
-    }
-  }
-  static const int kThreads[NSTREAMS] = {256, 512, 1024};
   c->order.clear();
+  std::vector<uint32_t> all(ng);
+  for (uint32_t k = 0; k < ng; ++k) all[k] = k;
   size_t scratch = 0;
-  for (int b = NSTREAMS - 1; b >= 0; --b) {  // largest CTA size first: its pairs are the longest
-    auto& v = byb[b];
-    if (v.empty()) continue;
-    std::sort(v.begin(), v.end(), [&](uint32_t x, uint32_t y) {
-      const PairDesc &a = c->descs[x], &bb = c->descs[y];
-      if (a.nq != bb.nq) return a.nq > bb.nq;
-      return a.u_len + a.v_len > bb.u_len + bb.v_len;
-    });
-    Bucket bk;
-    bk.threads = kThreads[b];
-    bk.first = (uint32_t)c->order.size();
-    bk.n = (uint32_t)v.size();
-    bk.nq_max = c->descs[v[0]].nq;
-    bk.smem = batch_smem_bytes(bk.threads, bk.nq_max);
-    int bps = 0;
-    if (batch_max_blocks_per_sm(bk.threads, bk.smem, &bps) != cudaSuccess || bps < 1) return MGCD_ERR_GRID;
-    bk.grid = (int)std::min<size_t>(v.size(), (size_t)c->sms * bps);
-    bk.scratch_off = scratch;
-    scratch += (size_t)bk.grid * 4 * bk.nq_max;
-    c->order.insert(c->order.end(), v.begin(), v.end());
-    c->buckets.push_back(bk);
-  }
-  uint32_t grid_nq_max = 0;
-  for (uint32_t k : c->grid_pairs) grid_nq_max = std::max(grid_nq_max, c->descs[k].nq);
-  c->grid_scratch_off = scratch;
-  scratch += 4 * (size_t)grid_nq_max;
+  int rc = schedule(c, c->descs, all, plain, c->buckets, c->grid_pairs, scratch);
+  if (rc != MGCD_OK) return rc;
   c->scratch_words = scratch;
+  c->eff_nq.clear();
+  for (const PairDesc& d : c->descs) c->eff_nq.push_back(d.nq);
 
   // Device buffers and upload.
   CK(c->d_limbs.grow(std::max<uint64_t>(limb_end, 1) * sizeof(uint32_t)));
@@ -396,7 +378,7 @@ static int plan_batch(mgcd_context* c, size_t np, const uint32_t* limbs, const u
   CK(c->d_count.grow(std::max<size_t>(ng, 1) * sizeof(uint32_t)));
   CK(c->d_iters.grow(std::max<size_t>(ng, 1) * sizeof(uint32_t)));
   CK(c->d_status.grow(std::max<size_t>(ng, 1) * sizeof(int32_t)));
-  CK(c->d_queue.grow(NSTREAMS * sizeof(uint32_t)));
+  CK(c->d_queue.grow(2 * NSTREAMS * sizeof(uint32_t)));
   CK(c->d_scratch.grow(std::max<size_t>(scratch, 1) * sizeof(uint32_t)));
   CK(c->d_gsync.grow(sizeof(GridSync)));
   CK(c->h_gsync.grow(sizeof(GridSync)));
@@ -411,36 +393,86 @@ static int plan_batch(mgcd_context* c, size_t np, const uint32_t* limbs, const u
   return MGCD_OK;
 }
 
+// Groups the pairs `subset` (indices into descs) into CTA-size buckets and cooperative-grid
+// pairs; appends the processing order to c->order and returns the scratch words needed.
+static int schedule(mgcd_context* c, const std::vector<PairDesc>& descs, const std::vector<uint32_t>& subset,
+                    bool plain, std::vector<Bucket>& buckets, std::vector<uint32_t>& grid_pairs, size_t& scratch)
+{
+  buckets.clear();
+  grid_pairs.clear();
+  const uint32_t plain_cta_max = (uint32_t)env_int("MGCD_PLAIN_CTA_MAX", 2048);
+  std::vector<uint32_t> byb[NSTREAMS];
+  for (uint32_t k : subset) {
+    const uint32_t nq = descs[k].nq;
+    if (plain) {
+      if (nq <= plain_cta_max) byb[2].push_back(k); else grid_pairs.push_back(k);
+    } else if (nq > CTA_MAX_NQ) {
+      grid_pairs.push_back(k);
+    } else {
+      byb[nq <= 1024 ? 0 : nq <= 4096 ? 1 : 2].push_back(k);
+    }
+  }
+  static const int kThreads[NSTREAMS] = {256, 512, 1024};
+  for (int b = NSTREAMS - 1; b >= 0; --b) {  // largest CTA size first: its pairs are the longest
+    auto& v = byb[b];
+    if (v.empty()) continue;
+    std::sort(v.begin(), v.end(), [&](uint32_t x, uint32_t y) {
+      const PairDesc &a = descs[x], &bb = descs[y];
+      if (a.nq != bb.nq) return a.nq > bb.nq;
+      return a.u_len + a.v_len > bb.u_len + bb.v_len;
+    });
+    Bucket bk;
+    bk.threads = kThreads[b];
+    bk.first = (uint32_t)c->order.size();
+    bk.n = (uint32_t)v.size();
+    bk.nq_max = descs[v[0]].nq;
+    bk.smem = batch_smem_bytes(bk.threads, bk.nq_max);
+    int bps = 0;
+    if (batch_max_blocks_per_sm(bk.threads, bk.smem, &bps) != cudaSuccess || bps < 1) return MGCD_ERR_GRID;
+    bk.grid = (int)std::min<size_t>(v.size(), (size_t)c->sms * bps);
+    bk.scratch_off = scratch;
+    scratch += (size_t)bk.grid * 4 * bk.nq_max;
+    c->order.insert(c->order.end(), v.begin(), v.end());
+    buckets.push_back(bk);
+  }
+  uint32_t grid_nq_max = 0;
+  for (uint32_t k : grid_pairs) grid_nq_max = std::max(grid_nq_max, descs[k].nq);
+  c->grid_scratch_off = scratch;
+  scratch += 4 * (size_t)grid_nq_max;
+  return MGCD_OK;
+}
+
 int mgcd_batch_upload(mgcd_context* c, size_t np, const uint32_t* limbs, const uint64_t* u_off,
                       const uint32_t* u_len, const uint64_t* v_off, const uint32_t* v_len)
 {
   return plan_batch(c, np, limbs, u_off, u_len, v_off, v_len, false);
 }
 
-static int run_plan(mgcd_context* c)
+int mgcd_set_nq_scale(mgcd_context* c, float scale)
 {
-  if (!c) return MGCD_ERR_INVALID_ARG;
-  CK(cudaSetDevice(c->device));
-  c->launches = 0;
-  const size_t ng = c->descs.size();
-  if (ng == 0) {
-    c->ran = true;
-    return MGCD_OK;
-  }
-  CK(cudaEventRecord(c->t_run0, c->stream));
-  CK(cudaMemsetAsync(c->d_queue.p, 0, NSTREAMS * sizeof(uint32_t), c->stream));
-  CK(cudaMemsetAsync(c->d_status.p, 0xFF, ng * sizeof(int32_t), c->stream));
+  if (!c || !(scale >= 0.5f && scale <= 1.0f)) return MGCD_ERR_INVALID_ARG;
+  c->nq_scale = scale;
+  return MGCD_OK;
+}
+
+// Launches the buckets (one stream each, joined back into c->stream) and then the
+// cooperative-grid pairs.  `pairs` is the descriptor array on the device, `queue_base`
+// the first of the bucket work counters (zeroed here).
+static int launch_set(mgcd_context* c, const std::vector<Bucket>& buckets, const std::vector<uint32_t>& grid_pairs,
+                      const std::vector<PairDesc>& descs, PairDesc* pairs, uint32_t* queue_base, bool time_buckets)
+{
+  CK(cudaMemsetAsync(queue_base, 0, NSTREAMS * sizeof(uint32_t), c->stream));
   CK(cudaEventRecord(c->ev_start, c->stream));
-  for (size_t b = 0; b < c->buckets.size(); ++b) {
-    const Bucket& bk = c->buckets[b];
+  for (size_t b = 0; b < buckets.size(); ++b) {
+    const Bucket& bk = buckets[b];
     BatchArgs a;
     a.limbs = c->d_limbs.as<uint32_t>();
-    a.pairs = c->d_pairs.as<PairDesc>();
+    a.pairs = pairs;
     a.order = c->d_order.as<uint32_t>() + bk.first;
     a.npairs = bk.n;
     a.mods = c->mods.as<ModConst>();
     a.L = c->L;
-    a.queue = c->d_queue.as<uint32_t>() + b;
+    a.queue = queue_base + b;
     a.scratch = c->d_scratch.as<uint32_t>() + bk.scratch_off;
     a.scratch_words = 4 * (size_t)bk.nq_max;
     a.nq_max = bk.nq_max;
@@ -449,23 +481,23 @@ static int run_plan(mgcd_context* c)
     a.iters = c->d_iters.as<uint32_t>();
     a.status = c->d_status.as<int32_t>();
     CK(cudaStreamWaitEvent(c->bstream[b], c->ev_start, 0));
-    CK(cudaEventRecord(c->t_b0[b], c->bstream[b]));
+    if (time_buckets) CK(cudaEventRecord(c->t_b0[b], c->bstream[b]));
     CK(launch_batch(a, bk.threads, bk.grid, bk.smem, c->bstream[b]));
-    CK(cudaEventRecord(c->t_b1[b], c->bstream[b]));
+    if (time_buckets) CK(cudaEventRecord(c->t_b1[b], c->bstream[b]));
     CK(cudaEventRecord(c->ev_b[b], c->bstream[b]));
     ++c->launches;
   }
-  for (size_t b = 0; b < c->buckets.size(); ++b) CK(cudaStreamWaitEvent(c->stream, c->ev_b[b], 0));
+  for (size_t b = 0; b < buckets.size(); ++b) CK(cudaStreamWaitEvent(c->stream, c->ev_b[b], 0));
 
-  if (!c->grid_pairs.empty()) {
+  if (!grid_pairs.empty()) {
     GridSync* hs = c->h_gsync.as<GridSync>();
     hs->slot[0] = hs->slot[1] = hs->slot[2] = ~0ull;
     hs->arrive = 0;
     hs->error = 0;
     hs->timeout_ns = (unsigned long long)env_int("MGCD_WAIT_TIMEOUT_MS", 2000) * 1000000ull;
     const uint32_t per_default = (uint32_t)env_int("MGCD_GRID_PER_CTA", GRID_THREADS);
-    for (uint32_t k : c->grid_pairs) {
-      const PairDesc& d = c->descs[k];
+    for (uint32_t k : grid_pairs) {
+      const PairDesc& d = descs[k];
       uint32_t per = std::max<uint32_t>(per_default, 32);
       int bps = 0;
       if (grid_max_blocks_per_sm(grid_smem_bytes(per), &bps) != cudaSuccess || bps < 1) return MGCD_ERR_GRID;
@@ -495,8 +527,84 @@ static int run_plan(mgcd_context* c)
       ++c->launches;
     }
   }
+  return MGCD_OK;
+}
+
+static int run_plan(mgcd_context* c)
+{
+  if (!c) return MGCD_ERR_INVALID_ARG;
+  CK(cudaSetDevice(c->device));
+  c->launches = 0;
+  c->retried = 0;
+  const size_t ng = c->descs.size();
+  if (ng == 0) {
+    c->ran = true;
+    return MGCD_OK;
+  }
+  CK(cudaEventRecord(c->t_run0, c->stream));
+  CK(cudaMemsetAsync(c->d_status.p, 0xFF, ng * sizeof(int32_t), c->stream));
+  int rc = launch_set(c, c->buckets, c->grid_pairs, c->descs, c->d_pairs.as<PairDesc>(), c->d_queue.as<uint32_t>(),
+                      true);
+  if (rc != MGCD_OK) return rc;
   CK(cudaEventRecord(c->t_run1, c->stream));
   c->ran = true;
+  c->synced = false;
+  return MGCD_OK;
+}
+
+// Waits for the run; pairs that ran with fewer moduli than the reference count and could
+// not be certified are rerun once with the reference count (same digit slots).
+static int sync_plan(mgcd_context* c)
+{
+  if (!c || !c->ran) return MGCD_ERR_INVALID_ARG;
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(c->stream));
+  if (c->synced) return MGCD_OK;
+  c->synced = true;
+  const size_t ng = c->descs.size();
+  bool scaled = false;
+  for (size_t k = 0; k < ng && !scaled; ++k) scaled = c->descs[k].nq < c->ref_nq[k];
+  if (!scaled) return MGCD_OK;
+  CK(c->h_status.grow(ng * sizeof(int32_t)));
+  CK(cudaMemcpy(c->h_status.p, c->d_status.p, ng * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  const int32_t* st = c->h_status.as<int32_t>();
+  std::vector<uint32_t> redo;
+  for (uint32_t k = 0; k < ng; ++k)
+    if (st[k] == ST_INSUFFICIENT && c->descs[k].nq < c->ref_nq[k]) redo.push_back(k);
+  if (redo.empty()) return MGCD_OK;
+  std::vector<PairDesc> rd = c->descs;
+  for (uint32_t k : redo) rd[k].nq = c->ref_nq[k];
+  const size_t main_order = c->order.size();
+  std::vector<Bucket> bks;
+  std::vector<uint32_t> gp;
+  size_t scratch = 0;
+  const size_t keep_grid_off = c->grid_scratch_off;
+  int rc = schedule(c, rd, redo, false, bks, gp, scratch);
+  if (rc != MGCD_OK) return rc;
+  // device buffers: retry descriptors after the main ones, retry order after the main order
+  CK(c->d_retry.grow(ng * sizeof(PairDesc)));
+  if (c->order.size() * sizeof(uint32_t) > c->d_order.bytes) {
+    // keep the main order: grow by copying
+    DevBuf nb;
+    CK(nb.grow(c->order.size() * sizeof(uint32_t)));
+    CK(cudaMemcpy(nb.p, c->d_order.p, main_order * sizeof(uint32_t), cudaMemcpyDeviceToDevice));
+    c->d_order.release();
+    c->d_order = nb;
+  }
+  if (scratch > c->d_scratch.bytes / sizeof(uint32_t)) {
+    c->d_scratch.release();
+    CK(c->d_scratch.grow(scratch * sizeof(uint32_t)));
+  }
+  CK(cudaMemcpyAsync(c->d_retry.p, rd.data(), ng * sizeof(PairDesc), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->d_order.as<uint32_t>() + main_order, c->order.data() + main_order,
+                     (c->order.size() - main_order) * sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream));
+  rc = launch_set(c, bks, gp, rd, c->d_retry.as<PairDesc>(), c->d_queue.as<uint32_t>() + NSTREAMS, false);
+  c->order.resize(main_order);               // the plan itself is unchanged for later runs
+  c->grid_scratch_off = keep_grid_off;
+  if (rc != MGCD_OK) return rc;
+  CK(cudaEventRecord(c->t_run1, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  c->retried = (int)redo.size();
   return MGCD_OK;
 }
 
@@ -558,11 +666,12 @@ int mgcd_int_peak(mgcd_context* c, double* ops)
 
 int mgcd_batch_run(mgcd_context* c) { return run_plan(c); }
 
-int mgcd_batch_sync(mgcd_context* c)
+int mgcd_batch_sync(mgcd_context* c) { return sync_plan(c); }
+
+int mgcd_batch_retried(const mgcd_context* c, int* pairs)
 {
-  if (!c) return MGCD_ERR_INVALID_ARG;
-  CK(cudaSetDevice(c->device));
-  CK(cudaStreamSynchronize(c->stream));
+  if (!c || !pairs) return MGCD_ERR_INVALID_ARG;
+  *pairs = c->retried;
   return MGCD_OK;
 }
 
@@ -599,7 +708,7 @@ static int fetch(mgcd_context* c)
     R += (double)d.nq * (d.u_len + d.v_len);
     B += 4.0 * (d.u_len + d.v_len);
     if (st[k] != ST_OK) continue;
-    const double I = it[k], K = cnt[k], N = d.nq;
+    const double I = it[k], K = cnt[k], N = c->eff_nq[k];
     E += I * N - I * (I + 1) / 2;
     M += K * (N - I) - K * (K + 1) / 2;
   }
@@ -665,7 +774,9 @@ int mgcd_batch_download(mgcd_context* c, uint32_t* g, const uint64_t* g_off, con
                         uint32_t* g_len, int32_t* status)
 {
   if (!c || !c->ran || (c->np && (!g || !g_off || !g_cap || !g_len || !status))) return MGCD_ERR_INVALID_ARG;
-  int rc = fetch(c);
+  int rc = sync_plan(c);
+  if (rc != MGCD_OK) return rc;
+  rc = fetch(c);
   if (rc != MGCD_OK) return rc;
   return convert_all(c, g, g_off, g_cap, g_len, status);
 }
@@ -696,6 +807,8 @@ static int single(mgcd_context* c, const uint32_t* u, size_t uSz, const uint32_t
   int rc = plan_batch(c, 1, buf.data(), &uo, &ul, &vo, &vl, true);
   if (rc != MGCD_OK) return rc;
   rc = run_plan(c);
+  if (rc != MGCD_OK) return rc;
+  rc = sync_plan(c);
   if (rc != MGCD_OK) return rc;
   return fetch(c);
 }

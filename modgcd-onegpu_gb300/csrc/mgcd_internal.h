@@ -25,6 +25,7 @@ enum : int32_t {
   ST_REDUX = 1,      // ran out of moduli in the reduction loop
   ST_RECOVERY = 2,   // ran out of moduli in the recovery loop
   ST_TIMEOUT = 3,    // a bounded cross-CTA wait expired
+  ST_INSUFFICIENT = 4,  // result not certified: too few moduli survived the reduction loop
   ST_PENDING = -1
 };
 

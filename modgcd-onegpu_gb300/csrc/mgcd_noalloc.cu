@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(NA_THREADS) noalloc_kernel(const NaArgs a)
                               rs, u0, v0, hist, nullptr, a.digits, a.count, &iters, a.status);
   if (threadIdx.x == 0) {
     const int32_t s = *a.status;
-    *a.status = s == ST_OK ? MGCD_OK : s == ST_REDUX ? MGCD_ERR_REDUX
+    *a.status = s == ST_OK ? MGCD_OK : (s == ST_REDUX || s == ST_INSUFFICIENT) ? MGCD_ERR_REDUX
               : s == ST_RECOVERY ? MGCD_ERR_RECOVERY : MGCD_ERR_KERNEL;
   }
 }

@@ -16,6 +16,7 @@ struct RedSmem {
   unsigned long long key[2][32];  // per-warp minima, double-buffered by parity
   unsigned long long bcast;       // grid mode: the grid-wide result
   uint32_t bad;                   // grid mode: a bounded wait expired
+  uint32_t cert;                  // the result could not be certified (more moduli needed)
 };
 
 static __device__ __forceinline__ unsigned long long globaltimer_ns()
@@ -169,9 +170,28 @@ __device__ void run_pair(const uint32_t* __restrict__ limbs, const PairDesc& d, 
   int remaining = (int)d.nq;
   int ubits = ((int)d.u_len + 1) * 32, vbits = ((int)d.v_len + 1) * 32;
   uint32_t iters = 0;
+  // Certification bounds (thread 0 of each CTA; every CTA computes the same values):
+  // lu >= log2|u_i|, lv >= log2|v_i| with |v_{i+1}| <= (|u_i| + |b| |v_i|) / p.
+  double lu = 0.0, lv = 0.0;
+  if (threadIdx.x == 0) {
+    lu = (double)(((int)d.u_len - 1) * 32 + (32 - __clz(limbs[d.u_off + d.u_len - 1])));
+    lv = (double)(((int)d.v_len - 1) * 32 + (32 - __clz(limbs[d.v_off + d.v_len - 1])));
+  }
   while (b != MOD_INFINITY) {
     if (writer) hist[iters] = make_int2((int)p, b);
     ++iters;
+    if (threadIdx.x == 0) {
+      const uint32_t ab = b < 0 ? 0u - (uint32_t)b : (uint32_t)b;
+      double s = lu;
+      if (ab != 0u) {
+        const double y = lv + (double)log2f((float)ab);
+        const double m = y > lu ? y : lu, dd = y > lu ? y - lu : lu - y;
+        s = m + (dd < 40.0 ? (double)log2f(1.0f + exp2f(-(float)dd)) : 0.0);
+      }
+      const double lnew = s - (double)log2f((float)p) + 1e-4;
+      lu = lv;
+      lv = lnew;
+    }
     kh = 0xFFFFFFFFu;
     kl = 0xFFFFFFFFu;
     for (uint32_t j = threadIdx.x; j < nloc; j += T) {
@@ -198,8 +218,19 @@ __device__ void run_pair(const uint32_t* __restrict__ limbs, const PairDesc& d, 
     key_pair(kh, kl, p, b);
   }
   if (writer) *iters_out = iters;
+  // Certify the result: all surviving residues of v are 0, so v = 0 if the surviving
+  // moduli (each > 2^(L-1)) multiply to more than |v|; recovery is exact if they exceed
+  // 2|u| (symmetric digits).  Otherwise report that more moduli are needed.
+  if (threadIdx.x == 0) {
+    const double cap = (double)remaining * (double)(L - 1);
+    rs.cert = (cap > lu + 2.0 && cap > lv + 1.0) ? 0u : 1u;
+  }
   if constexpr (GRID) __threadfence();
   __syncthreads();
+  if (rs.cert) {
+    if (writer) { *status = ST_INSUFFICIENT; *count = 0; }
+    return;
+  }
 
   // ---- replay: u mod q of the surviving moduli from (u0, v0) and the (p, b) history.
   // Invariant (U, V) = s * (u_i, v_i) mod q; each step (U, V, s) <- (V p, U - b V, s p) / R.

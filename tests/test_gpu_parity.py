@@ -65,6 +65,21 @@ def test_batch_mixed_sizes(device):
     assert res == [math.gcd(u, v) for u, v in zip(us, vs)]
 
 
+@pytest.mark.parametrize("scale", [0.8, 0.5])
+def test_batch_fewer_moduli_certified(mgcd, scale):
+    """Batches with fewer moduli than the reference count: every result certified or rerun
+    with the reference count -- results stay exact.  At 0.5 many pairs need the rerun."""
+    wl = __import__("importlib").import_module("modgcd-onegpu_gb300.workloads")
+    us, vs, _ = wl.mixed_batch(200, seed=9, hi_bits=20000)
+    with mgcd.Device(0, 32) as dev:
+        dev.set_nq_scale(scale)
+        res = dev.gcd_batch(us, vs)
+        retried = dev.batch_retried()
+    assert res == [math.gcd(u, v) for u, v in zip(us, vs)]
+    if scale == 0.5:
+        assert retried > 0
+
+
 def test_edge_cases(device):
     rng = random.Random(13)
     x = rng.getrandbits(5000) | 1

@@ -125,6 +125,17 @@ int mgcd_batch_download(mgcd_context *ctx, uint32_t *g, const uint64_t *g_off, c
    that cannot be certified is rerun with the reference's count, so results do not change.
    Single-pair calls always use the reference's count. */
 int mgcd_set_nq_scale(mgcd_context *ctx, float scale);
+/* Launch configuration of one size class of the batched path: class 0 = pairs needing
+   <= 1,024 moduli, 1 = <= 4,096, 2 = larger (up to 16,384; beyond that a pair runs on a
+   cooperative grid).  threads: CTA size (256, 512, 1024); k: pairs one CTA runs in
+   lockstep, sharing one modular inverse per modulus and iteration (1, 2, or 4 with
+   threads <= 512); nq_scale as above.  The autotuner writes these. */
+int mgcd_set_size_class(mgcd_context *ctx, int cls, int threads, int k, float nq_scale);
+int mgcd_get_size_class(const mgcd_context *ctx, int cls, int *threads, int *k, float *nq_scale);
+/* Per kernel of the last run (i < number of size classes present, largest first): its
+   size class, pair count and device time (the time includes waiting for SMs that other
+   concurrently running classes hold). */
+int mgcd_batch_kernel_stats(const mgcd_context *ctx, int i, int *cls, int *pairs, float *ms);
 /* Pairs the last run had to rerun with the reference's moduli count. */
 int mgcd_batch_retried(const mgcd_context *ctx, int *pairs);
 /* Kernel launches the last mgcd_batch_run issued. */

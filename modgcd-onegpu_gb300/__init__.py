@@ -60,6 +60,11 @@ SIGNATURES = {
     "mgcd_int_peak": (_c.c_int, [_P, _c.POINTER(_c.c_double)]),
     "mgcd_gcd_digits_noalloc": (_c.c_int, [_P, _c.c_size_t, _c.c_size_t, _P, _c.c_size_t, _P, _P, _P]),
     "mgcd_set_nq_scale": (_c.c_int, [_P, _c.c_float]),
+    "mgcd_set_size_class": (_c.c_int, [_P, _c.c_int, _c.c_int, _c.c_int, _c.c_float]),
+    "mgcd_get_size_class": (_c.c_int, [_P, _c.c_int, _c.POINTER(_c.c_int), _c.POINTER(_c.c_int),
+                                       _c.POINTER(_c.c_float)]),
+    "mgcd_batch_kernel_stats": (_c.c_int, [_P, _c.c_int, _c.POINTER(_c.c_int), _c.POINTER(_c.c_int),
+                                           _c.POINTER(_c.c_float)]),
     "mgcd_batch_retried": (_c.c_int, [_P, _c.POINTER(_c.c_int)]),
 }
 
@@ -270,6 +275,26 @@ class Device:
     def set_nq_scale(self, scale):
         """Fraction of the reference moduli count batches use (results are certified)."""
         _check(self._lib.mgcd_set_nq_scale(self._h, float(scale)))
+
+    def set_size_class(self, cls, threads, k, nq_scale):
+        """Launch configuration of size class cls (0: <= 1024 moduli, 1: <= 4096, 2: larger)."""
+        _check(self._lib.mgcd_set_size_class(self._h, int(cls), int(threads), int(k), float(nq_scale)))
+
+    def get_size_class(self, cls):
+        t, k, s = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+        _check(self._lib.mgcd_get_size_class(self._h, int(cls), ctypes.byref(t), ctypes.byref(k), ctypes.byref(s)))
+        return t.value, k.value, s.value
+
+    def batch_kernel_stats(self):
+        """[(size class, pairs, ms)] of the last run's kernels."""
+        out = []
+        i = 0
+        while True:
+            c, n, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+            if self._lib.mgcd_batch_kernel_stats(self._h, i, ctypes.byref(c), ctypes.byref(n), ctypes.byref(ms)) != 0:
+                return out
+            out.append((c.value, n.value, ms.value))
+            i += 1
 
     def batch_retried(self):
         n = ctypes.c_int()

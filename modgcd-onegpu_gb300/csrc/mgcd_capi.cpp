@@ -77,7 +77,8 @@ struct HostBuf {
 };
 
 struct Bucket {
-  int threads;
+  int threads, k;      // CTA size, pairs per CTA in lockstep
+  int cls;             // size class
   uint32_t first, n, nq_max;
   int grid;
   size_t smem;
@@ -86,6 +87,7 @@ struct Bucket {
 
 constexpr int NSTREAMS = 3;
 constexpr uint32_t CTA_MAX_NQ = 16384;   // larger pairs go to the cooperative grid
+constexpr size_t INVTAB_N = 16384;        // moduli covered by the pairwise inverse table
 
 int env_int(const char* name, int dflt)
 {
@@ -104,6 +106,9 @@ int to_status(int32_t st)
     default: return MGCD_ERR_KERNEL;
   }
 }
+
+// Size class of a pair by its moduli count: <= 1024, <= 4096, larger.
+int size_class(uint32_t nq) { return nq <= 1024 ? 0 : nq <= 4096 ? 1 : 2; }
 
 size_t strip(const uint32_t* x, size_t n)
 {
@@ -146,11 +151,15 @@ struct mgcd_context {
   int launches = 0;
   bool ran = false;
   double work[4] = {0, 0, 0, 0};
-  float nq_scale = 1.0f;               // batches: fraction of the reference moduli count
+  // Per size class of the batched path (reference moduli count <= 1024, <= 4096, larger):
+  // CTA size, pairs per CTA in lockstep, fraction of the reference moduli count.
+  struct { int threads, k; float nq_scale; } cfg[NSTREAMS] = {{256, 4, 1.0f}, {512, 4, 1.0f}, {1024, 2, 1.0f}};
   std::vector<uint32_t> ref_nq, eff_nq; // per GPU pair: reference count, count of the final run
   int retried = 0;
   bool synced = false;
   DevBuf d_retry;
+  DevBuf d_invtab;                     // pairwise inverse table (InvTab)
+  uint32_t invtab_n = 0;
   // timing: the whole run on `stream`, and each bucket launch on its stream
   cudaEvent_t t_run0 = nullptr, t_run1 = nullptr, t_b0[NSTREAMS] = {}, t_b1[NSTREAMS] = {};
   uint64_t h2d_bytes = 0, d2h_bytes = 0;
@@ -248,6 +257,15 @@ int mgcd_create(int device, int L, mgcd_context** out)
   if (rc == MGCD_OK &&
       cudaMemcpy(c->mods.p, mc.data(), mc.size() * sizeof(ModConstHost), cudaMemcpyHostToDevice) != cudaSuccess)
     rc = MGCD_ERR_CUDA;
+  // Pairwise inverses of the first INVTAB_N moduli (every pair of the batched path), for
+  // recovery: 1 GiB at n = 16,384.
+  c->invtab_n = (uint32_t)std::min<size_t>(INVTAB_N, c->moduli.size());
+  if (rc == MGCD_OK && c->d_invtab.grow((size_t)c->invtab_n * c->invtab_n * sizeof(uint32_t)) != cudaSuccess)
+    rc = MGCD_ERR_CUDA;
+  if (rc == MGCD_OK && (launch_build_invtab(c->mods.as<ModConst>(), c->invtab_n, c->d_invtab.as<uint32_t>(),
+                                            c->stream) != cudaSuccess ||
+                        cudaStreamSynchronize(c->stream) != cudaSuccess))
+    rc = MGCD_ERR_CUDA;
   if (rc != MGCD_OK) {
     mgcd_destroy(c);
     return rc;
@@ -262,7 +280,7 @@ int mgcd_destroy(mgcd_context* c)
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (DevBuf* b : {&c->mods, &c->d_limbs, &c->d_pairs, &c->d_order, &c->d_digits, &c->d_count, &c->d_iters,
-                    &c->d_status, &c->d_queue, &c->d_scratch, &c->d_gsync, &c->d_retry})
+                    &c->d_status, &c->d_queue, &c->d_scratch, &c->d_gsync, &c->d_retry, &c->d_invtab})
     b->release();
   for (HostBuf* b : {&c->h_count, &c->h_iters, &c->h_status, &c->h_digits, &c->h_gsync}) b->release();
   for (int i = 0; i < NSTREAMS; ++i) {
@@ -349,8 +367,9 @@ static int plan_batch(mgcd_context* c, size_t np, const uint32_t* limbs, const u
     // Batches may use fewer moduli than the reference formula (less work per iteration);
     // a pair whose result cannot then be certified is rerun with the reference count.
     int nq = ref_nq;
-    if (!plain && c->nq_scale < 1.0f)
-      nq = std::min(ref_nq, std::max(256, ((int)std::ceil(c->nq_scale * ref_nq) + 255) / 256 * 256));
+    const float scale = c->cfg[size_class(ref_nq)].nq_scale;
+    if (!plain && scale < 1.0f)
+      nq = std::min(ref_nq, std::max(256, ((int)std::ceil(scale * ref_nq) + 255) / 256 * 256));
     d.nq = (uint32_t)nq;
     d.out_off = out_off;
     out_off += (uint32_t)ref_nq + 1;
@@ -409,10 +428,14 @@ static int schedule(mgcd_context* c, const std::vector<PairDesc>& descs, const s
     } else if (nq > CTA_MAX_NQ) {
       grid_pairs.push_back(k);
     } else {
-      byb[nq <= 1024 ? 0 : nq <= 4096 ? 1 : 2].push_back(k);
+      byb[size_class(nq)].push_back(k);
     }
   }
-  static const int kThreads[NSTREAMS] = {256, 512, 1024};
+  int kThreads[NSTREAMS], kSlots[NSTREAMS];
+  for (int b = 0; b < NSTREAMS; ++b) {
+    kThreads[b] = c->cfg[b].threads;
+    kSlots[b] = c->cfg[b].k;
+  }
   for (int b = NSTREAMS - 1; b >= 0; --b) {  // largest CTA size first: its pairs are the longest
     auto& v = byb[b];
     if (v.empty()) continue;
@@ -423,15 +446,17 @@ static int schedule(mgcd_context* c, const std::vector<PairDesc>& descs, const s
     });
     Bucket bk;
     bk.threads = kThreads[b];
+    bk.k = plain ? 1 : kSlots[b];
+    bk.cls = b;
     bk.first = (uint32_t)c->order.size();
     bk.n = (uint32_t)v.size();
     bk.nq_max = descs[v[0]].nq;
-    bk.smem = batch_smem_bytes(bk.threads, bk.nq_max);
+    bk.smem = batch_smem_bytes(bk.threads, bk.k, bk.nq_max);
     int bps = 0;
-    if (batch_max_blocks_per_sm(bk.threads, bk.smem, &bps) != cudaSuccess || bps < 1) return MGCD_ERR_GRID;
-    bk.grid = (int)std::min<size_t>(v.size(), (size_t)c->sms * bps);
+    if (batch_max_blocks_per_sm(bk.threads, bk.k, bk.smem, &bps) != cudaSuccess || bps < 1) return MGCD_ERR_GRID;
+    bk.grid = (int)std::min<size_t>((v.size() + bk.k - 1) / bk.k, (size_t)c->sms * bps);
     bk.scratch_off = scratch;
-    scratch += (size_t)bk.grid * 4 * bk.nq_max;
+    scratch += (size_t)bk.grid * 4 * bk.k * bk.nq_max;
     c->order.insert(c->order.end(), v.begin(), v.end());
     buckets.push_back(bk);
   }
@@ -451,7 +476,38 @@ int mgcd_batch_upload(mgcd_context* c, size_t np, const uint32_t* limbs, const u
 int mgcd_set_nq_scale(mgcd_context* c, float scale)
 {
   if (!c || !(scale >= 0.5f && scale <= 1.0f)) return MGCD_ERR_INVALID_ARG;
-  c->nq_scale = scale;
+  for (auto& b : c->cfg) b.nq_scale = scale;
+  return MGCD_OK;
+}
+
+int mgcd_set_size_class(mgcd_context* c, int cls, int threads, int k, float nq_scale)
+{
+  if (!c || cls < 0 || cls >= NSTREAMS || !(nq_scale >= 0.5f && nq_scale <= 1.0f)) return MGCD_ERR_INVALID_ARG;
+  if (threads != 256 && threads != 512 && threads != 1024) return MGCD_ERR_INVALID_ARG;
+  if (k != 1 && k != 2 && !(k == 4 && threads <= 512)) return MGCD_ERR_INVALID_ARG;
+  c->cfg[cls].threads = threads;
+  c->cfg[cls].k = k;
+  c->cfg[cls].nq_scale = nq_scale;
+  return MGCD_OK;
+}
+
+int mgcd_get_size_class(const mgcd_context* c, int cls, int* threads, int* k, float* nq_scale)
+{
+  if (!c || cls < 0 || cls >= NSTREAMS) return MGCD_ERR_INVALID_ARG;
+  if (threads) *threads = c->cfg[cls].threads;
+  if (k) *k = c->cfg[cls].k;
+  if (nq_scale) *nq_scale = c->cfg[cls].nq_scale;
+  return MGCD_OK;
+}
+
+int mgcd_batch_kernel_stats(const mgcd_context* c, int i, int* cls, int* pairs, float* ms)
+{
+  if (!c || !c->ran || i < 0 || i >= (int)c->buckets.size()) return MGCD_ERR_INVALID_ARG;
+  float t = 0.f;
+  CK(cudaEventElapsedTime(&t, c->t_b0[i], c->t_b1[i]));
+  if (cls) *cls = c->buckets[i].cls;
+  if (pairs) *pairs = (int)c->buckets[i].n;
+  if (ms) *ms = t;
   return MGCD_OK;
 }
 
@@ -466,6 +522,7 @@ static int launch_set(mgcd_context* c, const std::vector<Bucket>& buckets, const
   for (size_t b = 0; b < buckets.size(); ++b) {
     const Bucket& bk = buckets[b];
     BatchArgs a;
+    a.inv = InvTab{c->d_invtab.as<uint32_t>(), c->invtab_n};
     a.limbs = c->d_limbs.as<uint32_t>();
     a.pairs = pairs;
     a.order = c->d_order.as<uint32_t>() + bk.first;
@@ -474,7 +531,7 @@ static int launch_set(mgcd_context* c, const std::vector<Bucket>& buckets, const
     a.L = c->L;
     a.queue = queue_base + b;
     a.scratch = c->d_scratch.as<uint32_t>() + bk.scratch_off;
-    a.scratch_words = 4 * (size_t)bk.nq_max;
+    a.scratch_words = 4 * (size_t)bk.k * bk.nq_max;
     a.nq_max = bk.nq_max;
     a.digits = c->d_digits.as<mgcd_pair>();
     a.count = c->d_count.as<uint32_t>();
@@ -482,7 +539,7 @@ static int launch_set(mgcd_context* c, const std::vector<Bucket>& buckets, const
     a.status = c->d_status.as<int32_t>();
     CK(cudaStreamWaitEvent(c->bstream[b], c->ev_start, 0));
     if (time_buckets) CK(cudaEventRecord(c->t_b0[b], c->bstream[b]));
-    CK(launch_batch(a, bk.threads, bk.grid, bk.smem, c->bstream[b]));
+    CK(launch_batch(a, bk.threads, bk.k, bk.grid, bk.smem, c->bstream[b]));
     if (time_buckets) CK(cudaEventRecord(c->t_b1[b], c->bstream[b]));
     CK(cudaEventRecord(c->ev_b[b], c->bstream[b]));
     ++c->launches;
@@ -509,6 +566,7 @@ static int launch_set(mgcd_context* c, const std::vector<Bucket>& buckets, const
         if (grid > (uint32_t)(c->sms * bps)) return MGCD_ERR_GRID;
       }
       GridArgs g;
+      g.inv = InvTab{c->d_invtab.as<uint32_t>(), c->invtab_n};
       g.limbs = c->d_limbs.as<uint32_t>();
       g.pair = d;
       g.mods = c->mods.as<ModConst>();
@@ -570,7 +628,7 @@ static int sync_plan(mgcd_context* c)
   const int32_t* st = c->h_status.as<int32_t>();
   std::vector<uint32_t> redo;
   for (uint32_t k = 0; k < ng; ++k)
-    if (st[k] == ST_INSUFFICIENT && c->descs[k].nq < c->ref_nq[k]) redo.push_back(k);
+    if (st[k] != ST_OK && st[k] != ST_TIMEOUT && c->descs[k].nq < c->ref_nq[k]) redo.push_back(k);
   if (redo.empty()) return MGCD_OK;
   std::vector<PairDesc> rd = c->descs;
   for (uint32_t k : redo) rd[k].nq = c->ref_nq[k];

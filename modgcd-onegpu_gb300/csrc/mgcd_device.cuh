@@ -14,8 +14,9 @@ namespace mgcd {
 //   q    : the prime modulus (table order = createModuli order, descending)
 //   qinv : -q^{-1} mod 2^32 (Montgomery)
 //   r2   : 2^64 mod q
+//   r1   : 2^32 mod q (the Montgomery form of 1)
 struct __align__(16) ModConst {
-  uint32_t q, qinv, r2, pad;
+  uint32_t q, qinv, r2, r1;
 };
 
 // State of one modulus during the reduction loop: t = u_q / v_q mod q, or a marker.
@@ -177,6 +178,45 @@ __device__ __forceinline__ uint32_t t_update(uint32_t t, uint32_t q, uint32_t qi
   if (d == 0u) return T_INF;
   // redc(d) = d/R, inv = R/d, mont_mul(pm, R/d) = pm/d
   return mont_mul(pm, inv_mod(redc((uint64_t)d, q, qinv), q, qinv), q, qinv);
+}
+
+// The same update for K pairs that share the modulus q (slot s uses pivot (p[s], b[s]);
+// slots outside `mask` are left alone).  The K inverses are all mod q, so Montgomery's
+// trick replaces them by one: with x_s = d_s / R and prefix products P_s = x_0..x_s R^-s,
+// Z = P_{K-1}^{-1} = (x_0..x_{K-1})^{-1} R^{K-1}; walking back, mont_mul(Z, P_{s-1}) = x_s^{-1}
+// and Z <- mont_mul(Z, x_s).  Slots that need no inverse contribute R mod q (the
+// Montgomery one).  Then t'_s = mont_mul(pm_s, x_s^{-1}) = pm_s / d_s.
+template <int K>
+__device__ __forceinline__ void t_update_k(uint32_t (&t)[K], uint32_t q, uint32_t qinv, uint32_t r1,
+                                           const uint32_t (&p)[K], const int32_t (&b)[K], uint32_t mask)
+{
+  uint32_t x[K];
+  uint32_t need = 0;
+#pragma unroll
+  for (int s = 0; s < K; ++s) {
+    x[s] = r1;
+    if (!((mask >> s) & 1u)) continue;
+    const uint32_t ts = t[s];
+    if (ts >= T_MARK) { t[s] = (ts == T_INF) ? 0u : ts; continue; }
+    if (q == p[s]) { t[s] = T_RETIRED; continue; }
+    const uint32_t d = mod_sub(ts, from_signed(b[s], q), q);
+    if (d == 0u) { t[s] = T_INF; continue; }
+    x[s] = redc((uint64_t)d, q, qinv);
+    need |= 1u << s;
+  }
+  if (!need) return;
+  uint32_t P[K];
+  P[0] = x[0];
+#pragma unroll
+  for (int s = 1; s < K; ++s) P[s] = mont_mul(P[s - 1], x[s], q, qinv);
+  uint32_t Z = inv_mod(P[K - 1], q, qinv);
+#pragma unroll
+  for (int s = K - 1; s >= 1; --s) {
+    const uint32_t y = mont_mul(Z, P[s - 1], q, qinv);
+    Z = mont_mul(Z, x[s], q, qinv);
+    if ((need >> s) & 1u) t[s] = mont_mul(p[s] > q ? p[s] - q : p[s], y, q, qinv);
+  }
+  if (need & 1u) t[0] = mont_mul(p[0] > q ? p[0] - q : p[0], Z, q, qinv);
 }
 
 // Initial state t = u/v mod q from the residues.

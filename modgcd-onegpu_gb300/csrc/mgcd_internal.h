@@ -29,7 +29,16 @@ enum : int32_t {
   ST_PENDING = -1
 };
 
+// Pairwise inverse table: invtab[i * invtab_n + j] = q_i^{-1} * 2^32 mod q_j for table
+// moduli i, j < invtab_n (Montgomery form; the diagonal is unused).  Recovery divides by
+// the digit's modulus with one load and one Montgomery product instead of an inverse.
+struct InvTab {
+  const uint32_t* tab;
+  uint32_t n;
+};
+
 struct BatchArgs {
+  InvTab inv;
   const uint32_t* limbs;
   const PairDesc* pairs;
   const uint32_t* order;     // processing order (indices into pairs)
@@ -55,6 +64,7 @@ struct GridSync {
 };
 
 struct GridArgs {
+  InvTab inv;
   const uint32_t* limbs;
   PairDesc pair;
   const ModConst* mods;
@@ -69,9 +79,11 @@ struct GridArgs {
 };
 
 // Launch helpers (mgcd_kernels.cu).
-size_t batch_smem_bytes(int threads, uint32_t nq_max);
-cudaError_t batch_max_blocks_per_sm(int threads, size_t smem, int* blocks);
-cudaError_t launch_batch(const BatchArgs& a, int threads, int grid, size_t smem, cudaStream_t s);
+// k = pairs per CTA run in lockstep (1: batch_kernel; 2, 4: batchk_kernel).  Scratch per
+// CTA: 4 * k * nq_max words.
+size_t batch_smem_bytes(int threads, int k, uint32_t nq_max);
+cudaError_t batch_max_blocks_per_sm(int threads, int k, size_t smem, int* blocks);
+cudaError_t launch_batch(const BatchArgs& a, int threads, int k, int grid, size_t smem, cudaStream_t s);
 
 size_t grid_smem_bytes(uint32_t per_cta);
 cudaError_t grid_max_blocks_per_sm(size_t smem, int* blocks);
@@ -80,5 +92,8 @@ cudaError_t launch_grid(const GridArgs& a, int grid, size_t smem, cudaStream_t s
 
 // 256-thread blocks, 8 IMADs per thread per iteration.
 cudaError_t launch_int_peak(uint32_t* out, int blocks, int iters, cudaStream_t s);
+
+// Fills the n x n pairwise inverse table for the first n moduli.
+cudaError_t launch_build_invtab(const ModConst* mods, uint32_t n, uint32_t* tab, cudaStream_t s);
 
 }  // namespace mgcd

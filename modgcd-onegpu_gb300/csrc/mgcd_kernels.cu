@@ -16,6 +16,7 @@
 //          modulus with a nonzero value, exactly as the reference selects it.
 // The (p, b) sequence and the digits are identical to the reference algorithm's.
 #include <cstdint>
+#include <cstdlib>
 #include <cuda_runtime.h>
 
 #include "mgcd_device.cuh"
@@ -48,8 +49,222 @@ __global__ void __launch_bounds__(T) batch_kernel(const BatchArgs a)
     const uint32_t pi = a.order[k];
     const PairDesc d = a.pairs[pi];
     run_pair<T, false>(a.limbs, d, a.mods, a.L, 0u, d.nq, st, acc2, chunk, rs, u0, v0, hist, nullptr,
-                       a.digits, a.count + pi, a.iters + pi, a.status + pi);
+                       a.digits, a.count + pi, a.iters + pi, a.status + pi, a.inv);
     __syncthreads();
+  }
+}
+
+// ------------------------------------------------------- K pairs per CTA, lockstep ----
+//
+// The reduction loops of K pairs run side by side in one CTA; thread i owns modulus index
+// i (+ multiples of T) in every pair, so its K inverses per iteration are all mod the same
+// prime and t_update_k turns them into one.  Each pair keeps its own pivot sequence,
+// exactly as if it ran alone; a pair whose loop has ended simply drops out of the update.
+// Set-up (residues) and finish (certification, replay, recovery) run pair by pair: when a
+// pair's loop ends, the CTA finishes it and loads the next pair of the queue into that
+// slot while the other slots keep their state, so the slots stay occupied.
+
+template <int K>
+struct SlotSmem {
+  unsigned long long key[2][K][32];  // per-warp minima per slot, double-buffered
+  PairDesc d[K];
+  uint32_t pi[K];                    // pair index of each slot (~0: empty)
+  double lu[K], lv[K];               // certification bounds (thread 0)
+};
+
+template <int T, int K>
+__device__ __forceinline__ void block_min_keys(uint32_t (&kh)[K], uint32_t (&kl)[K], SlotSmem<K>& ss,
+                                               uint32_t& parity)
+{
+  constexpr int NW = T / 32;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int s = 0; s < K; ++s) {
+    warp_min_key(kh[s], kl[s]);
+    if (lane == 0) ss.key[parity][s][w] = ((unsigned long long)kh[s] << 32) | kl[s];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int s = 0; s < K; ++s) {
+    const unsigned long long k = (lane < NW) ? ss.key[parity][s][lane] : ~0ull;
+    kh[s] = (uint32_t)(k >> 32);
+    kl[s] = (uint32_t)k;
+    warp_min_key(kh[s], kl[s]);
+  }
+  parity ^= 1u;
+}
+
+// Register arrays indexed by a runtime slot number, without spilling them to memory.
+template <int K, class V>
+__device__ __forceinline__ V pick(const V (&a)[K], int s)
+{
+  V r = a[0];
+#pragma unroll
+  for (int t = 1; t < K; ++t)
+    if (t == s) r = a[t];
+  return r;
+}
+
+template <int K, class V>
+__device__ __forceinline__ void put(V (&a)[K], int s, V v)
+{
+#pragma unroll
+  for (int t = 0; t < K; ++t)
+    if (t == s) a[t] = v;
+}
+
+template <int T, int K, int MINB = 1>
+__global__ void __launch_bounds__(T, MINB) batchk_kernel(const BatchArgs a)
+{
+  extern __shared__ __align__(16) uint32_t smem[];
+  __shared__ SlotSmem<K> ss;
+  __shared__ RedSmem rs;
+  __shared__ uint32_t next;
+  const uint32_t NQS = a.nq_max;
+  uint32_t* const tS = smem;                          // K x NQS states
+  uint32_t* const acc2 = smem + (size_t)K * NQS;      // residues of v during set-up
+  uint32_t* const chunk = acc2 + NQS;
+  uint32_t* const scr = a.scratch + (size_t)blockIdx.x * a.scratch_words;   // per slot u0, v0, hist
+  const int L = a.L;
+  uint32_t kparity = 0, rparity = 0, repoch = 0;
+  uint32_t valid = 0, active = 0, redux = 0;          // slots holding a pair / in the loop / ran out
+  int rem[K], ubits[K], vbits[K];
+  uint32_t iters[K], p[K], kh[K], kl[K];
+  int32_t b[K];
+
+  // Takes the next pair of the queue into slot s: residues, initial ratios, first pivot.
+  auto load = [&](int s) -> bool {
+    if (threadIdx.x == 0) next = atomicAdd(a.queue, 1u);
+    __syncthreads();
+    const uint32_t k = next;
+    __syncthreads();
+    if (k >= a.npairs) return false;
+    if (threadIdx.x == 0) {
+      ss.pi[s] = a.order[k];
+      ss.d[s] = a.pairs[ss.pi[s]];
+    }
+    __syncthreads();
+    const PairDesc& d = ss.d[s];
+    uint32_t* ts = tS + (size_t)s * NQS;
+    uint32_t* u0 = scr + (size_t)s * 4 * NQS;
+    residues<T>(a.limbs + d.u_off, d.u_len, a.mods, d.nq, ts, chunk);
+    residues<T>(a.limbs + d.v_off, d.v_len, a.mods, d.nq, acc2, chunk);
+    uint32_t h0 = 0xFFFFFFFFu, l0 = 0xFFFFFFFFu;
+    for (uint32_t j = threadIdx.x; j < d.nq; j += T) {
+      const ModConst c = a.mods[j];
+      const uint32_t u = ts[j], v = acc2[j];
+      u0[j] = u;
+      u0[NQS + j] = v;
+      const uint32_t t = t_init(u, v, c.q, c.qinv);
+      ts[j] = t;
+      uint32_t h, l;
+      t_key(t, c.q, h, l);
+      if (key_less(h, l, h0, l0)) { h0 = h; l0 = l; }
+    }
+    if (threadIdx.x == 32u * s) {
+      ss.lu[s] = (double)(((int)d.u_len - 1) * 32 + (32 - __clz(a.limbs[d.u_off + d.u_len - 1])));
+      ss.lv[s] = (double)(((int)d.v_len - 1) * 32 + (32 - __clz(a.limbs[d.v_off + d.v_len - 1])));
+    }
+    block_min_key<T>(h0, l0, rs, rparity);
+    uint32_t p0;
+    int32_t b0;
+    key_pair(h0, l0, p0, b0);
+    put(p, s, p0);
+    put(b, s, b0);
+    put(rem, s, (int)d.nq);
+    put(ubits, s, ((int)d.u_len + 1) * 32);
+    put(vbits, s, ((int)d.v_len + 1) * 32);
+    put(iters, s, 0u);
+    return true;
+  };
+
+#pragma unroll 1
+  for (int s = 0; s < K; ++s)
+    if (load(s)) { valid |= 1u << s; active |= 1u << s; }
+
+  for (;;) {
+    // ---- pairs whose reduction loop ended: finish them and refill their slots
+    const uint32_t done = valid & ~active;
+#pragma unroll 1
+    for (int s = 0; s < K; ++s) {
+      if (!((done >> s) & 1u)) continue;
+      const uint32_t pi = ss.pi[s];
+      const uint32_t it = pick(iters, s);
+      if (threadIdx.x == 0) a.iters[pi] = it;
+      if ((redux >> s) & 1u) {
+        if (threadIdx.x == 0) { a.status[pi] = ST_REDUX; a.count[pi] = 0; }
+      } else {
+        uint32_t* u0 = scr + (size_t)s * 4 * NQS;
+        finish_pair<T, false>(a.mods, ss.d[s], L, 0u, ss.d[s].nq, tS + (size_t)s * NQS, rs, rparity, repoch, nullptr,
+                              u0, u0 + NQS, reinterpret_cast<const int2*>(u0 + 2 * (size_t)NQS), it, pick(rem, s),
+                              ss.lu[s], ss.lv[s], a.digits, a.count + pi, a.status + pi, a.inv);
+      }
+      __syncthreads();
+      valid &= ~(1u << s);
+      redux &= ~(1u << s);
+      if (load(s)) { valid |= 1u << s; active |= 1u << s; }
+    }
+    if (!valid) break;
+
+    // ---- per-pair bookkeeping for this iteration's pivots (GmpCudaDevice-getGcdKernel.cu:365-402)
+#pragma unroll
+    for (int s = 0; s < K; ++s) {
+      if (!((active >> s) & 1u)) continue;
+      if (b[s] == MOD_INFINITY) { active &= ~(1u << s); continue; }
+      int2* hist = reinterpret_cast<int2*>(scr + (size_t)s * 4 * NQS + 2 * (size_t)NQS);
+      if (threadIdx.x == 32u * s) {   // one warp per slot keeps the history and the size bounds
+        hist[iters[s]] = make_int2((int)p[s], b[s]);
+        const uint32_t ab = b[s] < 0 ? 0u - (uint32_t)b[s] : (uint32_t)b[s];
+        double sum = ss.lu[s];
+        if (ab != 0u) {
+          const double y = ss.lv[s] + (double)log2f((float)ab);
+          const double m = y > sum ? y : sum, dd = y > sum ? y - sum : sum - y;
+          sum = m + (dd < 40.0 ? (double)log2f(1.0f + exp2f(-(float)dd)) : 0.0);
+        }
+        ss.lu[s] = ss.lv[s];
+        ss.lv[s] = sum - (double)log2f((float)p[s]) + 1e-4;
+      }
+      ++iters[s];
+      rem[s] -= 1;
+      const uint32_t ab = b[s] < 0 ? 0u - (uint32_t)b[s] : (uint32_t)b[s];
+      const int tbits = ubits[s] - (L - 1) + __ffs((int)ab);
+      ubits[s] = vbits[s];
+      vbits[s] = tbits;
+      if (rem[s] * (L - 2) <= ubits[s]) { redux |= 1u << s; active &= ~(1u << s); }
+    }
+    if (!active) continue;
+
+    // ---- one update of every active pair, then the next pivots
+    uint32_t nq_max = 0;
+#pragma unroll
+    for (int s = 0; s < K; ++s) {
+      if ((active >> s) & 1u) nq_max = max(nq_max, ss.d[s].nq);
+      kh[s] = kl[s] = 0xFFFFFFFFu;
+    }
+    for (uint32_t j = threadIdx.x; j < nq_max; j += T) {
+      uint32_t m = 0, tv[K];
+#pragma unroll
+      for (int s = 0; s < K; ++s) {
+        const bool on = ((active >> s) & 1u) && j < ss.d[s].nq;
+        m |= (uint32_t)on << s;
+        tv[s] = on ? tS[(size_t)s * NQS + j] : T_RETIRED;
+      }
+      if (!m) continue;
+      const ModConst c = a.mods[j];
+      t_update_k<K>(tv, c.q, c.qinv, c.r1, p, b, m);
+#pragma unroll
+      for (int s = 0; s < K; ++s) {
+        if (!((m >> s) & 1u)) continue;
+        tS[(size_t)s * NQS + j] = tv[s];
+        uint32_t h, l;
+        t_key(tv[s], c.q, h, l);
+        if (key_less(h, l, kh[s], kl[s])) { kh[s] = h; kl[s] = l; }
+      }
+    }
+    block_min_keys<T, K>(kh, kl, ss, kparity);
+#pragma unroll
+    for (int s = 0; s < K; ++s)
+      if ((active >> s) & 1u) key_pair(kh[s], kl[s], p[s], b[s]);
   }
 }
 
@@ -69,7 +284,7 @@ __global__ void __launch_bounds__(GRID_THREADS) grid_kernel(const GridArgs a)
   uint32_t* v0 = a.scratch + nq + j0;
   int2* hist = reinterpret_cast<int2*>(a.scratch + 2 * (size_t)nq);
   run_pair<GRID_THREADS, true>(a.limbs, a.pair, a.mods, a.L, j0, nloc, st, acc2, chunk, rs, u0, v0, hist,
-                               a.sync, a.digits, a.count, a.iters, a.status);
+                               a.sync, a.digits, a.count, a.iters, a.status, a.inv);
 }
 
 // Integer-pipe microbenchmark: eight independent IMAD chains per thread.
@@ -93,41 +308,74 @@ cudaError_t launch_int_peak(uint32_t* out, int blocks, int iters, cudaStream_t s
   return cudaGetLastError();
 }
 
+// tab[i * n + j] = R / q_i mod q_j (Montgomery form of q_i^{-1}); moduli of one width
+// satisfy q_i < 2 q_j, so q_i mod q_j is one conditional subtraction.
+__global__ void __launch_bounds__(256) build_invtab_kernel(const ModConst* __restrict__ mods, uint32_t n,
+                                                           uint32_t* __restrict__ tab)
+{
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = blockIdx.y;
+  if (j >= n) return;
+  const ModConst c = mods[j];
+  const uint32_t p = mods[i].q;
+  uint32_t v = 0u;
+  if (i != j) v = inv_mod(redc((uint64_t)(p > c.q ? p - c.q : p), c.q, c.qinv), c.q, c.qinv);
+  tab[(size_t)i * n + j] = v;
+}
+
+cudaError_t launch_build_invtab(const ModConst* mods, uint32_t n, uint32_t* tab, cudaStream_t s)
+{
+  build_invtab_kernel<<<dim3((n + 255) / 256, n), 256, 0, s>>>(mods, n, tab);
+  return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------- launchers ----
 
-size_t batch_smem_bytes(int /*threads*/, uint32_t nq_max)
+size_t batch_smem_bytes(int /*threads*/, int k, uint32_t nq_max)
 {
-  return sizeof(uint32_t) * (2 * (size_t)nq_max + CHUNK);
+  return sizeof(uint32_t) * ((size_t)(k > 1 ? k + 1 : 2) * nq_max + CHUNK);
 }
 
-template <int T>
-static const void* batch_fn()
+static const void* batch_fn_for(int threads, int k)
 {
-  return reinterpret_cast<const void*>(&batch_kernel<T>);
-}
-
-static const void* batch_fn_for(int threads)
-{
-  switch (threads) {
-    case 256: return batch_fn<256>();
-    case 512: return batch_fn<512>();
-    case 1024: return batch_fn<1024>();
-    default: return nullptr;
+  if (k == 1) {
+    switch (threads) {
+      case 256: return reinterpret_cast<const void*>(&batch_kernel<256>);
+      case 512: return reinterpret_cast<const void*>(&batch_kernel<512>);
+      case 1024: return reinterpret_cast<const void*>(&batch_kernel<1024>);
+      default: return nullptr;
+    }
   }
+  if (k == 2) {
+    switch (threads) {
+      case 256: return reinterpret_cast<const void*>(&batchk_kernel<256, 2>);
+      case 512: return reinterpret_cast<const void*>(&batchk_kernel<512, 2>);
+      case 1024: return reinterpret_cast<const void*>(&batchk_kernel<1024, 2>);
+      default: return nullptr;
+    }
+  }
+  if (k == 4) {
+    switch (threads) {
+      case 256: return reinterpret_cast<const void*>(&batchk_kernel<256, 4>);
+      case 512: return reinterpret_cast<const void*>(&batchk_kernel<512, 4>);
+      default: return nullptr;
+    }
+  }
+  return nullptr;
 }
 
-cudaError_t batch_max_blocks_per_sm(int threads, size_t smem, int* blocks)
+cudaError_t batch_max_blocks_per_sm(int threads, int k, size_t smem, int* blocks)
 {
-  const void* fn = batch_fn_for(threads);
+  const void* fn = batch_fn_for(threads, k);
   if (!fn) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, fn, threads, smem);
 }
 
-cudaError_t launch_batch(const BatchArgs& a, int threads, int grid, size_t smem, cudaStream_t s)
+cudaError_t launch_batch(const BatchArgs& a, int threads, int k, int grid, size_t smem, cudaStream_t s)
 {
-  const void* fn = batch_fn_for(threads);
+  const void* fn = batch_fn_for(threads, k);
   if (!fn) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;

@@ -91,7 +91,7 @@ void mod_constants(const uint32_t* q, size_t n, ModConstHost* out)
     out[i].q = m;
     out[i].qinv = 0u - x;
     out[i].r2 = (uint32_t)((r1 * r1) % m);
-    out[i].pad = 0u;
+    out[i].r1 = (uint32_t)r1;
   }
 }
 

@@ -5,9 +5,10 @@
 
 namespace mgcd {
 
-// Host mirror of the device ModConst record (mgcd_device.cuh).
+// Host mirror of the device ModConst record (mgcd_device.cuh): q, -q^-1 mod 2^32,
+// 2^64 mod q, 2^32 mod q.
 struct ModConstHost {
-  uint32_t q, qinv, r2, pad;
+  uint32_t q, qinv, r2, r1;
 };
 
 // The first `count` usable L-bit primes, descending (createModuli order).  Returns the

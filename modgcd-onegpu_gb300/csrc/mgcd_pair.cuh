@@ -127,6 +127,13 @@ __device__ void residues(const uint32_t* __restrict__ x, uint32_t n, const ModCo
   __syncthreads();
 }
 
+template <int T, bool GRID>
+__device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d, int L, uint32_t j0, uint32_t nloc,
+                            uint32_t* st, RedSmem& rs, uint32_t& parity, uint32_t& epoch, GridSync* gs,
+                            const uint32_t* u0g, const uint32_t* v0g, const int2* hist, uint32_t iters, int remaining,
+                            double lu, double lv, mgcd_pair* digits, uint32_t* count, int32_t* status,
+                            InvTab inv);
+
 // The whole gcd of one pair by this CTA (GRID = false) or by the cooperative grid, the
 // calling CTA owning global moduli [j0, j0 + nloc).
 //   st, acc2   shared arrays of nloc words; chunk: CHUNK words
@@ -136,7 +143,8 @@ template <int T, bool GRID>
 __device__ void run_pair(const uint32_t* __restrict__ limbs, const PairDesc& d, const ModConst* __restrict__ mods,
                          int L, uint32_t j0, uint32_t nloc, uint32_t* st, uint32_t* acc2, uint32_t* chunk,
                          RedSmem& rs, uint32_t* u0g, uint32_t* v0g, int2* hist, GridSync* gs,
-                         mgcd_pair* digits, uint32_t* count, uint32_t* iters_out, int32_t* status)
+                         mgcd_pair* digits, uint32_t* count, uint32_t* iters_out, int32_t* status,
+                         InvTab inv)
 {
   const bool writer = threadIdx.x == 0 && (!GRID || blockIdx.x == 0);
   const ModConst* __restrict__ my = mods + j0;
@@ -218,6 +226,23 @@ __device__ void run_pair(const uint32_t* __restrict__ limbs, const PairDesc& d, 
     key_pair(kh, kl, p, b);
   }
   if (writer) *iters_out = iters;
+  finish_pair<T, GRID>(mods, d, L, j0, nloc, st, rs, parity, epoch, gs, u0g, v0g, hist, iters, remaining, lu, lv,
+                       digits, count, status, inv);
+}
+
+// After the reduction loop of one pair: certification, replay and recovery (MGCD4).
+// st holds the final t states of this CTA's moduli; `remaining` the surviving count;
+// lu, lv (meaningful in thread 0) the size bounds of the final u and v.
+template <int T, bool GRID>
+__device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d, int L, uint32_t j0, uint32_t nloc,
+                            uint32_t* st, RedSmem& rs, uint32_t& parity, uint32_t& epoch, GridSync* gs,
+                            const uint32_t* u0g, const uint32_t* v0g, const int2* hist, uint32_t iters, int remaining,
+                            double lu, double lv, mgcd_pair* digits, uint32_t* count, int32_t* status,
+                            InvTab inv)
+{
+  const bool writer = threadIdx.x == 0 && (!GRID || blockIdx.x == 0);
+  const ModConst* __restrict__ my = mods + j0;
+  uint32_t p, kh, kl;
   // Certify the result: all surviving residues of v are 0, so v = 0 if the surviving
   // moduli (each > 2^(L-1)) multiply to more than |v|; recovery is exact if they exceed
   // 2|u| (symmetric digits).  Otherwise report that more moduli are needed.
@@ -229,6 +254,7 @@ __device__ void run_pair(const uint32_t* __restrict__ limbs, const PairDesc& d, 
   __syncthreads();
   if (rs.cert) {
     if (writer) { *status = ST_INSUFFICIENT; *count = 0; }
+    __syncthreads();
     return;
   }
 
@@ -266,6 +292,7 @@ __device__ void run_pair(const uint32_t* __restrict__ limbs, const PairDesc& d, 
   }
   uint32_t ndig = 0;
   int32_t g;
+  uint32_t pidx = kh == 0xFFFFFFFFu ? 0u : kh;      // table index of the digit's modulus
   if (kh == 0xFFFFFFFFu) { p = mods[0].q; g = 0; } else { p = mods[kh].q; g = (int32_t)kl; }
   do {
     kh = 0xFFFFFFFFu;
@@ -276,8 +303,11 @@ __device__ void run_pair(const uint32_t* __restrict__ limbs, const PairDesc& d, 
       const ModConst c = my[j];
       const uint32_t q = c.q, qi = c.qinv;
       if (q == p) { st[j] = U_RETIRED; continue; }
-      const uint32_t pm = p > q ? p - q : p;
-      u = mont_mul(mod_sub(u, from_signed(g, q), q), inv_mod(redc((uint64_t)pm, q, qi), q, qi), q, qi);
+      const uint32_t jj = j0 + j;
+      const uint32_t dinv = (pidx < inv.n && jj < inv.n)
+                                ? __ldg(inv.tab + (size_t)pidx * inv.n + jj)            // R / p mod q
+                                : inv_mod(redc((uint64_t)(p > q ? p - q : p), q, qi), q, qi);
+      u = mont_mul(mod_sub(u, from_signed(g, q), q), dinv, q, qi);
       st[j] = u;
       if (u != 0u && kh == 0xFFFFFFFFu) { kh = j0 + j; kl = (uint32_t)to_signed(u, q); }
     }
@@ -289,6 +319,7 @@ __device__ void run_pair(const uint32_t* __restrict__ limbs, const PairDesc& d, 
       if (writer) *status = ST_TIMEOUT;
       return;
     }
+    pidx = kh == 0xFFFFFFFFu ? 0u : kh;
     if (kh == 0xFFFFFFFFu) { p = mods[0].q; g = 0; } else { p = mods[kh].q; g = (int32_t)kl; }
   } while (g != 0);
   if (writer) {

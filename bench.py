@@ -50,6 +50,9 @@ def parse():
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--plain-sample", type=int, default=64)
     ap.add_argument("--cpu-reps", type=int, default=10)
+    ap.add_argument("--workload", choices=["mixed", "sweep"], default="mixed")
+    ap.add_argument("--sizes", default="4096,16384,65536,262144,1048576")
+    ap.add_argument("--reps", type=int, default=3)
     return ap.parse_args()
 
 
@@ -301,10 +304,64 @@ def run_ours(args, rank, local, world, pg):
     print(json.dumps(line), flush=True)
 
 
+def run_sweep(args, rank, local):
+    """Single-pair latency sweep: n-bit operands with an n/4-bit planted gcd, at modulus
+    widths 22/27/32, one pair per call (the plain method), median over reps."""
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    mg = importlib.import_module("modgcd-onegpu_gb300")
+    wl = importlib.import_module("modgcd-onegpu_gb300.workloads")
+    sizes = [int(x) for x in args.sizes.split(",")]
+    rows = []
+    for L in (32, 27, 22):
+        dev = mg.Device(local, L)
+        for n in sizes:
+            u, v = wl.size_sweep_pair(n, seed=1)
+            packed = mg.pack_pairs([u], [v])
+            gsec = [po.cpu_gmp_gcd_batch(*packed, 1, want_results=False)[0] for _ in range(3)]
+            _, gx, gxo, gxn = po.cpu_gmp_gcd_batch(*packed, 1)
+            expect = po.from_limbs(gx[: int(gxn[0])])
+            wall, dev_ms, ok = [], [], True
+            for r in range(args.reps + 1):
+                t0 = time.perf_counter()
+                try:
+                    g = dev.gcd(u, v)
+                except mg.GcdError as e:
+                    rows.append({"L": L, "bits": n, "error": str(e)})
+                    ok = None
+                    break
+                t1 = time.perf_counter()
+                ok = ok and g == expect
+                if r:
+                    wall.append(1e3 * (t1 - t0))
+                    dev_ms.append(dev.batch_elapsed_ms()[0])
+            if ok is None:
+                continue
+            # the same pair in the reference's launch shape (256-thread CTAs, grid-wide exchange)
+            dev.set_single_pair_policy(1)
+            ref_ms = []
+            for _ in range(max(1, args.reps - 1)):
+                ok = ok and dev.gcd(u, v) == expect
+                ref_ms.append(dev.batch_elapsed_ms()[0])
+            dev.set_single_pair_policy(0)
+            rows.append({"L": L, "bits": n, "moduli": mg.moduli_needed(n, L), "device_ms": statistics.median(dev_ms),
+                         "wall_ms": statistics.median(wall), "p99_wall_ms": max(wall),
+                         "reference_shape_ms": statistics.median(ref_ms), "gmp_ms": 1e3 * min(gsec),
+                         "bit_exact": bool(ok)})
+            print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
+        dev.close()
+    print(json.dumps({"metric": "single-pair gcd latency (plain method), n-bit operands, n/4-bit gcd",
+                      "unit": "ms", "higher_is_better": False, "data": "synthetic", "rows": rows}), flush=True)
+
+
 def main():
     args = parse()
     rank, local, world, pg = dist()
-    if args.impl == "reference":
+    if args.workload == "sweep":
+        run_sweep(args, rank, local)
+    elif args.impl == "reference":
         run_reference(args, rank, pg)
     else:
         run_ours(args, rank, local, world, pg)

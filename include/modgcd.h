@@ -125,6 +125,28 @@ int mgcd_batch_download(mgcd_context *ctx, uint32_t *g, const uint64_t *g_off, c
    that cannot be certified is rerun with the reference's count, so results do not change.
    Single-pair calls always use the reference's count. */
 int mgcd_set_nq_scale(mgcd_context *ctx, float scale);
+/* Launch shape of single pairs too large for one CTA:
+     MGCD_SINGLE_AUTO              a thread-block cluster of up to 16 CTAs (pivot exchange
+                                   through distributed shared memory) while the pair's
+                                   moduli fit 16 x 1024 threads, else a cooperative grid
+                                   with one CTA per SM (default);
+     MGCD_SINGLE_REFERENCE_SHAPE   the reference's launch shape: a cooperative grid of
+                                   256-thread CTAs with 256 moduli each, one grid-wide
+                                   exchange per iteration (GmpCudaDevice-gcd.cu:80-96). */
+#define MGCD_SINGLE_AUTO            0
+#define MGCD_SINGLE_REFERENCE_SHAPE 1
+int mgcd_set_single_pair_policy(mgcd_context *ctx, int policy);
+/* Bound of every wait a cooperative-grid pair makes on the other CTAs (default 2,000 ms).
+   When it runs out, every CTA returns and the pair fails with MGCD_ERR_TIMEOUT; the
+   context stays usable.  (The reference's grid barrier spins without a bound,
+   GmpCuda.h:68-83.) */
+int mgcd_set_wait_timeout_ms(mgcd_context *ctx, unsigned ms);
+/* Test hook for the bounded waits: CTA `cta` of the next cooperative-grid pairs never
+   publishes its minimum, so the other CTAs' waits run out (-1 turns the hook off). */
+int mgcd_test_withhold_cta(mgcd_context *ctx, int cta);
+/* Test hook for the "ran out of moduli" paths: every following pair uses exactly nq
+   moduli (a multiple of 256; 0 restores the reference's count) and is not rerun. */
+int mgcd_test_force_moduli(mgcd_context *ctx, unsigned nq);
 /* Launch configuration of one size class of the batched path: class 0 = pairs needing
    <= 1,024 moduli, 1 = <= 4,096, 2 = larger (up to 16,384; beyond that a pair runs on a
    cooperative grid).  threads: CTA size (256, 512, 1024); k: pairs one CTA runs in

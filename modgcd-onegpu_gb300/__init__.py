@@ -61,6 +61,10 @@ SIGNATURES = {
     "mgcd_gcd_digits_noalloc": (_c.c_int, [_P, _c.c_size_t, _c.c_size_t, _P, _c.c_size_t, _P, _P, _P]),
     "mgcd_set_nq_scale": (_c.c_int, [_P, _c.c_float]),
     "mgcd_set_size_class": (_c.c_int, [_P, _c.c_int, _c.c_int, _c.c_int, _c.c_float]),
+    "mgcd_set_single_pair_policy": (_c.c_int, [_P, _c.c_int]),
+    "mgcd_set_wait_timeout_ms": (_c.c_int, [_P, _c.c_uint]),
+    "mgcd_test_withhold_cta": (_c.c_int, [_P, _c.c_int]),
+    "mgcd_test_force_moduli": (_c.c_int, [_P, _c.c_uint]),
     "mgcd_get_size_class": (_c.c_int, [_P, _c.c_int, _c.POINTER(_c.c_int), _c.POINTER(_c.c_int),
                                        _c.POINTER(_c.c_float)]),
     "mgcd_batch_kernel_stats": (_c.c_int, [_P, _c.c_int, _c.POINTER(_c.c_int), _c.POINTER(_c.c_int),
@@ -279,6 +283,21 @@ class Device:
     def set_size_class(self, cls, threads, k, nq_scale):
         """Launch configuration of size class cls (0: <= 1024 moduli, 1: <= 4096, 2: larger)."""
         _check(self._lib.mgcd_set_size_class(self._h, int(cls), int(threads), int(k), float(nq_scale)))
+
+    def set_single_pair_policy(self, policy):
+        """0: cluster / grid (default); 1: the reference's launch shape (grid of 256-thread CTAs)."""
+        _check(self._lib.mgcd_set_single_pair_policy(self._h, int(policy)))
+
+    def set_wait_timeout_ms(self, ms):
+        _check(self._lib.mgcd_set_wait_timeout_ms(self._h, int(ms)))
+
+    def test_withhold_cta(self, cta):
+        """Test hook: CTA `cta` of grid-mode pairs never publishes (-1: off)."""
+        _check(self._lib.mgcd_test_withhold_cta(self._h, int(cta)))
+
+    def test_force_moduli(self, nq):
+        """Test hook: every pair uses exactly nq moduli, no rerun (0: reference count)."""
+        _check(self._lib.mgcd_test_force_moduli(self._h, int(nq)))
 
     def get_size_class(self, cls):
         t, k, s = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()

@@ -159,6 +159,10 @@ struct mgcd_context {
   bool synced = false;
   DevBuf d_retry;
   DevBuf d_invtab;                     // pairwise inverse table (InvTab)
+  int single_policy = MGCD_SINGLE_AUTO;  // launch shape of pairs that span several CTAs
+  unsigned long long wait_timeout_ns = 2000000000ull;   // bound of every cross-CTA wait
+  uint32_t withhold_cta = 0xFFFFFFFFu;                  // test hook (mgcd_test_withhold_cta)
+  uint32_t force_nq = 0;                                // test hook (mgcd_test_force_moduli)
   uint32_t invtab_n = 0;
   // timing: the whole run on `stream`, and each bucket launch on its stream
   cudaEvent_t t_run0 = nullptr, t_run1 = nullptr, t_b0[NSTREAMS] = {}, t_b1[NSTREAMS] = {};
@@ -359,7 +363,7 @@ static int plan_batch(mgcd_context* c, size_t np, const uint32_t* limbs, const u
     }
     const uint32_t top = limbs[d.u_off + d.u_len - 1];
     const size_t ubits = (size_t)(d.u_len - 1) * 32 + (32 - __builtin_clz(top));
-    const int ref_nq = moduli_needed(c->L, ubits);
+    const int ref_nq = c->force_nq ? (int)c->force_nq : moduli_needed(c->L, ubits);
     if ((size_t)ref_nq > c->moduli.size()) {
       c->status[i] = MGCD_ERR_NOT_ENOUGH_MODULI;
       continue;
@@ -419,12 +423,12 @@ static int schedule(mgcd_context* c, const std::vector<PairDesc>& descs, const s
 {
   buckets.clear();
   grid_pairs.clear();
-  const uint32_t plain_cta_max = (uint32_t)env_int("MGCD_PLAIN_CTA_MAX", 2048);
+  const uint32_t plain_cta_max = 256;   // single pairs: one CTA, else a cluster or a grid
   std::vector<uint32_t> byb[NSTREAMS];
   for (uint32_t k : subset) {
     const uint32_t nq = descs[k].nq;
     if (plain) {
-      if (nq <= plain_cta_max) byb[2].push_back(k); else grid_pairs.push_back(k);
+      if (nq <= plain_cta_max) byb[0].push_back(k); else grid_pairs.push_back(k);
     } else if (nq > CTA_MAX_NQ) {
       grid_pairs.push_back(k);
     } else {
@@ -445,7 +449,7 @@ static int schedule(mgcd_context* c, const std::vector<PairDesc>& descs, const s
       return a.u_len + a.v_len > bb.u_len + bb.v_len;
     });
     Bucket bk;
-    bk.threads = kThreads[b];
+    bk.threads = plain ? 256 : kThreads[b];
     bk.k = plain ? 1 : kSlots[b];
     bk.cls = b;
     bk.first = (uint32_t)c->order.size();
@@ -488,6 +492,34 @@ int mgcd_set_size_class(mgcd_context* c, int cls, int threads, int k, float nq_s
   c->cfg[cls].threads = threads;
   c->cfg[cls].k = k;
   c->cfg[cls].nq_scale = nq_scale;
+  return MGCD_OK;
+}
+
+int mgcd_set_single_pair_policy(mgcd_context* c, int policy)
+{
+  if (!c || (policy != MGCD_SINGLE_AUTO && policy != MGCD_SINGLE_REFERENCE_SHAPE)) return MGCD_ERR_INVALID_ARG;
+  c->single_policy = policy;
+  return MGCD_OK;
+}
+
+int mgcd_set_wait_timeout_ms(mgcd_context* c, unsigned ms)
+{
+  if (!c || ms == 0) return MGCD_ERR_INVALID_ARG;
+  c->wait_timeout_ns = (unsigned long long)ms * 1000000ull;
+  return MGCD_OK;
+}
+
+int mgcd_test_force_moduli(mgcd_context* c, unsigned nq)
+{
+  if (!c || nq % 256 || nq > c->moduli.size()) return MGCD_ERR_INVALID_ARG;
+  c->force_nq = nq;
+  return MGCD_OK;
+}
+
+int mgcd_test_withhold_cta(mgcd_context* c, int cta)
+{
+  if (!c) return MGCD_ERR_INVALID_ARG;
+  c->withhold_cta = cta < 0 ? 0xFFFFFFFFu : (uint32_t)cta;
   return MGCD_OK;
 }
 
@@ -548,23 +580,12 @@ static int launch_set(mgcd_context* c, const std::vector<Bucket>& buckets, const
 
   if (!grid_pairs.empty()) {
     GridSync* hs = c->h_gsync.as<GridSync>();
+    std::memset(hs, 0, sizeof(GridSync));
     hs->slot[0] = hs->slot[1] = hs->slot[2] = ~0ull;
-    hs->arrive = 0;
-    hs->error = 0;
-    hs->timeout_ns = (unsigned long long)env_int("MGCD_WAIT_TIMEOUT_MS", 2000) * 1000000ull;
-    const uint32_t per_default = (uint32_t)env_int("MGCD_GRID_PER_CTA", GRID_THREADS);
+    hs->timeout_ns = c->wait_timeout_ns;
+    hs->withhold_cta = c->withhold_cta;
     for (uint32_t k : grid_pairs) {
       const PairDesc& d = descs[k];
-      uint32_t per = std::max<uint32_t>(per_default, 32);
-      int bps = 0;
-      if (grid_max_blocks_per_sm(grid_smem_bytes(per), &bps) != cudaSuccess || bps < 1) return MGCD_ERR_GRID;
-      uint32_t grid = (d.nq + per - 1) / per;
-      if (grid > (uint32_t)(c->sms * bps)) {
-        per = (d.nq + c->sms * bps - 1) / (c->sms * bps);
-        if (grid_max_blocks_per_sm(grid_smem_bytes(per), &bps) != cudaSuccess || bps < 1) return MGCD_ERR_GRID;
-        grid = (d.nq + per - 1) / per;
-        if (grid > (uint32_t)(c->sms * bps)) return MGCD_ERR_GRID;
-      }
       GridArgs g;
       g.inv = InvTab{c->d_invtab.as<uint32_t>(), c->invtab_n};
       g.limbs = c->d_limbs.as<uint32_t>();
@@ -572,14 +593,39 @@ static int launch_set(mgcd_context* c, const std::vector<Bucket>& buckets, const
       g.mods = c->mods.as<ModConst>();
       g.L = c->L;
       g.scratch = c->d_scratch.as<uint32_t>() + c->grid_scratch_off;
-      g.sync = c->d_gsync.as<GridSync>();
-      g.per_cta = per;
       g.digits = c->d_digits.as<mgcd_pair>();
       g.count = c->d_count.as<uint32_t>() + k;
       g.iters = c->d_iters.as<uint32_t>() + k;
       g.status = c->d_status.as<int32_t>() + k;
+      const bool ref_shape = c->single_policy == MGCD_SINGLE_REFERENCE_SHAPE;
+      if (!ref_shape && d.nq <= (uint32_t)MAX_CLUSTER * 1024) {
+        // thread-block cluster: as many CTAs (<= 16) as keep one modulus per thread
+        const int ctas = (int)std::min<uint32_t>(MAX_CLUSTER, (d.nq + 255) / 256);
+        const uint32_t per = (d.nq + ctas - 1) / ctas;
+        const int threads = per <= 256 ? 256 : per <= 512 ? 512 : 1024;
+        g.per_cta = per;
+        g.sync = nullptr;
+        if (launch_cluster(g, threads, ctas, grid_smem_bytes(per), c->stream) != cudaSuccess) return MGCD_ERR_GRID;
+        ++c->launches;
+        continue;
+      }
+      // cooperative grid: one CTA per SM (or the reference's shape: 256-thread CTAs, 256 moduli)
+      const int threads = ref_shape ? 256 : GRID_THREADS;
+      uint32_t per = ref_shape ? 256u : std::max<uint32_t>(32, (d.nq + c->sms - 1) / c->sms);
+      int bps = 0;
+      if (grid_max_blocks_per_sm(threads, grid_smem_bytes(per), &bps) != cudaSuccess || bps < 1) return MGCD_ERR_GRID;
+      uint32_t grid = (d.nq + per - 1) / per;
+      if (grid > (uint32_t)(c->sms * bps)) {
+        per = (d.nq + c->sms * bps - 1) / (c->sms * bps);
+        grid = (d.nq + per - 1) / per;
+        if (grid_max_blocks_per_sm(threads, grid_smem_bytes(per), &bps) != cudaSuccess ||
+            grid > (uint32_t)(c->sms * bps))
+          return MGCD_ERR_GRID;
+      }
+      g.per_cta = per;
+      g.sync = c->d_gsync.as<GridSync>();
       CK(cudaMemcpyAsync(c->d_gsync.p, hs, sizeof(GridSync), cudaMemcpyHostToDevice, c->stream));
-      cudaError_t e = launch_grid(g, (int)grid, grid_smem_bytes(per), c->stream);
+      cudaError_t e = launch_grid(g, threads, (int)grid, grid_smem_bytes(per), c->stream);
       if (e == cudaErrorCooperativeLaunchTooLarge) return MGCD_ERR_GRID;
       if (e != cudaSuccess) return MGCD_ERR_CUDA;
       ++c->launches;

@@ -56,11 +56,16 @@ struct BatchArgs {
 };
 
 // State of the cross-CTA reduction used by a single pair spread over a cooperative grid.
+// Exchange e: thread 0 of every CTA folds its minimum into slot[e % 3] (atomic min) and
+// arrives on a monotonic counter; CTAs wait (bounded) for e + 1 full rounds of arrivals,
+// then read the slot.  CTA 0 resets slot[(e + 1) % 3] before arriving: all CTAs have read
+// that slot (exchange e - 2) once CTA 0 is past exchange e - 1.
 struct GridSync {
-  unsigned long long slot[3];
+  unsigned long long slot[3];              // ~0 before use
   unsigned int arrive;
-  unsigned int error;
-  unsigned long long timeout_ns;
+  unsigned int error;                      // set by the first CTA whose wait expired
+  unsigned int withhold_cta;               // test hook: this CTA never publishes (0xFFFFFFFF: none)
+  unsigned long long timeout_ns;           // bound of every wait
 };
 
 struct GridArgs {
@@ -85,10 +90,15 @@ size_t batch_smem_bytes(int threads, int k, uint32_t nq_max);
 cudaError_t batch_max_blocks_per_sm(int threads, int k, size_t smem, int* blocks);
 cudaError_t launch_batch(const BatchArgs& a, int threads, int k, int grid, size_t smem, cudaStream_t s);
 
+// One pair on a cluster of `ctas` CTAs (<= 16) of `threads` threads; same arguments and
+// shared-memory size as the grid path.
+cudaError_t launch_cluster(const GridArgs& a, int threads, int ctas, size_t smem, cudaStream_t s);
+
 size_t grid_smem_bytes(uint32_t per_cta);
-cudaError_t grid_max_blocks_per_sm(size_t smem, int* blocks);
-constexpr int GRID_THREADS = 1024;
-cudaError_t launch_grid(const GridArgs& a, int grid, size_t smem, cudaStream_t s);
+constexpr int GRID_THREADS = 1024;   // CTA size of the grid path (256 for the reference's shape)
+constexpr int MAX_CLUSTER = 16;      // largest thread-block cluster (non-portable size)
+cudaError_t grid_max_blocks_per_sm(int threads, size_t smem, int* blocks);
+cudaError_t launch_grid(const GridArgs& a, int threads, int grid, size_t smem, cudaStream_t s);
 
 // 256-thread blocks, 8 IMADs per thread per iteration.
 cudaError_t launch_int_peak(uint32_t* out, int blocks, int iters, cudaStream_t s);

@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(T) batch_kernel(const BatchArgs a)
     if (k >= a.npairs) break;
     const uint32_t pi = a.order[k];
     const PairDesc d = a.pairs[pi];
-    run_pair<T, false>(a.limbs, d, a.mods, a.L, 0u, d.nq, st, acc2, chunk, rs, u0, v0, hist, nullptr,
+    run_pair<T, SYNC_CTA>(a.limbs, d, a.mods, a.L, 0u, d.nq, st, acc2, chunk, rs, u0, v0, hist, nullptr,
                        a.digits, a.count + pi, a.iters + pi, a.status + pi, a.inv);
     __syncthreads();
   }
@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(T, MINB) batchk_kernel(const BatchArgs a)
         if (threadIdx.x == 0) { a.status[pi] = ST_REDUX; a.count[pi] = 0; }
       } else {
         uint32_t* u0 = scr + (size_t)s * 4 * NQS;
-        finish_pair<T, false>(a.mods, ss.d[s], L, 0u, ss.d[s].nq, tS + (size_t)s * NQS, rs, rparity, repoch, nullptr,
+        finish_pair<T, SYNC_CTA>(a.mods, ss.d[s], L, 0u, ss.d[s].nq, tS + (size_t)s * NQS, rs, rparity, repoch, nullptr,
                               u0, u0 + NQS, reinterpret_cast<const int2*>(u0 + 2 * (size_t)NQS), it, pick(rem, s),
                               ss.lu[s], ss.lv[s], a.digits, a.count + pi, a.status + pi, a.inv);
       }
@@ -270,7 +270,8 @@ __global__ void __launch_bounds__(T, MINB) batchk_kernel(const BatchArgs a)
 
 // One pair over a cooperative grid of GRID_THREADS-thread CTAs; CTA c owns moduli
 // [c * per_cta, min(nq, (c + 1) * per_cta)).
-__global__ void __launch_bounds__(GRID_THREADS) grid_kernel(const GridArgs a)
+template <int T>
+__global__ void __launch_bounds__(T) grid_kernel(const GridArgs a)
 {
   extern __shared__ __align__(16) uint32_t smem[];
   __shared__ RedSmem rs;
@@ -283,8 +284,32 @@ __global__ void __launch_bounds__(GRID_THREADS) grid_kernel(const GridArgs a)
   uint32_t* u0 = a.scratch + j0;
   uint32_t* v0 = a.scratch + nq + j0;
   int2* hist = reinterpret_cast<int2*>(a.scratch + 2 * (size_t)nq);
-  run_pair<GRID_THREADS, true>(a.limbs, a.pair, a.mods, a.L, j0, nloc, st, acc2, chunk, rs, u0, v0, hist,
+  run_pair<T, SYNC_GRID>(a.limbs, a.pair, a.mods, a.L, j0, nloc, st, acc2, chunk, rs, u0, v0, hist,
                                a.sync, a.digits, a.count, a.iters, a.status, a.inv);
+}
+
+// One pair over a thread-block cluster (up to 16 CTAs, one per SM); CTA r owns moduli
+// [r * per_cta, min(nq, (r + 1) * per_cta)).  Pivot keys travel through distributed shared
+// memory; each reduction is one hardware cluster barrier (no global-memory round trip).
+template <int T>
+__global__ void __launch_bounds__(T) cluster_kernel(const GridArgs a)
+{
+  extern __shared__ __align__(16) uint32_t smem[];
+  __shared__ RedSmem rs;
+  __shared__ ClusterSmem cs;
+  const uint32_t nq = a.pair.nq;
+  const uint32_t j0 = cluster_rank() * a.per_cta;
+  const uint32_t nloc = j0 >= nq ? 0u : (nq - j0 < a.per_cta ? nq - j0 : a.per_cta);
+  uint32_t* st = smem;
+  uint32_t* acc2 = smem + a.per_cta;
+  uint32_t* chunk = acc2 + a.per_cta;
+  uint32_t* u0 = a.scratch + j0;
+  uint32_t* v0 = a.scratch + nq + j0;
+  int2* hist = reinterpret_cast<int2*>(a.scratch + 2 * (size_t)nq);
+  cluster_sync_all();   // every CTA of the cluster is running before remote stores begin
+  run_pair<T, SYNC_CLUSTER>(a.limbs, a.pair, a.mods, a.L, j0, nloc, st, acc2, chunk, rs, u0, v0, hist,
+                            reinterpret_cast<GridSync*>(&cs), a.digits, a.count, a.iters, a.status, a.inv);
+  cluster_sync_all();   // no CTA leaves while others may still address its shared memory
 }
 
 // Integer-pipe microbenchmark: eight independent IMAD chains per thread.
@@ -383,26 +408,73 @@ cudaError_t launch_batch(const BatchArgs& a, int threads, int k, int grid, size_
   return cudaLaunchKernel(fn, dim3(grid), dim3(threads), args, smem, s);
 }
 
+static const void* cluster_fn(int threads)
+{
+  switch (threads) {
+    case 256: return reinterpret_cast<const void*>(&cluster_kernel<256>);
+    case 512: return reinterpret_cast<const void*>(&cluster_kernel<512>);
+    case 1024: return reinterpret_cast<const void*>(&cluster_kernel<1024>);
+    default: return nullptr;
+  }
+}
+
+cudaError_t launch_cluster(const GridArgs& a, int threads, int ctas, size_t smem, cudaStream_t s)
+{
+  const void* fn = cluster_fn(threads);
+  if (!fn || ctas < 1 || ctas > MAX_CLUSTER) return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  if (ctas > 8) {
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return e;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(ctas);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = ctas;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  void* args[] = {const_cast<GridArgs*>(&a)};
+  return cudaLaunchKernelExC(&cfg, fn, args);
+}
+
 size_t grid_smem_bytes(uint32_t per_cta)
 {
   return sizeof(uint32_t) * (2 * (size_t)per_cta + CHUNK);
 }
 
-cudaError_t grid_max_blocks_per_sm(size_t smem, int* blocks)
+static const void* grid_fn(int threads)
 {
-  const void* fn = reinterpret_cast<const void*>(&grid_kernel);
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, fn, GRID_THREADS, smem);
+  switch (threads) {
+    case 256: return reinterpret_cast<const void*>(&grid_kernel<256>);
+    case 1024: return reinterpret_cast<const void*>(&grid_kernel<1024>);
+    default: return nullptr;
+  }
 }
 
-cudaError_t launch_grid(const GridArgs& a, int grid, size_t smem, cudaStream_t s)
+cudaError_t grid_max_blocks_per_sm(int threads, size_t smem, int* blocks)
 {
-  const void* fn = reinterpret_cast<const void*>(&grid_kernel);
+  const void* fn = grid_fn(threads);
+  if (!fn) return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, fn, threads, smem);
+}
+
+cudaError_t launch_grid(const GridArgs& a, int threads, int grid, size_t smem, cudaStream_t s)
+{
+  const void* fn = grid_fn(threads);
+  if (!fn) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   void* args[] = {const_cast<GridArgs*>(&a)};
-  return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(GRID_THREADS), args, smem, s);
+  return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(threads), args, smem, s);
 }
 
 }  // namespace mgcd

@@ -12,12 +12,76 @@ namespace mgcd {
 
 constexpr int CHUNK = 1024;  // operand limbs staged per residue pass
 
+// How the CTAs that share one pair synchronise.
+enum SyncMode : int {
+  SYNC_CTA = 0,      // the pair lives in one CTA
+  SYNC_CLUSTER = 1,  // the pair spans a thread-block cluster: DSMEM exchange + barrier.cluster
+  SYNC_GRID = 2      // the pair spans a cooperative grid: global-memory exchange, bounded wait
+};
+
 struct RedSmem {
   unsigned long long key[2][32];  // per-warp minima, double-buffered by parity
   unsigned long long bcast;       // grid mode: the grid-wide result
   uint32_t bad;                   // grid mode: a bounded wait expired
   uint32_t cert;                  // the result could not be certified (more moduli needed)
 };
+
+// Cluster mode: every warp's minimum lands in every CTA of the cluster, so one cluster
+// barrier per reduction suffices.  Double-buffered by parity.
+struct ClusterSmem {
+  unsigned long long key[2][MAX_CLUSTER][32];
+};
+
+__device__ __forceinline__ uint32_t cluster_rank()
+{
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+__device__ __forceinline__ uint32_t cluster_size()
+{
+  uint32_t n;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(n));
+  return n;
+}
+
+__device__ __forceinline__ void cluster_sync_all()
+{
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// Stores v at the same shared-memory offset as *local in CTA `rank` of this cluster.
+__device__ __forceinline__ void st_cluster_u64(unsigned long long* local, uint32_t rank, unsigned long long v)
+{
+  const uint32_t a = (uint32_t)__cvta_generic_to_shared(local);
+  uint32_t ra;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
+  asm volatile("st.shared::cluster.u64 [%0], %1;" :: "r"(ra), "l"(v) : "memory");
+}
+
+// Minimum over the whole cluster: each warp's minimum is written into every CTA's
+// slots, one cluster barrier, then each warp reduces all slots locally.
+template <int T>
+__device__ __forceinline__ void cluster_min_key(uint32_t& hi, uint32_t& lo, ClusterSmem& cs, uint32_t& parity)
+{
+  constexpr int NW = T / 32;
+  const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+  const uint32_t me = cluster_rank(), nc = cluster_size();
+  warp_min_key(hi, lo);
+  const unsigned long long k = ((unsigned long long)hi << 32) | lo;
+  if (lane < nc) st_cluster_u64(&cs.key[parity][me][w], lane, k);   // lane r writes into CTA r
+  cluster_sync_all();
+  unsigned long long m = ~0ull;
+  for (uint32_t e = lane; e < nc * NW; e += 32) {
+    const unsigned long long x = cs.key[parity][e / NW][e % NW];
+    m = x < m ? x : m;
+  }
+  hi = (uint32_t)(m >> 32);
+  lo = (uint32_t)m;
+  warp_min_key(hi, lo);
+  parity ^= 1u;
+}
 
 static __device__ __forceinline__ unsigned long long globaltimer_ns()
 {
@@ -37,6 +101,13 @@ static __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsign
 {
   unsigned long long v;
   asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+static __device__ __forceinline__ unsigned int ld_relaxed_u32(const unsigned int* p)
+{
+  unsigned int v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
 
@@ -64,25 +135,31 @@ __device__ __forceinline__ void block_min_key(uint32_t& hi, uint32_t& lo, RedSme
 // all CTAs of this epoch arrived.  CTA 0 clears the slot of epoch + 1 before arriving:
 // every CTA has finished reading that slot (epoch - 2) once CTA 0 is past epoch - 1.
 // Returns false if the wait expired (the grid then unwinds; the host sees ST_TIMEOUT).
-template <int T, bool GRID>
+template <int T, int MODE>
 __device__ __forceinline__ bool reduce_min(uint32_t& hi, uint32_t& lo, RedSmem& rs, uint32_t& parity,
                                            GridSync* gs, uint32_t& epoch)
 {
+  if constexpr (MODE == SYNC_CLUSTER) {
+    cluster_min_key<T>(hi, lo, *reinterpret_cast<ClusterSmem*>(gs), parity);
+    return true;
+  }
   block_min_key<T>(hi, lo, rs, parity);
-  if constexpr (!GRID) {
+  if constexpr (MODE == SYNC_CTA) {
     return true;
   } else {
     if (threadIdx.x == 0) {
       const uint32_t s = epoch % 3u;
-      atomicMin(&gs->slot[s], ((unsigned long long)hi << 32) | lo);
-      if (blockIdx.x == 0) gs->slot[(epoch + 1u) % 3u] = ~0ull;
-      __threadfence();
-      atomicAdd(&gs->arrive, 1u);
+      uint32_t bad = 0;
+      if (blockIdx.x != gs->withhold_cta) {
+        atomicMin(&gs->slot[s], ((unsigned long long)hi << 32) | lo);
+        if (blockIdx.x == 0) gs->slot[(epoch + 1u) % 3u] = ~0ull;
+        __threadfence();
+        atomicAdd(&gs->arrive, 1u);
+      }
       const unsigned int target = (epoch + 1u) * gridDim.x;
       const unsigned long long t0 = globaltimer_ns();
-      uint32_t bad = 0;
       while (ld_acquire_u32(&gs->arrive) < target) {
-        if (*(volatile unsigned int*)&gs->error) { bad = 1; break; }
+        if (ld_relaxed_u32(&gs->error)) { bad = 1; break; }
         if (globaltimer_ns() - t0 > gs->timeout_ns) { atomicExch(&gs->error, 1u); bad = 1; break; }
       }
       rs.bcast = bad ? ~0ull : ld_relaxed_u64(&gs->slot[s]);
@@ -127,7 +204,7 @@ __device__ void residues(const uint32_t* __restrict__ x, uint32_t n, const ModCo
   __syncthreads();
 }
 
-template <int T, bool GRID>
+template <int T, int MODE>
 __device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d, int L, uint32_t j0, uint32_t nloc,
                             uint32_t* st, RedSmem& rs, uint32_t& parity, uint32_t& epoch, GridSync* gs,
                             const uint32_t* u0g, const uint32_t* v0g, const int2* hist, uint32_t iters, int remaining,
@@ -139,14 +216,14 @@ __device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d
 //   st, acc2   shared arrays of nloc words; chunk: CHUNK words
 //   u0g, v0g   this CTA's initial residues (global scratch, nloc words each)
 //   hist       (p, b) history, one entry per reduction iteration (global scratch, nq entries)
-template <int T, bool GRID>
+template <int T, int MODE>
 __device__ void run_pair(const uint32_t* __restrict__ limbs, const PairDesc& d, const ModConst* __restrict__ mods,
                          int L, uint32_t j0, uint32_t nloc, uint32_t* st, uint32_t* acc2, uint32_t* chunk,
                          RedSmem& rs, uint32_t* u0g, uint32_t* v0g, int2* hist, GridSync* gs,
                          mgcd_pair* digits, uint32_t* count, uint32_t* iters_out, int32_t* status,
                          InvTab inv)
 {
-  const bool writer = threadIdx.x == 0 && (!GRID || blockIdx.x == 0);
+  const bool writer = threadIdx.x == 0 && (MODE == SYNC_CTA || blockIdx.x == 0);
   const ModConst* __restrict__ my = mods + j0;
   uint32_t parity = 0, epoch = 0;
 
@@ -166,7 +243,7 @@ __device__ void run_pair(const uint32_t* __restrict__ limbs, const PairDesc& d, 
     t_key(t, c.q, h, l);
     if (key_less(h, l, kh, kl)) { kh = h; kl = l; }
   }
-  if (!reduce_min<T, GRID>(kh, kl, rs, parity, gs, epoch)) {
+  if (!reduce_min<T, MODE>(kh, kl, rs, parity, gs, epoch)) {
     if (writer) *status = ST_TIMEOUT;
     return;
   }
@@ -219,28 +296,28 @@ __device__ void run_pair(const uint32_t* __restrict__ limbs, const PairDesc& d, 
       if (writer) { *status = ST_REDUX; *count = 0; }
       return;
     }
-    if (!reduce_min<T, GRID>(kh, kl, rs, parity, gs, epoch)) {
+    if (!reduce_min<T, MODE>(kh, kl, rs, parity, gs, epoch)) {
       if (writer) *status = ST_TIMEOUT;
       return;
     }
     key_pair(kh, kl, p, b);
   }
   if (writer) *iters_out = iters;
-  finish_pair<T, GRID>(mods, d, L, j0, nloc, st, rs, parity, epoch, gs, u0g, v0g, hist, iters, remaining, lu, lv,
+  finish_pair<T, MODE>(mods, d, L, j0, nloc, st, rs, parity, epoch, gs, u0g, v0g, hist, iters, remaining, lu, lv,
                        digits, count, status, inv);
 }
 
 // After the reduction loop of one pair: certification, replay and recovery (MGCD4).
 // st holds the final t states of this CTA's moduli; `remaining` the surviving count;
 // lu, lv (meaningful in thread 0) the size bounds of the final u and v.
-template <int T, bool GRID>
+template <int T, int MODE>
 __device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d, int L, uint32_t j0, uint32_t nloc,
                             uint32_t* st, RedSmem& rs, uint32_t& parity, uint32_t& epoch, GridSync* gs,
                             const uint32_t* u0g, const uint32_t* v0g, const int2* hist, uint32_t iters, int remaining,
                             double lu, double lv, mgcd_pair* digits, uint32_t* count, int32_t* status,
                             InvTab inv)
 {
-  const bool writer = threadIdx.x == 0 && (!GRID || blockIdx.x == 0);
+  const bool writer = threadIdx.x == 0 && (MODE == SYNC_CTA || blockIdx.x == 0);
   const ModConst* __restrict__ my = mods + j0;
   uint32_t p, kh, kl;
   // Certify the result: all surviving residues of v are 0, so v = 0 if the surviving
@@ -250,7 +327,7 @@ __device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d
     const double cap = (double)remaining * (double)(L - 1);
     rs.cert = (cap > lu + 2.0 && cap > lv + 1.0) ? 0u : 1u;
   }
-  if constexpr (GRID) __threadfence();
+  if constexpr (MODE == SYNC_GRID) __threadfence();
   __syncthreads();
   if (rs.cert) {
     if (writer) { *status = ST_INSUFFICIENT; *count = 0; }
@@ -286,7 +363,7 @@ __device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d
     const uint32_t u = st[j];
     if (u != U_RETIRED && u != 0u) { kh = j0 + j; kl = (uint32_t)to_signed(u, my[j].q); break; }
   }
-  if (!reduce_min<T, GRID>(kh, kl, rs, parity, gs, epoch)) {
+  if (!reduce_min<T, MODE>(kh, kl, rs, parity, gs, epoch)) {
     if (writer) *status = ST_TIMEOUT;
     return;
   }
@@ -315,7 +392,7 @@ __device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d
     ++ndig;
     remaining -= 1;
     if (remaining <= 0) break;
-    if (!reduce_min<T, GRID>(kh, kl, rs, parity, gs, epoch)) {
+    if (!reduce_min<T, MODE>(kh, kl, rs, parity, gs, epoch)) {
       if (writer) *status = ST_TIMEOUT;
       return;
     }

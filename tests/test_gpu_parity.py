@@ -138,6 +138,29 @@ def test_large_pairs_cooperative_grid(device):
     assert device.gcd_batch([u2, u], [v2, v]) == [math.gcd(u2, v2), math.gcd(u, v)]
 
 
+def test_single_pair_launch_shapes_agree(mgcd, oracle):
+    """Cluster (DSMEM exchange), cooperative grid and the reference's launch shape give
+    the oracle's digits."""
+    rng = random.Random(17)
+    mod32 = oracle.gen_moduli(32, 8192)
+    with mgcd.Device(0, 32) as dev:
+        for nbits, gbits in [(3000, 700), (20000, 5000), (60000, 15000)]:
+            u, v = rand_pair(rng, nbits, gbits)
+            uu, vv = max(u, v), min(u, v)
+            nq = oracle.num_moduli_needed(uu.bit_length(), 32)
+            st, dig, _, _ = oracle.modgcd(uu, vv, 32, mod32, nq)
+            assert st == 0
+            dev.set_single_pair_policy(0)
+            assert dev.gcd_digits(u, v) == dig
+            dev.set_single_pair_policy(1)
+            assert dev.gcd_digits(u, v) == dig
+        u, v = rand_pair(rng, 300000, 80000)                  # > 16 x 1024 moduli: grid
+        g = math.gcd(u, v)
+        for pol in (0, 1):
+            dev.set_single_pair_policy(pol)
+            assert dev.gcd(u, v) == g
+
+
 def test_not_enough_moduli(mgcd):
     with mgcd.Device(0, 22) as dev:
         x = (1 << 1_300_000) + 1

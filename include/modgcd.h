@@ -148,12 +148,24 @@ int mgcd_test_withhold_cta(mgcd_context *ctx, int cta);
    moduli (a multiple of 256; 0 restores the reference's count) and is not rerun. */
 int mgcd_test_force_moduli(mgcd_context *ctx, unsigned nq);
 /* Launch configuration of one size class of the batched path: class 0 = pairs needing
-   <= 1,024 moduli, 1 = <= 4,096, 2 = larger (up to 16,384; beyond that a pair runs on a
-   cooperative grid).  threads: CTA size (256, 512, 1024); k: pairs one CTA runs in
-   lockstep, sharing one modular inverse per modulus and iteration (1, 2, or 4 with
-   threads <= 512); nq_scale as above.  The autotuner writes these. */
+   <= 1,024 moduli, 1 = <= 4,096, 2 = <= 16,384 (one CTA per pair), 3 = larger (one
+   thread-block cluster per pair).  threads: CTA size (256, 512, 1024); k: pairs one CTA
+   runs in lockstep, sharing one modular inverse per modulus and iteration (1, 2, or 4 with
+   threads <= 512; 1 for class 3); nq_scale as above.  The autotuner writes these. */
+#define MGCD_NUM_SIZE_CLASSES 4
 int mgcd_set_size_class(mgcd_context *ctx, int cls, int threads, int k, float nq_scale);
 int mgcd_get_size_class(const mgcd_context *ctx, int cls, int *threads, int *k, float *nq_scale);
+/* CTAs per thread-block cluster of size class 3 (2..16, default 8; raised automatically
+   when a pair's share of moduli would not fit one CTA's shared memory). */
+int mgcd_set_cluster_size(mgcd_context *ctx, int ctas);
+int mgcd_get_cluster_size(const mgcd_context *ctx, int *ctas);
+/* Records the GPU work of a batch (status reset, queue resets, one persistent kernel per
+   size class on its own stream) into a CUDA graph at the first mgcd_batch_run after an
+   upload; every later mgcd_batch_run of the same upload is one graph launch.  The graph
+   is rebuilt after the next upload (or a change of the wait bound); enable = 0 returns to
+   direct launches.  Per-kernel times (mgcd_batch_kernel_stats) exist only for direct
+   launches. */
+int mgcd_batch_use_graph(mgcd_context *ctx, int enable);
 /* Per kernel of the last run (i < number of size classes present, largest first): its
    size class, pair count and device time (the time includes waiting for SMs that other
    concurrently running classes hold). */
@@ -192,8 +204,9 @@ int mgcd_int_peak(mgcd_context *ctx, double *int_ops_per_s);
    overlap on the GPU race and must be serialised by the caller. */
 int mgcd_gcd_digits_noalloc(const uint32_t *d_limbs, size_t uSz, size_t vSz, mgcd_pair *d_digits, size_t cap,
                             uint32_t *d_count, int32_t *d_status, void *stream);
-/* Total work of the uploaded batch by the algorithmic cost model (see DESIGN): residue
-   limb steps, reduction-loop updates and recovery updates, after a run completed. */
+/* Total work of the uploaded batch by the algorithmic cost model, after a run completed:
+   residue limb steps (N_Q x operand limbs), reduction-loop updates (sum over iterations of
+   the surviving moduli), recovery updates (the same over digits) and operand bytes. */
 int mgcd_batch_work(const mgcd_context *ctx, double *residue_steps, double *euclid_updates,
                     double *recovery_updates, double *operand_bytes);
 

@@ -70,6 +70,9 @@ SIGNATURES = {
     "mgcd_batch_kernel_stats": (_c.c_int, [_P, _c.c_int, _c.POINTER(_c.c_int), _c.POINTER(_c.c_int),
                                            _c.POINTER(_c.c_float)]),
     "mgcd_batch_retried": (_c.c_int, [_P, _c.POINTER(_c.c_int)]),
+    "mgcd_set_cluster_size": (_c.c_int, [_P, _c.c_int]),
+    "mgcd_get_cluster_size": (_c.c_int, [_P, _c.POINTER(_c.c_int)]),
+    "mgcd_batch_use_graph": (_c.c_int, [_P, _c.c_int]),
 }
 
 _lib = None
@@ -281,8 +284,22 @@ class Device:
         _check(self._lib.mgcd_set_nq_scale(self._h, float(scale)))
 
     def set_size_class(self, cls, threads, k, nq_scale):
-        """Launch configuration of size class cls (0: <= 1024 moduli, 1: <= 4096, 2: larger)."""
+        """Launch configuration of size class cls (0: <= 1024 moduli, 1: <= 4096,
+        2: <= 16384, 3: larger, one thread-block cluster per pair)."""
         _check(self._lib.mgcd_set_size_class(self._h, int(cls), int(threads), int(k), float(nq_scale)))
+
+    def set_cluster_size(self, ctas):
+        """CTAs per cluster of size class 3."""
+        _check(self._lib.mgcd_set_cluster_size(self._h, int(ctas)))
+
+    def get_cluster_size(self):
+        n = ctypes.c_int()
+        _check(self._lib.mgcd_get_cluster_size(self._h, ctypes.byref(n)))
+        return n.value
+
+    def batch_use_graph(self, enable=True):
+        """Record each upload's GPU work into a CUDA graph and replay it on every run."""
+        _check(self._lib.mgcd_batch_use_graph(self._h, 1 if enable else 0))
 
     def set_single_pair_policy(self, policy):
         """0: cluster / grid (default); 1: the reference's launch shape (grid of 256-thread CTAs)."""

@@ -78,15 +78,19 @@ struct HostBuf {
 
 struct Bucket {
   int threads, k;      // CTA size, pairs per CTA in lockstep
+  int csize;           // CTAs per thread-block cluster (0: one CTA per pair)
   int cls;             // size class
   uint32_t first, n, nq_max;
-  int grid;
+  int grid;            // CTAs (csize = 0) or clusters
   size_t smem;
   size_t scratch_off;  // words
 };
 
-constexpr int NSTREAMS = 3;
-constexpr uint32_t CTA_MAX_NQ = 16384;   // larger pairs go to the cooperative grid
+// Size classes of the batched path, one persistent kernel (and stream) each: pairs with at
+// most 1,024 / 4,096 / 16,384 moduli run one per CTA; larger pairs one per cluster.
+constexpr int NSTREAMS = 4;
+constexpr int CLUSTER_CLASS = 3;
+constexpr uint32_t CTA_MAX_NQ = 16384;
 constexpr size_t INVTAB_N = 16384;        // moduli covered by the pairwise inverse table
 
 int env_int(const char* name, int dflt)
@@ -107,8 +111,7 @@ int to_status(int32_t st)
   }
 }
 
-// Size class of a pair by its moduli count: <= 1024, <= 4096, larger.
-int size_class(uint32_t nq) { return nq <= 1024 ? 0 : nq <= 4096 ? 1 : 2; }
+int size_class(uint32_t nq) { return nq <= 1024 ? 0 : nq <= 4096 ? 1 : nq <= CTA_MAX_NQ ? 2 : CLUSTER_CLASS; }
 
 size_t strip(const uint32_t* x, size_t n)
 {
@@ -128,6 +131,7 @@ int cmp_mag(const uint32_t* a, size_t na, const uint32_t* b, size_t nb)
 
 struct mgcd_context {
   int device = 0, L = 32, sms = 0;
+  size_t smem_optin = 0;               // largest dynamic shared memory per CTA
   cudaStream_t stream = nullptr;
   cudaStream_t bstream[NSTREAMS] = {};
   cudaEvent_t ev_start = nullptr, ev_b[NSTREAMS] = {};
@@ -147,13 +151,18 @@ struct mgcd_context {
   bool plain = false;                  // single-pair latency policy
 
   DevBuf d_limbs, d_pairs, d_order, d_digits, d_count, d_iters, d_status, d_queue, d_scratch, d_gsync;
-  HostBuf h_count, h_iters, h_status, h_digits, h_gsync;
+  HostBuf h_count, h_iters, h_status, h_digits;
   int launches = 0;
   bool ran = false;
   double work[4] = {0, 0, 0, 0};
-  // Per size class of the batched path (reference moduli count <= 1024, <= 4096, larger):
-  // CTA size, pairs per CTA in lockstep, fraction of the reference moduli count.
-  struct { int threads, k; float nq_scale; } cfg[NSTREAMS] = {{256, 4, 1.0f}, {512, 4, 1.0f}, {1024, 2, 1.0f}};
+  // Per size class of the batched path: CTA size, pairs per CTA in lockstep, fraction of
+  // the reference moduli count, CTAs per cluster (cluster class only).
+  struct { int threads, k; float nq_scale; int csize; } cfg[NSTREAMS] = {
+      {256, 4, 1.0f, 0}, {512, 4, 1.0f, 0}, {1024, 2, 1.0f, 0}, {1024, 1, 1.0f, 8}};
+  // CUDA graph of the plan's GPU work (mgcd_batch_use_graph); rebuilt after every upload
+  bool use_graph = false, bucket_timed = false;
+  cudaGraphExec_t graph = nullptr;
+  int graph_kernels = 0;
   std::vector<uint32_t> ref_nq, eff_nq; // per GPU pair: reference count, count of the final run
   int retried = 0;
   bool synced = false;
@@ -174,6 +183,15 @@ struct mgcd_context {
     cudaError_t e_ = (call);                         \
     if (e_ != cudaSuccess) return MGCD_ERR_CUDA;     \
   } while (0)
+
+// The recorded graph holds device pointers and launch parameters of the current plan:
+// dropped whenever a buffer it uses moves or a captured parameter changes.
+static void drop_graph(mgcd_context* c)
+{
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  c->graph = nullptr;
+  c->graph_kernels = 0;
+}
 
 extern "C" {
 
@@ -238,6 +256,7 @@ int mgcd_create(int device, int L, mgcd_context** out)
   c->device = device;
   c->L = L;
   c->sms = prop.multiProcessorCount;
+  c->smem_optin = prop.sharedMemPerBlockOptin;
   // Table size: enough moduli for ~1.2M-bit operands at every width (L = 22 is limited by
   // the 97,358 usable 22-bit primes).
   const size_t want = (L == 22) ? 97280 : 131072;
@@ -283,10 +302,11 @@ int mgcd_destroy(mgcd_context* c)
   if (!c) return MGCD_ERR_INVALID_ARG;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  drop_graph(c);
   for (DevBuf* b : {&c->mods, &c->d_limbs, &c->d_pairs, &c->d_order, &c->d_digits, &c->d_count, &c->d_iters,
                     &c->d_status, &c->d_queue, &c->d_scratch, &c->d_gsync, &c->d_retry, &c->d_invtab})
     b->release();
-  for (HostBuf* b : {&c->h_count, &c->h_iters, &c->h_status, &c->h_digits, &c->h_gsync}) b->release();
+  for (HostBuf* b : {&c->h_count, &c->h_iters, &c->h_status, &c->h_digits}) b->release();
   for (int i = 0; i < NSTREAMS; ++i) {
     if (c->bstream[i]) cudaStreamDestroy(c->bstream[i]);
     if (c->ev_b[i]) cudaEventDestroy(c->ev_b[i]);
@@ -332,6 +352,8 @@ static int plan_batch(mgcd_context* c, size_t np, const uint32_t* limbs, const u
 {
   if (!c || (np && (!limbs || !u_off || !u_len || !v_off || !v_len))) return MGCD_ERR_INVALID_ARG;
   CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(c->stream));   // buffers below may be reallocated
+  drop_graph(c);
   c->np = np;
   c->plain = plain;
   c->ran = false;
@@ -404,7 +426,6 @@ static int plan_batch(mgcd_context* c, size_t np, const uint32_t* limbs, const u
   CK(c->d_queue.grow(2 * NSTREAMS * sizeof(uint32_t)));
   CK(c->d_scratch.grow(std::max<size_t>(scratch, 1) * sizeof(uint32_t)));
   CK(c->d_gsync.grow(sizeof(GridSync)));
-  CK(c->h_gsync.grow(sizeof(GridSync)));
   c->h2d_bytes = ng ? limb_end * sizeof(uint32_t) + ng * sizeof(PairDesc) + c->order.size() * sizeof(uint32_t) : 0;
   if (ng) {
     CK(cudaMemcpyAsync(c->d_limbs.p, limbs, limb_end * sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream));
@@ -416,8 +437,9 @@ static int plan_batch(mgcd_context* c, size_t np, const uint32_t* limbs, const u
   return MGCD_OK;
 }
 
-// Groups the pairs `subset` (indices into descs) into CTA-size buckets and cooperative-grid
-// pairs; appends the processing order to c->order and returns the scratch words needed.
+// Groups the pairs `subset` (indices into descs) into size-class buckets (batches) or
+// single-pair launches (plain); appends the processing order to c->order and returns the
+// scratch words needed.
 static int schedule(mgcd_context* c, const std::vector<PairDesc>& descs, const std::vector<uint32_t>& subset,
                     bool plain, std::vector<Bucket>& buckets, std::vector<uint32_t>& grid_pairs, size_t& scratch)
 {
@@ -429,8 +451,6 @@ static int schedule(mgcd_context* c, const std::vector<PairDesc>& descs, const s
     const uint32_t nq = descs[k].nq;
     if (plain) {
       if (nq <= plain_cta_max) byb[0].push_back(k); else grid_pairs.push_back(k);
-    } else if (nq > CTA_MAX_NQ) {
-      grid_pairs.push_back(k);
     } else {
       byb[size_class(nq)].push_back(k);
     }
@@ -451,16 +471,33 @@ static int schedule(mgcd_context* c, const std::vector<PairDesc>& descs, const s
     Bucket bk;
     bk.threads = plain ? 256 : kThreads[b];
     bk.k = plain ? 1 : kSlots[b];
+    bk.csize = 0;
     bk.cls = b;
     bk.first = (uint32_t)c->order.size();
     bk.n = (uint32_t)v.size();
     bk.nq_max = descs[v[0]].nq;
-    bk.smem = batch_smem_bytes(bk.threads, bk.k, bk.nq_max);
-    int bps = 0;
-    if (batch_max_blocks_per_sm(bk.threads, bk.k, bk.smem, &bps) != cudaSuccess || bps < 1) return MGCD_ERR_GRID;
-    bk.grid = (int)std::min<size_t>((v.size() + bk.k - 1) / bk.k, (size_t)c->sms * bps);
     bk.scratch_off = scratch;
-    scratch += (size_t)bk.grid * 4 * bk.k * bk.nq_max;
+    if (b == CLUSTER_CLASS) {
+      // one pair per cluster; more CTAs per cluster when a pair's share exceeds shared memory
+      int cs = c->cfg[b].csize;
+      while (cs < MAX_CLUSTER && cluster_batch_smem_bytes(cs, bk.nq_max) > c->smem_optin) cs *= 2;
+      cs = std::min(cs, MAX_CLUSTER);
+      bk.csize = cs;
+      bk.k = 1;
+      bk.smem = cluster_batch_smem_bytes(cs, bk.nq_max);
+      int nc = 0;
+      if (bk.smem > c->smem_optin || cluster_batch_max_clusters(bk.threads, cs, bk.smem, &nc) != cudaSuccess ||
+          nc < 1)
+        return MGCD_ERR_GRID;
+      bk.grid = (int)std::min<size_t>(v.size(), (size_t)nc);
+      scratch += (size_t)bk.grid * 4 * bk.nq_max;
+    } else {
+      bk.smem = batch_smem_bytes(bk.threads, bk.k, bk.nq_max);
+      int bps = 0;
+      if (batch_max_blocks_per_sm(bk.threads, bk.k, bk.smem, &bps) != cudaSuccess || bps < 1) return MGCD_ERR_GRID;
+      bk.grid = (int)std::min<size_t>((v.size() + bk.k - 1) / bk.k, (size_t)c->sms * bps);
+      scratch += (size_t)bk.grid * 4 * bk.k * bk.nq_max;
+    }
     c->order.insert(c->order.end(), v.begin(), v.end());
     buckets.push_back(bk);
   }
@@ -489,9 +526,36 @@ int mgcd_set_size_class(mgcd_context* c, int cls, int threads, int k, float nq_s
   if (!c || cls < 0 || cls >= NSTREAMS || !(nq_scale >= 0.5f && nq_scale <= 1.0f)) return MGCD_ERR_INVALID_ARG;
   if (threads != 256 && threads != 512 && threads != 1024) return MGCD_ERR_INVALID_ARG;
   if (k != 1 && k != 2 && !(k == 4 && threads <= 512)) return MGCD_ERR_INVALID_ARG;
+  if (cls == CLUSTER_CLASS && k != 1) return MGCD_ERR_INVALID_ARG;
   c->cfg[cls].threads = threads;
   c->cfg[cls].k = k;
   c->cfg[cls].nq_scale = nq_scale;
+  return MGCD_OK;
+}
+
+int mgcd_set_cluster_size(mgcd_context* c, int ctas)
+{
+  if (!c || ctas < 2 || ctas > MAX_CLUSTER) return MGCD_ERR_INVALID_ARG;
+  c->cfg[CLUSTER_CLASS].csize = ctas;
+  return MGCD_OK;
+}
+
+int mgcd_get_cluster_size(const mgcd_context* c, int* ctas)
+{
+  if (!c || !ctas) return MGCD_ERR_INVALID_ARG;
+  *ctas = c->cfg[CLUSTER_CLASS].csize;
+  return MGCD_OK;
+}
+
+int mgcd_batch_use_graph(mgcd_context* c, int enable)
+{
+  if (!c) return MGCD_ERR_INVALID_ARG;
+  c->use_graph = enable != 0;
+  if (!c->use_graph) {
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    drop_graph(c);
+  }
   return MGCD_OK;
 }
 
@@ -506,6 +570,8 @@ int mgcd_set_wait_timeout_ms(mgcd_context* c, unsigned ms)
 {
   if (!c || ms == 0) return MGCD_ERR_INVALID_ARG;
   c->wait_timeout_ns = (unsigned long long)ms * 1000000ull;
+  cudaStreamSynchronize(c->stream);
+  drop_graph(c);
   return MGCD_OK;
 }
 
@@ -520,6 +586,8 @@ int mgcd_test_withhold_cta(mgcd_context* c, int cta)
 {
   if (!c) return MGCD_ERR_INVALID_ARG;
   c->withhold_cta = cta < 0 ? 0xFFFFFFFFu : (uint32_t)cta;
+  cudaStreamSynchronize(c->stream);
+  drop_graph(c);
   return MGCD_OK;
 }
 
@@ -534,7 +602,7 @@ int mgcd_get_size_class(const mgcd_context* c, int cls, int* threads, int* k, fl
 
 int mgcd_batch_kernel_stats(const mgcd_context* c, int i, int* cls, int* pairs, float* ms)
 {
-  if (!c || !c->ran || i < 0 || i >= (int)c->buckets.size()) return MGCD_ERR_INVALID_ARG;
+  if (!c || !c->ran || !c->bucket_timed || i < 0 || i >= (int)c->buckets.size()) return MGCD_ERR_INVALID_ARG;
   float t = 0.f;
   CK(cudaEventElapsedTime(&t, c->t_b0[i], c->t_b1[i]));
   if (cls) *cls = c->buckets[i].cls;
@@ -571,7 +639,10 @@ static int launch_set(mgcd_context* c, const std::vector<Bucket>& buckets, const
     a.status = c->d_status.as<int32_t>();
     CK(cudaStreamWaitEvent(c->bstream[b], c->ev_start, 0));
     if (time_buckets) CK(cudaEventRecord(c->t_b0[b], c->bstream[b]));
-    CK(launch_batch(a, bk.threads, bk.k, bk.grid, bk.smem, c->bstream[b]));
+    if (bk.csize)
+      CK(launch_cluster_batch(a, bk.threads, bk.csize, bk.grid, bk.smem, c->bstream[b]));
+    else
+      CK(launch_batch(a, bk.threads, bk.k, bk.grid, bk.smem, c->bstream[b]));
     if (time_buckets) CK(cudaEventRecord(c->t_b1[b], c->bstream[b]));
     CK(cudaEventRecord(c->ev_b[b], c->bstream[b]));
     ++c->launches;
@@ -579,11 +650,6 @@ static int launch_set(mgcd_context* c, const std::vector<Bucket>& buckets, const
   for (size_t b = 0; b < buckets.size(); ++b) CK(cudaStreamWaitEvent(c->stream, c->ev_b[b], 0));
 
   if (!grid_pairs.empty()) {
-    GridSync* hs = c->h_gsync.as<GridSync>();
-    std::memset(hs, 0, sizeof(GridSync));
-    hs->slot[0] = hs->slot[1] = hs->slot[2] = ~0ull;
-    hs->timeout_ns = c->wait_timeout_ns;
-    hs->withhold_cta = c->withhold_cta;
     for (uint32_t k : grid_pairs) {
       const PairDesc& d = descs[k];
       GridArgs g;
@@ -610,8 +676,8 @@ static int launch_set(mgcd_context* c, const std::vector<Bucket>& buckets, const
         continue;
       }
       // cooperative grid: one CTA per SM (or the reference's shape: 256-thread CTAs, 256 moduli)
-      const int threads = ref_shape ? 256 : GRID_THREADS;
       uint32_t per = ref_shape ? 256u : std::max<uint32_t>(32, (d.nq + c->sms - 1) / c->sms);
+      const int threads = (ref_shape || per <= 256) ? 256 : per <= 512 ? 512 : GRID_THREADS;
       int bps = 0;
       if (grid_max_blocks_per_sm(threads, grid_smem_bytes(per), &bps) != cudaSuccess || bps < 1) return MGCD_ERR_GRID;
       uint32_t grid = (d.nq + per - 1) / per;
@@ -624,7 +690,8 @@ static int launch_set(mgcd_context* c, const std::vector<Bucket>& buckets, const
       }
       g.per_cta = per;
       g.sync = c->d_gsync.as<GridSync>();
-      CK(cudaMemcpyAsync(c->d_gsync.p, hs, sizeof(GridSync), cudaMemcpyHostToDevice, c->stream));
+      CK(launch_gridsync_init(g.sync, c->wait_timeout_ns, c->withhold_cta, c->stream));
+      ++c->launches;
       cudaError_t e = launch_grid(g, threads, (int)grid, grid_smem_bytes(per), c->stream);
       if (e == cudaErrorCooperativeLaunchTooLarge) return MGCD_ERR_GRID;
       if (e != cudaSuccess) return MGCD_ERR_CUDA;
@@ -645,11 +712,39 @@ static int run_plan(mgcd_context* c)
     c->ran = true;
     return MGCD_OK;
   }
-  CK(cudaEventRecord(c->t_run0, c->stream));
-  CK(cudaMemsetAsync(c->d_status.p, 0xFF, ng * sizeof(int32_t), c->stream));
-  int rc = launch_set(c, c->buckets, c->grid_pairs, c->descs, c->d_pairs.as<PairDesc>(), c->d_queue.as<uint32_t>(),
-                      true);
-  if (rc != MGCD_OK) return rc;
+  if (c->use_graph && !c->plain) {
+    if (!c->graph) {
+      // Record the run once (status reset, queue reset, every bucket kernel on its stream,
+      // joined back into c->stream); each later run is a single graph launch.
+      CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+      int rc = MGCD_OK;
+      if (cudaMemsetAsync(c->d_status.p, 0xFF, ng * sizeof(int32_t), c->stream) != cudaSuccess) rc = MGCD_ERR_CUDA;
+      if (rc == MGCD_OK)
+        rc = launch_set(c, c->buckets, c->grid_pairs, c->descs, c->d_pairs.as<PairDesc>(), c->d_queue.as<uint32_t>(),
+                        false);
+      cudaGraph_t g = nullptr;
+      const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+      if (rc == MGCD_OK && e != cudaSuccess) rc = MGCD_ERR_CUDA;
+      if (rc == MGCD_OK && cudaGraphInstantiate(&c->graph, g, 0) != cudaSuccess) {
+        c->graph = nullptr;
+        rc = MGCD_ERR_CUDA;
+      }
+      if (g) cudaGraphDestroy(g);
+      if (rc != MGCD_OK) return rc;
+      c->graph_kernels = c->launches;
+    }
+    CK(cudaEventRecord(c->t_run0, c->stream));
+    CK(cudaGraphLaunch(c->graph, c->stream));
+    c->launches = c->graph_kernels;
+    c->bucket_timed = false;
+  } else {
+    CK(cudaEventRecord(c->t_run0, c->stream));
+    CK(cudaMemsetAsync(c->d_status.p, 0xFF, ng * sizeof(int32_t), c->stream));
+    int rc = launch_set(c, c->buckets, c->grid_pairs, c->descs, c->d_pairs.as<PairDesc>(), c->d_queue.as<uint32_t>(),
+                        true);
+    if (rc != MGCD_OK) return rc;
+    c->bucket_timed = true;
+  }
   CK(cudaEventRecord(c->t_run1, c->stream));
   c->ran = true;
   c->synced = false;
@@ -692,10 +787,12 @@ static int sync_plan(mgcd_context* c)
     DevBuf nb;
     CK(nb.grow(c->order.size() * sizeof(uint32_t)));
     CK(cudaMemcpy(nb.p, c->d_order.p, main_order * sizeof(uint32_t), cudaMemcpyDeviceToDevice));
+    drop_graph(c);
     c->d_order.release();
     c->d_order = nb;
   }
   if (scratch > c->d_scratch.bytes / sizeof(uint32_t)) {
+    drop_graph(c);
     c->d_scratch.release();
     CK(c->d_scratch.grow(scratch * sizeof(uint32_t)));
   }

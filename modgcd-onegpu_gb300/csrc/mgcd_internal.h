@@ -94,6 +94,16 @@ cudaError_t launch_batch(const BatchArgs& a, int threads, int k, int grid, size_
 // shared-memory size as the grid path.
 cudaError_t launch_cluster(const GridArgs& a, int threads, int ctas, size_t smem, cudaStream_t s);
 
+// Persistent batched kernel for pairs larger than one CTA: `clusters` thread-block
+// clusters of `csize` CTAs each pull pairs from the queue.  a.scratch_words = 4 * nq_max.
+size_t cluster_batch_smem_bytes(int csize, uint32_t nq_max);
+cudaError_t cluster_batch_max_clusters(int threads, int csize, size_t smem, int* clusters);
+cudaError_t launch_cluster_batch(const BatchArgs& a, int threads, int csize, int clusters, size_t smem,
+                                 cudaStream_t s);
+
+// Resets the grid exchange state on the device (capturable in a CUDA graph).
+cudaError_t launch_gridsync_init(GridSync* gs, unsigned long long timeout_ns, uint32_t withhold, cudaStream_t s);
+
 size_t grid_smem_bytes(uint32_t per_cta);
 constexpr int GRID_THREADS = 1024;   // CTA size of the grid path (256 for the reference's shape)
 constexpr int MAX_CLUSTER = 16;      // largest thread-block cluster (non-portable size)

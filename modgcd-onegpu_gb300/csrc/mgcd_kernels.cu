@@ -312,6 +312,49 @@ __global__ void __launch_bounds__(T) cluster_kernel(const GridArgs a)
   cluster_sync_all();   // no CTA leaves while others may still address its shared memory
 }
 
+// Persistent batched kernel for pairs too large for one CTA: each thread-block cluster of
+// C CTAs takes the next pair of the queue and computes it with the cluster path above
+// (pair moduli split into C contiguous ranges).  The queue is popped by CTA 0 of the
+// cluster, which writes the index into every CTA's shared memory.  Scratch per cluster:
+// u0[nq_max], v0[nq_max], hist[2 * nq_max].
+template <int T>
+__global__ void __launch_bounds__(T) cluster_batch_kernel(const BatchArgs a)
+{
+  extern __shared__ __align__(16) uint32_t smem[];
+  __shared__ RedSmem rs;
+  __shared__ ClusterSmem cs;
+  __shared__ uint32_t next;
+  const uint32_t C = cluster_size(), r = cluster_rank();
+  const uint32_t per_max = (a.nq_max + C - 1) / C;
+  uint32_t* st = smem;
+  uint32_t* acc2 = smem + per_max;
+  uint32_t* chunk = acc2 + per_max;
+  uint32_t* scr = a.scratch + (size_t)(blockIdx.x / C) * a.scratch_words;
+  cluster_sync_all();
+  for (;;) {
+    if (r == 0 && threadIdx.x < C) {
+      const uint32_t k = __shfl_sync(0xFFFFFFFFu >> (32 - C), threadIdx.x == 0 ? atomicAdd(a.queue, 1u) : 0u, 0);
+      const uint32_t ad = (uint32_t)__cvta_generic_to_shared(&next);
+      uint32_t ra;
+      asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(ad), "r"(threadIdx.x));
+      asm volatile("st.shared::cluster.u32 [%0], %1;" :: "r"(ra), "r"(k) : "memory");
+    }
+    cluster_sync_all();
+    const uint32_t k = next;
+    if (k >= a.npairs) break;
+    const uint32_t pi = a.order[k];
+    const PairDesc d = a.pairs[pi];
+    const uint32_t per = (d.nq + C - 1) / C;
+    const uint32_t j0 = r * per;
+    const uint32_t nloc = j0 >= d.nq ? 0u : (d.nq - j0 < per ? d.nq - j0 : per);
+    run_pair<T, SYNC_CLUSTER>(a.limbs, d, a.mods, a.L, j0, nloc, st, acc2, chunk, rs, scr + j0, scr + d.nq + j0,
+                              reinterpret_cast<int2*>(scr + 2 * (size_t)d.nq), reinterpret_cast<GridSync*>(&cs),
+                              a.digits, a.count + pi, a.iters + pi, a.status + pi, a.inv);
+    cluster_sync_all();   // every CTA is done with `next` and with the pair's scratch
+  }
+  cluster_sync_all();     // no CTA leaves while others may still address its shared memory
+}
+
 // Integer-pipe microbenchmark: eight independent IMAD chains per thread.
 __global__ void __launch_bounds__(256) int_peak_kernel(uint32_t* out, int iters)
 {
@@ -325,6 +368,21 @@ __global__ void __launch_bounds__(256) int_peak_kernel(uint32_t* out, int iters)
     a4 = a4 * m + c; a5 = a5 * m + c; a6 = a6 * m + c; a7 = a7 * m + c;
   }
   if ((a0 ^ a1 ^ a2 ^ a3 ^ a4 ^ a5 ^ a6 ^ a7) == 0x2545F491u) out[0] = 1u;
+}
+
+__global__ void gridsync_init_kernel(GridSync* gs, unsigned long long timeout_ns, uint32_t withhold)
+{
+  gs->slot[0] = gs->slot[1] = gs->slot[2] = ~0ull;
+  gs->arrive = 0u;
+  gs->error = 0u;
+  gs->withhold_cta = withhold;
+  gs->timeout_ns = timeout_ns;
+}
+
+cudaError_t launch_gridsync_init(GridSync* gs, unsigned long long timeout_ns, uint32_t withhold, cudaStream_t s)
+{
+  gridsync_init_kernel<<<1, 1, 0, s>>>(gs, timeout_ns, withhold);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_int_peak(uint32_t* out, int blocks, int iters, cudaStream_t s)
@@ -418,29 +476,75 @@ static const void* cluster_fn(int threads)
   }
 }
 
-cudaError_t launch_cluster(const GridArgs& a, int threads, int ctas, size_t smem, cudaStream_t s)
+static const void* cluster_batch_fn(int threads)
 {
-  const void* fn = cluster_fn(threads);
-  if (!fn || ctas < 1 || ctas > MAX_CLUSTER) return cudaErrorInvalidValue;
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  if (ctas > 8) {
-    e = cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-    if (e != cudaSuccess) return e;
+  switch (threads) {
+    case 256: return reinterpret_cast<const void*>(&cluster_batch_kernel<256>);
+    case 512: return reinterpret_cast<const void*>(&cluster_batch_kernel<512>);
+    case 1024: return reinterpret_cast<const void*>(&cluster_batch_kernel<1024>);
+    default: return nullptr;
   }
+}
+
+static cudaLaunchConfig_t cluster_config(int ctas, int threads, int csize, size_t smem, cudaStream_t s,
+                                         cudaLaunchAttribute* attr)
+{
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(ctas);
   cfg.blockDim = dim3(threads);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
-  cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = ctas;
+  attr[0].val.clusterDim.x = csize;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
+  return cfg;
+}
+
+static cudaError_t prepare_cluster_fn(const void* fn, int csize, size_t smem)
+{
+  if (!fn || csize < 1 || csize > MAX_CLUSTER) return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess && csize > 8) e = cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  return e;
+}
+
+size_t cluster_batch_smem_bytes(int csize, uint32_t nq_max)
+{
+  return grid_smem_bytes((nq_max + csize - 1) / csize);
+}
+
+cudaError_t cluster_batch_max_clusters(int threads, int csize, size_t smem, int* clusters)
+{
+  const void* fn = cluster_batch_fn(threads);
+  cudaError_t e = prepare_cluster_fn(fn, csize, smem);
+  if (e != cudaSuccess) return e;
+  cudaLaunchAttribute attr[1];
+  const cudaLaunchConfig_t cfg = cluster_config(csize, threads, csize, smem, nullptr, attr);
+  return cudaOccupancyMaxActiveClusters(clusters, fn, &cfg);
+}
+
+cudaError_t launch_cluster(const GridArgs& a, int threads, int ctas, size_t smem, cudaStream_t s)
+{
+  const void* fn = cluster_fn(threads);
+  cudaError_t e = prepare_cluster_fn(fn, ctas, smem);
+  if (e != cudaSuccess) return e;
+  cudaLaunchAttribute attr[1];
+  const cudaLaunchConfig_t cfg = cluster_config(ctas, threads, ctas, smem, s, attr);
   void* args[] = {const_cast<GridArgs*>(&a)};
+  return cudaLaunchKernelExC(&cfg, fn, args);
+}
+
+cudaError_t launch_cluster_batch(const BatchArgs& a, int threads, int csize, int clusters, size_t smem, cudaStream_t s)
+{
+  const void* fn = cluster_batch_fn(threads);
+  cudaError_t e = prepare_cluster_fn(fn, csize, smem);
+  if (e != cudaSuccess) return e;
+  cudaLaunchAttribute attr[1];
+  const cudaLaunchConfig_t cfg = cluster_config(clusters * csize, threads, csize, smem, s, attr);
+  void* args[] = {const_cast<BatchArgs*>(&a)};
   return cudaLaunchKernelExC(&cfg, fn, args);
 }
 
@@ -453,6 +557,7 @@ static const void* grid_fn(int threads)
 {
   switch (threads) {
     case 256: return reinterpret_cast<const void*>(&grid_kernel<256>);
+    case 512: return reinterpret_cast<const void*>(&grid_kernel<512>);
     case 1024: return reinterpret_cast<const void*>(&grid_kernel<1024>);
     default: return nullptr;
   }

@@ -111,6 +111,16 @@ static __device__ __forceinline__ unsigned int ld_relaxed_u32(const unsigned int
   return v;
 }
 
+// The CTA that writes a pair's results: the only one (CTA scope), cluster rank 0, or CTA 0
+// of the cooperative grid.
+template <int MODE>
+__device__ __forceinline__ bool lead_cta()
+{
+  if constexpr (MODE == SYNC_CTA) return true;
+  else if constexpr (MODE == SYNC_CLUSTER) return cluster_rank() == 0;
+  else return blockIdx.x == 0;
+}
+
 // Lexicographic (hi, lo) minimum over the CTA; every thread gets the result.
 // One __syncthreads; the two slot buffers alternate so the next call cannot overwrite
 // slots still being read.
@@ -223,7 +233,7 @@ __device__ void run_pair(const uint32_t* __restrict__ limbs, const PairDesc& d, 
                          mgcd_pair* digits, uint32_t* count, uint32_t* iters_out, int32_t* status,
                          InvTab inv)
 {
-  const bool writer = threadIdx.x == 0 && (MODE == SYNC_CTA || blockIdx.x == 0);
+  const bool writer = threadIdx.x == 0 && lead_cta<MODE>();
   const ModConst* __restrict__ my = mods + j0;
   uint32_t parity = 0, epoch = 0;
 
@@ -317,7 +327,7 @@ __device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d
                             double lu, double lv, mgcd_pair* digits, uint32_t* count, int32_t* status,
                             InvTab inv)
 {
-  const bool writer = threadIdx.x == 0 && (MODE == SYNC_CTA || blockIdx.x == 0);
+  const bool writer = threadIdx.x == 0 && lead_cta<MODE>();
   const ModConst* __restrict__ my = mods + j0;
   uint32_t p, kh, kl;
   // Certify the result: all surviving residues of v are 0, so v = 0 if the surviving

@@ -1,0 +1,113 @@
+"""Batches holding pairs larger than one CTA (size class 3: one thread-block cluster per
+pair, pulled from a persistent queue) and batches replayed from a recorded CUDA graph.
+Every result is compared with Python's exact gcd; graph replays must equal direct runs."""
+import math
+import random
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _pair(rng, nbits, gbits):
+    g = rng.getrandbits(gbits) | (1 << (gbits - 1)) if gbits > 0 else 1
+    return (g * (rng.getrandbits(max(nbits - gbits, 1)) | 1),
+            g * (rng.getrandbits(max(nbits - gbits, 1)) | 1))
+
+
+def _skewed(rng, n_large, large_bits, n_small):
+    """n_large pairs of large_bits bits plus n_small pairs of 512..4096 bits, random
+    planted gcd sizes (the skewed-batch shape, scaled down)."""
+    us, vs = [], []
+    for _ in range(n_large):
+        u, v = _pair(rng, large_bits, rng.randint(0, large_bits // 2))
+        us.append(u)
+        vs.append(v)
+    for _ in range(n_small):
+        nb = rng.randint(512, 4096)
+        u, v = _pair(rng, nb, rng.randint(0, nb // 2))
+        us.append(u)
+        vs.append(v)
+    return us, vs
+
+
+def _results(mgcd, dev):
+    g, g_off, g_len, st = dev.batch_download()
+    assert (st == 0).all()
+    return [mgcd.from_limbs(g[int(o): int(o) + int(n)]) for o, n in zip(g_off, g_len)]
+
+
+def test_batch_with_cluster_class_pairs(mgcd):
+    rng = random.Random(41)
+    us, vs = _skewed(rng, 5, 300000, 200)
+    with mgcd.Device(0, 32) as dev:
+        assert dev.gcd_batch(us, vs) == [math.gcd(u, v) for u, v in zip(us, vs)]
+        assert dev.get_cluster_size() == 8
+
+
+@pytest.mark.parametrize("ctas", [2, 4, 16])
+def test_cluster_sizes_agree(mgcd, ctas):
+    rng = random.Random(42)
+    us, vs = _skewed(rng, 3, 200000, 20)
+    with mgcd.Device(0, 32) as dev:
+        dev.set_cluster_size(ctas)
+        assert dev.gcd_batch(us, vs) == [math.gcd(u, v) for u, v in zip(us, vs)]
+
+
+def test_cluster_size_rejects_out_of_range(mgcd):
+    with mgcd.Device(0, 32) as dev:
+        for bad in (0, 1, 17):
+            with pytest.raises(mgcd.GcdError):
+                dev.set_cluster_size(bad)
+        with pytest.raises(mgcd.GcdError):
+            dev.set_size_class(3, 1024, 2, 1.0)
+
+
+def test_graph_replay_matches_direct(mgcd):
+    rng = random.Random(43)
+    us, vs = _skewed(rng, 2, 250000, 3000)
+    exp = [math.gcd(u, v) for u, v in zip(us, vs)]
+    packed = mgcd.pack_pairs(us, vs)
+    with mgcd.Device(0, 32) as dev:
+        dev.batch_upload(*packed)
+        dev.batch_run()
+        dev.batch_sync()
+        direct_launches = dev.batch_launches()
+        assert _results(mgcd, dev) == exp
+
+        dev.batch_use_graph(True)
+        for _ in range(3):
+            dev.batch_run()
+            dev.batch_sync()
+            assert dev.batch_launches() == direct_launches
+            assert _results(mgcd, dev) == exp
+
+        # a new upload records a new graph; the old plan's buffers are not reused stale
+        us2, vs2 = _skewed(random.Random(44), 1, 120000, 500)
+        dev.batch_upload(*mgcd.pack_pairs(us2, vs2))
+        dev.batch_run()
+        dev.batch_sync()
+        assert _results(mgcd, dev) == [math.gcd(u, v) for u, v in zip(us2, vs2)]
+        dev.batch_use_graph(False)
+
+
+def test_graph_replay_with_fewer_moduli_and_retries(mgcd):
+    """Scaled moduli counts under graph replay: uncertified pairs are rerun outside the
+    graph (direct launches) and the next replay still gives exact results."""
+    rng = random.Random(45)
+    us, vs = _skewed(rng, 0, 0, 1500)
+    for _ in range(40):   # coprime-ish and v | u pairs push the certification bound
+        nb = rng.randint(3000, 20000)
+        v = rng.getrandbits(nb) | 1
+        us.append(v * (rng.getrandbits(rng.randint(1, 64)) | 1))
+        vs.append(v)
+    exp = [math.gcd(u, v) for u, v in zip(us, vs)]
+    with mgcd.Device(0, 32) as dev:
+        dev.set_nq_scale(0.5)
+        dev.batch_use_graph(True)
+        dev.batch_upload(*mgcd.pack_pairs(us, vs))
+        for _ in range(2):
+            dev.batch_run()
+            dev.batch_sync()
+            assert _results(mgcd, dev) == exp

@@ -50,9 +50,13 @@ def parse():
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--plain-sample", type=int, default=64)
     ap.add_argument("--cpu-reps", type=int, default=10)
-    ap.add_argument("--workload", choices=["mixed", "sweep"], default="mixed")
+    ap.add_argument("--workload", choices=["mixed", "sweep", "serve", "skewed"], default="mixed")
     ap.add_argument("--sizes", default="4096,16384,65536,262144,1048576")
     ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--serve-rates", default="10000",
+                    help="arrival rates (req/s) of the serving leg; --workload serve defaults to the full sweep")
+    ap.add_argument("--serve-requests", type=int, default=1000)
+    ap.add_argument("--tuning", default=None, help="tuning table (default: the package's table for this GPU)")
     return ap.parse_args()
 
 
@@ -151,6 +155,43 @@ def results_equal(mg, g1, o1, n1, g2, o2, n2):
     return True
 
 
+def serve_leg(mg, wl, po, dev, rates, n_req, nthreads, seed=5):
+    """Open-loop serving: n_req requests (mixed 1k-64k-bit sizes plus 1% 1M-bit), Poisson
+    arrivals at each rate, through the request server (mgcd_serve_replay, C ABI); latency
+    = scheduled arrival -> answer.  Results checked against GMP."""
+    import numpy as np
+    us, vs, arr1 = wl.serve_requests(n_req, 1.0, seed=seed)
+    packed = mg.pack_pairs(us, vs)
+    _, gx, gxo, gxn = po.cpu_gmp_gcd_batch(*packed, nthreads)
+    big = np.array([max(u.bit_length(), v.bit_length()) > (1 << 19) for u, v in zip(us, vs)])
+    rows = []
+    with mg.Server(dev, budget_bytes=8 << 30) as srv:
+        for rate in rates:
+            g, go, gn, st, lat, mk = srv.replay_packed(*packed, np.asarray(arr1) / rate)
+            ok = bool((st == 0).all()) and results_equal(mg, g, go, gn, gx, gxo, gxn)
+            ms = lat * 1e3
+            row = {"rate_req_s": rate, "requests": n_req, "gcds_per_s": n_req / mk, "makespan_s": mk,
+                   "p50_ms": float(np.percentile(ms, 50)), "p99_ms": float(np.percentile(ms, 99)),
+                   "p50_ms_small": float(np.percentile(ms[~big], 50)), "p99_ms_small": float(np.percentile(ms[~big], 99)),
+                   "bit_exact": ok}
+            if big.any():
+                row.update({"n_1M": int(big.sum()), "p50_ms_1M": float(np.percentile(ms[big], 50)),
+                            "max_ms_1M": float(ms[big].max())})
+            rows.append(row)
+            print(json.dumps(row), file=sys.stderr, flush=True)
+        stats = srv.stats()
+    return rows, stats
+
+
+def apply_tuning(dev, path):
+    """Loads the tuning table (mgcd_load_tuning); returns its path or None."""
+    try:
+        dev.load_tuning(path)
+        return path
+    except (OSError, RuntimeError):
+        return None
+
+
 def run_reference(args, rank, pg):
     if rank != 0:
         return
@@ -197,6 +238,7 @@ def run_ours(args, rank, local, world, pg):
     cpu_times, gx, gxo, gxn = gmp_baseline(po, packed, nthreads, args.cpu_reps if rank == 0 else 1)
 
     dev = mg.Device(local, 32)
+    tuning = apply_tuning(dev, args.tuning or mg.default_tuning_path(dev))
     int_peak = dev.int_peak()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")   # > L2 (129 MB)
 
@@ -252,6 +294,10 @@ def run_ours(args, rank, local, world, pg):
     plain_rate = len(idx) / sum(lat)
     lat_ms = sorted(1e3 * x for x in lat)
 
+    # ---- serving: Poisson arrivals through the request server
+    rates = [float(r) for r in args.serve_rates.split(",") if r]
+    serve_rows, serve_stats = serve_leg(mg, wl, po, dev, rates, args.serve_requests, nthreads) if rates else ([], {})
+
     if rank != 0:
         return
     peaks, peaks_kind = measured_peaks()
@@ -277,13 +323,17 @@ def run_ours(args, rank, local, world, pg):
                                "25%% coprime, 5%% v|u, 70%% planted gcd U[0,50%%] of the smaller" % n,
                    "modulus_bits": 32, "parallelism": "replicas" if world > 1 else "single",
                    "l2": "flushed before every step (256 MB write)"},
-        "bit_exact": ok_dev and ok_e2e and ok_plain,
+        "bit_exact": ok_dev and ok_e2e and ok_plain and all(r["bit_exact"] for r in serve_rows),
         "e2e": {"value": n * world * args.steps / e2e_s, "unit": "GCDs/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "plain": {"value": plain_rate, "unit": "GCDs/s", "sample_pairs": len(idx),
                   "p50_ms": lat_ms[len(lat_ms) // 2], "p99_ms": lat_ms[min(len(lat_ms) - 1, int(0.99 * len(lat_ms)))],
                   "batched_over_plain": value / world / plain_rate},
         "batch_latency_ms": {"p50": statistics.median(run_ms), "max": max(run_ms)},
+        "serving": {"rows": serve_rows, "server": serve_stats,
+                    "workload": "mixed 1k-64k-bit sizes + 1% 1M-bit, Poisson arrivals, 8 GB admission budget",
+                    "bit_exact": all(r["bit_exact"] for r in serve_rows)},
+        "tuning": tuning,
         "roofline": {"bound": "int", "achieved": achieved / 1e9, "peak": int_peak / 1e9, "unit": "Gop/s",
                      "frac": achieved / int_peak, "traffic": traffic,
                      "kernel": "all launches of one step (%d persistent bucket kernels)" % launches,
@@ -356,11 +406,70 @@ def run_sweep(args, rank, local):
                       "unit": "ms", "higher_is_better": False, "data": "synthetic", "rows": rows}), flush=True)
 
 
+def run_serve(args, rank, local):
+    """Serving sweep: Poisson arrivals at each rate (default 1k-200k req/s), sizes from the
+    mixed distribution plus 1% 1M-bit requests, 8 GB admission budget."""
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    mg = importlib.import_module("modgcd-onegpu_gb300")
+    wl = importlib.import_module("modgcd-onegpu_gb300.workloads")
+    dev = mg.Device(local, 32)
+    tuning = apply_tuning(dev, args.tuning or mg.default_tuning_path(dev))
+    rates = [float(r) for r in (args.serve_rates if args.serve_rates != "10000" else
+                                "1000,10000,50000,100000,200000").split(",")]
+    rows, stats = serve_leg(mg, wl, po, dev, rates, args.serve_requests, os.cpu_count() or 1)
+    print(json.dumps({"metric": "served GCDs/s and p50/p99 latency (enqueue -> result)", "unit": "GCDs/s, ms",
+                      "data": "synthetic", "workload": "mixed 1k-64k-bit + 1% 1M-bit requests, Poisson arrivals, "
+                      "8 GB admission budget", "tuning": tuning, "rows": rows, "server": stats,
+                      "bit_exact": all(r["bit_exact"] for r in rows)}), flush=True)
+
+
+def run_skewed(args, rank, local):
+    """The skewed batch (64 pairs at 1M bits + 16,384 pairs of 512-4096 bits) recorded into
+    one CUDA graph and replayed; device time per replay, results against GMP."""
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    mg = importlib.import_module("modgcd-onegpu_gb300")
+    wl = importlib.import_module("modgcd-onegpu_gb300.workloads")
+    us, vs = wl.skewed_batch()
+    packed = mg.pack_pairs(us, vs)
+    nthreads = os.cpu_count() or 1
+    cpu_s, gx, gxo, gxn = po.cpu_gmp_gcd_batch(*packed, nthreads)
+    dev = mg.Device(local, 32)
+    tuning = apply_tuning(dev, args.tuning or mg.default_tuning_path(dev))
+    dev.batch_use_graph(True)
+    dev.batch_upload(*packed)
+    ms = []
+    for _ in range(max(1, args.steps) + 1):
+        dev.batch_run()
+        dev.batch_sync()
+        ms.append(dev.batch_elapsed_ms()[0])
+    g, go, gn, st = dev.batch_download()
+    ok = bool((st == 0).all()) and results_equal(mg, g, go, gn, gx, gxo, gxn)
+    n = len(us)
+    t = statistics.median(ms[1:]) / 1e3
+    print(json.dumps({"metric": "GCDs/s (skewed batch in one CUDA graph launch)", "value": n / t, "unit": "GCDs/s",
+                      "ms_per_step": 1e3 * t, "graph_kernels": dev.batch_launches(), "steps": len(ms) - 1,
+                      "config": {"workload": "64 pairs at 1M bits + 16384 pairs of U[512,4096] bits, planted gcds",
+                                 "modulus_bits": 32},
+                      "tuning": tuning, "bit_exact": ok,
+                      "cpu_baseline": {"value": n / cpu_s, "unit": "GCDs/s", "cores": nthreads, "kind": "reference",
+                                       "sample": "GMP mpz_gcd over the whole batch"}}), flush=True)
+
+
 def main():
     args = parse()
     rank, local, world, pg = dist()
     if args.workload == "sweep":
         run_sweep(args, rank, local)
+    elif args.workload == "serve":
+        run_serve(args, rank, local)
+    elif args.workload == "skewed":
+        run_skewed(args, rank, local)
     elif args.impl == "reference":
         run_reference(args, rank, pg)
     else:

@@ -159,6 +159,12 @@ int mgcd_get_size_class(const mgcd_context *ctx, int cls, int *threads, int *k, 
    when a pair's share of moduli would not fit one CTA's shared memory). */
 int mgcd_set_cluster_size(mgcd_context *ctx, int ctas);
 int mgcd_get_cluster_size(const mgcd_context *ctx, int *ctas);
+/* Tuning table (the autotuner's output, modgcd-onegpu_gb300/tune.py): a text file with one
+   line per size class, "class threads k nq_scale cluster_ctas" (cluster_ctas 0 except for
+   class 3), '#' comments.  Load checks every line before applying any (MGCD_ERR_INVALID_ARG
+   for a missing file or a bad line); save writes the context's current table. */
+int mgcd_load_tuning(mgcd_context *ctx, const char *path);
+int mgcd_save_tuning(const mgcd_context *ctx, const char *path);
 /* Records the GPU work of a batch (status reset, queue resets, one persistent kernel per
    size class on its own stream) into a CUDA graph at the first mgcd_batch_run after an
    upload; every later mgcd_batch_run of the same upload is one graph launch.  The graph
@@ -183,6 +189,55 @@ int mgcd_batch_transfer_bytes(const mgcd_context *ctx, uint64_t *h2d, uint64_t *
 /* Integer-pipe throughput of this GPU measured by a microbenchmark (independent 32-bit
    IMAD chains on every SM): instructions per second. */
 int mgcd_int_peak(mgcd_context *ctx, double *int_ops_per_s);
+/* Certifies, on this device, the float-reciprocal quotient steps of the modular inverse
+   for every operand pair they can see (replaces certifyQuoRemQuasi.cu:25-48, which checks
+   the reference's quoRem<QUASI> per device): the estimate must be the true quotient or one
+   less, so that the single exact correction step is always right.  The estimate is
+   monotone in the dividend for a fixed divisor, so checking both ends of every quotient
+   interval of every divisor covers all pairs: *checked end points (about 6e10), *failures
+   of them (0 on a certified device), the first failing (r0, r1). */
+int mgcd_certify_inverse(mgcd_context *ctx, uint64_t *checked, uint64_t *failures, uint32_t *first_r0,
+                         uint32_t *first_r1);
+
+/* ------------------------------------------------------------------------ serving ----
+   No counterpart in the reference (one blocking GmpCudaDevice::gcd call per pair).  A
+   request server on a context: callers submit single gcd requests from any thread and take
+   the results later.  A server thread batches the queued requests continuously: each size
+   class (lane, as in mgcd_set_size_class) turns its queue into a wave -- a batch with its
+   own streams and buffers -- whenever one of its wave slots (2; 8 for class 3) is free and the admission
+   budget allows, and launches it while earlier waves are still on the GPU, so requests
+   that arrive later overlap with earlier ones on the device.  The moduli table and the
+   inverse tables stay resident; a wave holds only its operands, scratch and digits.
+   Admission budget: the device bytes admitted, unanswered requests occupy (operands,
+   descriptors, digit slots and their share of the reduction scratch, about
+   24 x moduli + 4 x limbs bytes per request) never exceed budget_bytes; a request larger
+   than the budget on its own is refused with MGCD_ERR_BUDGET, a full queue (4M requests)
+   with MGCD_ERR_BUSY.  While a server runs, the context's own calls return MGCD_ERR_BUSY. */
+typedef struct mgcd_server mgcd_server;
+int mgcd_serve_start(mgcd_context *ctx, size_t budget_bytes, mgcd_server **server);
+/* Answers every submitted request, then stops the server thread and frees the server. */
+int mgcd_serve_stop(mgcd_server *server);
+/* Queues gcd(u, v) (operands copied; either order; zero operands allowed). */
+int mgcd_serve_submit(mgcd_server *server, const uint32_t *u, size_t uSz, const uint32_t *v, size_t vSz,
+                      uint64_t *ticket);
+/* *done = 1 once the ticket's result is ready. */
+int mgcd_serve_poll(mgcd_server *server, uint64_t ticket, int *done);
+/* Waits up to timeout_ms (0: no limit; MGCD_ERR_TIMEOUT keeps the ticket) for the result,
+   copies g (little-endian limbs, *g_len of them) and the latency from submission to the
+   answer, releases the ticket and returns the request's status. */
+int mgcd_serve_take(mgcd_server *server, uint64_t ticket, unsigned timeout_ms, uint32_t *g, size_t g_cap,
+                    size_t *g_len, double *latency_s);
+/* Open-loop load: submits pair i (batch layout as in mgcd_gcd_batch) at arrival_s[i]
+   seconds after the call starts, waits for every answer and returns each request's status,
+   result and latency (scheduled arrival to answer); *makespan_s = last answer - start. */
+int mgcd_serve_replay(mgcd_server *server, size_t npairs, const uint32_t *limbs,
+                      const uint64_t *u_off, const uint32_t *u_len,
+                      const uint64_t *v_off, const uint32_t *v_len, const double *arrival_s,
+                      uint32_t *g, const uint64_t *g_off, const uint32_t *g_cap, uint32_t *g_len,
+                      int32_t *status, double *latency_s, double *makespan_s);
+/* Waves launched, kernel launches, peak admitted bytes, requests answered. */
+int mgcd_serve_stats(mgcd_server *server, uint64_t *waves, uint64_t *launches, uint64_t *peak_bytes,
+                     uint64_t *completed);
 
 /* ------------------------------------------------------------ allocation-free call ----
    No counterpart in the reference.  For callers that cannot allocate device memory when

@@ -73,6 +73,20 @@ SIGNATURES = {
     "mgcd_set_cluster_size": (_c.c_int, [_P, _c.c_int]),
     "mgcd_get_cluster_size": (_c.c_int, [_P, _c.POINTER(_c.c_int)]),
     "mgcd_batch_use_graph": (_c.c_int, [_P, _c.c_int]),
+    "mgcd_certify_inverse": (_c.c_int, [_P, _c.POINTER(_c.c_uint64), _c.POINTER(_c.c_uint64),
+                                        _c.POINTER(_c.c_uint32), _c.POINTER(_c.c_uint32)]),
+    "mgcd_load_tuning": (_c.c_int, [_P, _c.c_char_p]),
+    "mgcd_save_tuning": (_c.c_int, [_P, _c.c_char_p]),
+    "mgcd_serve_start": (_c.c_int, [_P, _c.c_size_t, _P]),
+    "mgcd_serve_stop": (_c.c_int, [_P]),
+    "mgcd_serve_submit": (_c.c_int, [_P, _P, _c.c_size_t, _P, _c.c_size_t, _c.POINTER(_c.c_uint64)]),
+    "mgcd_serve_poll": (_c.c_int, [_P, _c.c_uint64, _c.POINTER(_c.c_int)]),
+    "mgcd_serve_take": (_c.c_int, [_P, _c.c_uint64, _c.c_uint, _P, _c.c_size_t, _c.POINTER(_c.c_size_t),
+                                   _c.POINTER(_c.c_double)]),
+    "mgcd_serve_replay": (_c.c_int, [_P, _c.c_size_t, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
+                                     _c.POINTER(_c.c_double)]),
+    "mgcd_serve_stats": (_c.c_int, [_P, _c.POINTER(_c.c_uint64), _c.POINTER(_c.c_uint64),
+                                    _c.POINTER(_c.c_uint64), _c.POINTER(_c.c_uint64)]),
 }
 
 _lib = None
@@ -159,6 +173,14 @@ def gen_moduli(L, count):
     out = np.zeros(count, dtype=np.uint32)
     n = load().mgcd_gen_moduli(int(L), out.ctypes.data, count)
     return out[:n]
+
+
+TUNING_DIR = os.path.join(HERE, "tuning")
+
+
+def default_tuning_path(dev):
+    """The committed tuning table for this modulus width on GB300 (written by tune.py)."""
+    return os.path.join(TUNING_DIR, "gb300_L%d.txt" % dev.L)
 
 
 def device_count():
@@ -297,6 +319,24 @@ class Device:
         _check(self._lib.mgcd_get_cluster_size(self._h, ctypes.byref(n)))
         return n.value
 
+    def certify_inverse(self):
+        """Exhaustive end-point certification of the inverse's quotient steps on this GPU:
+        {"checked", "failures", "first_failure"}."""
+        n, f, a, b = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint32(), ctypes.c_uint32()
+        _check(self._lib.mgcd_certify_inverse(self._h, ctypes.byref(n), ctypes.byref(f), ctypes.byref(a),
+                                              ctypes.byref(b)))
+        return {"checked": n.value, "failures": f.value,
+                "first_failure": (a.value, b.value) if f.value else None}
+
+    def load_tuning(self, path):
+        """Applies a tuning table (mgcd_load_tuning)."""
+        if not os.path.exists(path):
+            raise OSError("no tuning table at %s" % path)
+        _check(self._lib.mgcd_load_tuning(self._h, os.fsencode(path)))
+
+    def save_tuning(self, path):
+        _check(self._lib.mgcd_save_tuning(self._h, os.fsencode(path)))
+
     def batch_use_graph(self, enable=True):
         """Record each upload's GPU work into a CUDA graph and replay it on every run."""
         _check(self._lib.mgcd_batch_use_graph(self._h, 1 if enable else 0))
@@ -365,6 +405,86 @@ class Device:
                                          ctypes.byref(b)))
         return {"residue_steps": r.value, "euclid_updates": e.value, "recovery_updates": m.value,
                 "operand_bytes": b.value}
+
+
+class Server:
+    """Request server on a Device (mgcd_serve_*): continuous batching of single requests
+    under an HBM admission budget.  The Device's own calls are refused while it runs."""
+
+    def __init__(self, device, budget_bytes=8 << 30):
+        self._lib = device._lib
+        self.device = device
+        h = ctypes.c_void_p()
+        _check(self._lib.mgcd_serve_start(device._h, int(budget_bytes), ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.mgcd_serve_stop(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, u, v):
+        a, b = to_limbs(u), to_limbs(v)
+        t = ctypes.c_uint64()
+        _check(self._lib.mgcd_serve_submit(self._h, _ptr(a), len(a), _ptr(b), len(b), ctypes.byref(t)))
+        return t.value
+
+    def poll(self, ticket):
+        d = ctypes.c_int()
+        _check(self._lib.mgcd_serve_poll(self._h, int(ticket), ctypes.byref(d)))
+        return bool(d.value)
+
+    def take(self, ticket, cap, timeout_ms=0):
+        """(gcd, latency_s) of a ticket; cap >= the result's limb count."""
+        g = np.zeros(max(int(cap), 1), dtype=np.uint32)
+        n, lat = ctypes.c_size_t(), ctypes.c_double()
+        _check(self._lib.mgcd_serve_take(self._h, int(ticket), int(timeout_ms), g.ctypes.data, len(g),
+                                         ctypes.byref(n), ctypes.byref(lat)))
+        return from_limbs(g[: n.value]), lat.value
+
+    def gcd(self, u, v):
+        """One request, submitted and waited for."""
+        t = self.submit(u, v)
+        return self.take(t, max(len(to_limbs(u)), len(to_limbs(v))) + 1)[0]
+
+    def replay_packed(self, limbs, u_off, u_len, v_off, v_len, arrival_s):
+        """Open-loop load (mgcd_serve_replay): (g, g_off, g_len, status, latency_s, makespan_s)."""
+        n = len(u_off)
+        g_off, g_cap, tot = result_layout(u_len, v_len)
+        g = np.zeros(max(tot, 1), dtype=np.uint32)
+        g_len = np.zeros(n, dtype=np.uint32)
+        st = np.zeros(n, dtype=np.int32)
+        lat = np.zeros(n, dtype=np.float64)
+        arr = np.ascontiguousarray(arrival_s, dtype=np.float64)
+        mk = ctypes.c_double()
+        self._lib.mgcd_serve_replay(self._h, n, _ptr(limbs), _ptr(u_off), _ptr(u_len), _ptr(v_off), _ptr(v_len),
+                                    _ptr(arr), g.ctypes.data, _ptr(g_off), _ptr(g_cap), _ptr(g_len), _ptr(st),
+                                    _ptr(lat), ctypes.byref(mk))
+        return g, g_off, g_len, st, lat, mk.value
+
+    def replay(self, us, vs, arrival_s):
+        """[gcd] per request, statuses, latencies (s) and the makespan (s)."""
+        g, g_off, g_len, st, lat, mk = self.replay_packed(*pack_pairs(us, vs), arrival_s)
+        res = [from_limbs(g[int(o): int(o) + int(n)]) for o, n in zip(g_off, g_len)]
+        return res, st, lat, mk
+
+    def stats(self):
+        w, l, p, c = (ctypes.c_uint64() for _ in range(4))
+        _check(self._lib.mgcd_serve_stats(self._h, ctypes.byref(w), ctypes.byref(l), ctypes.byref(p),
+                                          ctypes.byref(c)))
+        return {"waves": w.value, "launches": l.value, "peak_admitted_bytes": p.value, "completed": c.value}
 
 
 def build(verbose=False):

@@ -63,13 +63,13 @@ def build(verbose=False, force=False):
     hdrs = _headers()
     cuda_inc = "-I" + os.path.join(CUDA_HOME, "include")
     units = []
-    for f in ("mgcd_kernels.cu", "mgcd_noalloc.cu"):
+    for f in ("mgcd_kernels.cu", "mgcd_noalloc.cu", "mgcd_radix_dev.cu", "mgcd_certify.cu"):
         src = os.path.join(CSRC, f)
         obj = os.path.join(BUILD, f + ".o")
         cmd = [NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-v",
                                "-c", src, "-o", obj]
         units.append((obj, [src] + hdrs, cmd))
-    for f in ("mgcd_capi.cpp", "mgcd_moduli.cpp", "mgcd_radix.cpp", "GmpCudaDevice.cpp"):
+    for f in ("mgcd_capi.cpp", "mgcd_serve.cpp", "mgcd_moduli.cpp", "mgcd_radix.cpp", "GmpCudaDevice.cpp"):
         src = os.path.join(CSRC, f)
         obj = os.path.join(BUILD, f + ".o")
         cmd = [CXX, "-O2", "-fPIC", "-std=c++17", "-Wall", cuda_inc, "-I" + os.path.join(ROOT, "include")] + \

@@ -7,15 +7,16 @@
 //             :61-62), strip leading zero limbs, size the moduli (numModuliNeededFor,
 //             :49-55) and reject pairs that need more moduli than the table holds (:76-78);
 //             pairs with a zero operand are answered on the host (gcd(x, 0) = x);
-//             group the rest by size into CTA-size buckets, largest first; copy the batch.
+//             group the rest by size into size-class buckets, largest first; copy the batch.
 //   run       one persistent kernel per bucket, each on its own stream so buckets overlap;
-//             pairs too large for one CTA run one at a time on a cooperative grid.
+//             single pairs too large for one CTA run on a cluster or a cooperative grid.
 //   download  copy digits back and convert each pair's digits to binary.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <thread>
@@ -24,79 +25,112 @@
 #include "../../include/modgcd.h"
 #include "mgcd_internal.h"
 #include "mgcd_moduli.h"
+#include "mgcd_plan.h"
 #include "mgcd_radix.h"
 
 using namespace mgcd;
 
-namespace {
+#define CK(call)                                     \
+  do {                                               \
+    cudaError_t e_ = (call);                         \
+    if (e_ != cudaSuccess) return MGCD_ERR_CUDA;     \
+  } while (0)
 
-struct DevBuf {
-  void* p = nullptr;
-  size_t bytes = 0;
-  cudaError_t grow(size_t want)
-  {
-    if (want <= bytes) return cudaSuccess;
-    if (p) cudaFree(p);
-    p = nullptr;
-    bytes = 0;
-    const size_t sz = std::max<size_t>(want + want / 4, 256);
-    cudaError_t e = cudaMalloc(&p, sz);
-    if (e == cudaSuccess) bytes = sz;
-    return e;
-  }
-  void release()
-  {
-    if (p) cudaFree(p);
-    p = nullptr;
-    bytes = 0;
-  }
-  template <class T> T* as() const { return static_cast<T*>(p); }
-};
+namespace mgcd {
 
-struct HostBuf {
-  void* p = nullptr;
-  size_t bytes = 0;
-  cudaError_t grow(size_t want)
-  {
-    if (want <= bytes) return cudaSuccess;
-    if (p) cudaFreeHost(p);
-    p = nullptr;
-    bytes = 0;
-    const size_t sz = std::max<size_t>(want + want / 4, 256);
-    cudaError_t e = cudaHostAlloc(&p, sz, cudaHostAllocDefault);
-    if (e == cudaSuccess) bytes = sz;
-    return e;
-  }
-  void release()
-  {
-    if (p) cudaFreeHost(p);
-    p = nullptr;
-    bytes = 0;
-  }
-  template <class T> T* as() const { return static_cast<T*>(p); }
-};
-
-struct Bucket {
-  int threads, k;      // CTA size, pairs per CTA in lockstep
-  int csize;           // CTAs per thread-block cluster (0: one CTA per pair)
-  int cls;             // size class
-  uint32_t first, n, nq_max;
-  int grid;            // CTAs (csize = 0) or clusters
-  size_t smem;
-  size_t scratch_off;  // words
-};
-
-// Size classes of the batched path, one persistent kernel (and stream) each: pairs with at
-// most 1,024 / 4,096 / 16,384 moduli run one per CTA; larger pairs one per cluster.
-constexpr int NSTREAMS = 4;
-constexpr int CLUSTER_CLASS = 3;
-constexpr uint32_t CTA_MAX_NQ = 16384;
-constexpr size_t INVTAB_N = 16384;        // moduli covered by the pairwise inverse table
-
-int env_int(const char* name, int dflt)
+cudaError_t DevBuf::grow(size_t want, cudaMemPool_t pool, cudaStream_t s)
 {
-  const char* s = std::getenv(name);
-  return s ? std::atoi(s) : dflt;
+  if (want <= bytes) return cudaSuccess;
+  if (p) cudaFreeAsync(p, s);
+  p = nullptr;
+  bytes = 0;
+  const size_t sz = std::max<size_t>(want + want / 4, 256);
+  cudaError_t e = cudaMallocFromPoolAsync(&p, sz, pool, s);
+  if (e == cudaSuccess) bytes = sz;
+  return e;
+}
+
+void DevBuf::release(cudaStream_t s)
+{
+  if (p) cudaFreeAsync(p, s);
+  p = nullptr;
+  bytes = 0;
+}
+
+cudaError_t HostBuf::grow(size_t want)
+{
+  if (want <= bytes) return cudaSuccess;
+  if (p) retired.push_back(p);
+  p = nullptr;
+  const size_t sz = std::max<size_t>(std::max(want, 2 * bytes), 4096);
+  bytes = 0;
+  cudaError_t e = cudaHostAlloc(&p, sz, cudaHostAllocDefault);
+  if (e == cudaSuccess) bytes = sz;
+  return e;
+}
+
+void HostBuf::release()
+{
+  for (void* q : retired) cudaFreeHost(q);
+  retired.clear();
+  if (p) cudaFreeHost(p);
+  p = nullptr;
+  bytes = 0;
+}
+
+cudaError_t Plan::create()
+{
+  if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) return cudaErrorUnknown;
+  for (int i = 0; i < NSTREAMS; ++i)
+    if (cudaStreamCreateWithFlags(&bstream[i], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ev_b[i], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreate(&t_b0[i]) != cudaSuccess || cudaEventCreate(&t_b1[i]) != cudaSuccess)
+      return cudaErrorUnknown;
+  if (cudaEventCreateWithFlags(&ev_start, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreate(&t_run0) != cudaSuccess || cudaEventCreate(&t_run1) != cudaSuccess)
+    return cudaErrorUnknown;
+  return cudaSuccess;
+}
+
+void Plan::drop_graph()
+{
+  if (graph) cudaGraphExecDestroy(graph);
+  graph = nullptr;
+  graph_kernels = 0;
+}
+
+void Plan::destroy(cudaMemPool_t)
+{
+  if (stream) cudaStreamSynchronize(stream);
+  drop_graph();
+  for (DevBuf* b : {&d_limbs, &d_pairs, &d_order, &d_digits, &d_count, &d_iters, &d_status, &d_queue, &d_scratch,
+                    &d_gsync, &d_retry, &d_glimbs, &d_glen})
+    b->release(stream);
+  if (stream) cudaStreamSynchronize(stream);
+  for (HostBuf* b : {&h_count, &h_iters, &h_status, &h_digits, &h_glimbs, &h_glen}) b->release();
+  for (int i = 0; i < NSTREAMS; ++i) {
+    if (bstream[i]) cudaStreamDestroy(bstream[i]);
+    if (ev_b[i]) cudaEventDestroy(ev_b[i]);
+    if (t_b0[i]) cudaEventDestroy(t_b0[i]);
+    if (t_b1[i]) cudaEventDestroy(t_b1[i]);
+    bstream[i] = nullptr;
+    ev_b[i] = t_b0[i] = t_b1[i] = nullptr;
+  }
+  if (t_run0) cudaEventDestroy(t_run0);
+  if (t_run1) cudaEventDestroy(t_run1);
+  if (ev_start) cudaEventDestroy(ev_start);
+  if (stream) cudaStreamDestroy(stream);
+  t_run0 = t_run1 = ev_start = nullptr;
+  stream = nullptr;
+}
+
+size_t Plan::device_bytes() const
+{
+  size_t s = 0;
+  for (const DevBuf* b : {&d_limbs, &d_pairs, &d_order, &d_digits, &d_count, &d_iters, &d_status, &d_queue,
+                          &d_scratch, &d_gsync, &d_retry, &d_glimbs, &d_glen})
+    s += b->bytes;
+  return s;
 }
 
 int to_status(int32_t st)
@@ -111,7 +145,9 @@ int to_status(int32_t st)
   }
 }
 
-int size_class(uint32_t nq) { return nq <= 1024 ? 0 : nq <= 4096 ? 1 : nq <= CTA_MAX_NQ ? 2 : CLUSTER_CLASS; }
+}  // namespace mgcd
+
+namespace {
 
 size_t strip(const uint32_t* x, size_t n)
 {
@@ -127,71 +163,9 @@ int cmp_mag(const uint32_t* a, size_t na, const uint32_t* b, size_t nb)
   return 0;
 }
 
+bool busy(const mgcd_context* c) { return c->serving; }
+
 }  // namespace
-
-struct mgcd_context {
-  int device = 0, L = 32, sms = 0;
-  size_t smem_optin = 0;               // largest dynamic shared memory per CTA
-  cudaStream_t stream = nullptr;
-  cudaStream_t bstream[NSTREAMS] = {};
-  cudaEvent_t ev_start = nullptr, ev_b[NSTREAMS] = {};
-  std::vector<uint32_t> moduli;
-  DevBuf mods;
-
-  // current plan
-  size_t np = 0;                       // pairs in the plan
-  std::vector<int32_t> status;         // per pair: MGCD_OK / error code / -1 = computed on the GPU
-  std::vector<int> slot;               // per pair: index into GPU arrays, or -1
-  std::vector<std::vector<uint32_t>> trivial;  // per pair: host-decided result (zero operand)
-  std::vector<PairDesc> descs;         // GPU pairs
-  std::vector<uint32_t> order;
-  std::vector<Bucket> buckets;
-  std::vector<uint32_t> grid_pairs;    // GPU indices run on the cooperative grid
-  size_t ndig = 0, scratch_words = 0, grid_scratch_off = 0;
-  bool plain = false;                  // single-pair latency policy
-
-  DevBuf d_limbs, d_pairs, d_order, d_digits, d_count, d_iters, d_status, d_queue, d_scratch, d_gsync;
-  HostBuf h_count, h_iters, h_status, h_digits;
-  int launches = 0;
-  bool ran = false;
-  double work[4] = {0, 0, 0, 0};
-  // Per size class of the batched path: CTA size, pairs per CTA in lockstep, fraction of
-  // the reference moduli count, CTAs per cluster (cluster class only).
-  struct { int threads, k; float nq_scale; int csize; } cfg[NSTREAMS] = {
-      {256, 4, 1.0f, 0}, {512, 4, 1.0f, 0}, {1024, 2, 1.0f, 0}, {1024, 1, 1.0f, 8}};
-  // CUDA graph of the plan's GPU work (mgcd_batch_use_graph); rebuilt after every upload
-  bool use_graph = false, bucket_timed = false;
-  cudaGraphExec_t graph = nullptr;
-  int graph_kernels = 0;
-  std::vector<uint32_t> ref_nq, eff_nq; // per GPU pair: reference count, count of the final run
-  int retried = 0;
-  bool synced = false;
-  DevBuf d_retry;
-  DevBuf d_invtab;                     // pairwise inverse table (InvTab)
-  int single_policy = MGCD_SINGLE_AUTO;  // launch shape of pairs that span several CTAs
-  unsigned long long wait_timeout_ns = 2000000000ull;   // bound of every cross-CTA wait
-  uint32_t withhold_cta = 0xFFFFFFFFu;                  // test hook (mgcd_test_withhold_cta)
-  uint32_t force_nq = 0;                                // test hook (mgcd_test_force_moduli)
-  uint32_t invtab_n = 0;
-  // timing: the whole run on `stream`, and each bucket launch on its stream
-  cudaEvent_t t_run0 = nullptr, t_run1 = nullptr, t_b0[NSTREAMS] = {}, t_b1[NSTREAMS] = {};
-  uint64_t h2d_bytes = 0, d2h_bytes = 0;
-};
-
-#define CK(call)                                     \
-  do {                                               \
-    cudaError_t e_ = (call);                         \
-    if (e_ != cudaSuccess) return MGCD_ERR_CUDA;     \
-  } while (0)
-
-// The recorded graph holds device pointers and launch parameters of the current plan:
-// dropped whenever a buffer it uses moves or a captured parameter changes.
-static void drop_graph(mgcd_context* c)
-{
-  if (c->graph) cudaGraphExecDestroy(c->graph);
-  c->graph = nullptr;
-  c->graph_kernels = 0;
-}
 
 extern "C" {
 
@@ -266,28 +240,33 @@ int mgcd_create(int device, int L, mgcd_context** out)
   std::vector<ModConstHost> mc(c->moduli.size());
   mod_constants(c->moduli.data(), c->moduli.size(), mc.data());
   int rc = MGCD_OK;
-  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) rc = MGCD_ERR_CUDA;
-  for (int i = 0; i < NSTREAMS && rc == MGCD_OK; ++i)
-    if (cudaStreamCreateWithFlags(&c->bstream[i], cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->ev_b[i], cudaEventDisableTiming) != cudaSuccess)
-      rc = MGCD_ERR_CUDA;
-  if (rc == MGCD_OK && cudaEventCreateWithFlags(&c->ev_start, cudaEventDisableTiming) != cudaSuccess) rc = MGCD_ERR_CUDA;
-  if (rc == MGCD_OK && (cudaEventCreate(&c->t_run0) != cudaSuccess || cudaEventCreate(&c->t_run1) != cudaSuccess))
+  // A private stream-ordered pool that keeps freed memory for reuse.
+  cudaMemPoolProps pp = {};
+  pp.allocType = cudaMemAllocationTypePinned;
+  pp.location.type = cudaMemLocationTypeDevice;
+  pp.location.id = device;
+  if (cudaMemPoolCreate(&c->pool, &pp) != cudaSuccess) {
+    c->pool = nullptr;
     rc = MGCD_ERR_CUDA;
-  for (int i = 0; i < NSTREAMS && rc == MGCD_OK; ++i)
-    if (cudaEventCreate(&c->t_b0[i]) != cudaSuccess || cudaEventCreate(&c->t_b1[i]) != cudaSuccess) rc = MGCD_ERR_CUDA;
-  if (rc == MGCD_OK && c->mods.grow(mc.size() * sizeof(ModConstHost)) != cudaSuccess) rc = MGCD_ERR_CUDA;
+  }
+  if (rc == MGCD_OK) {
+    uint64_t keep = ~0ull;
+    cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  if (rc == MGCD_OK && c->main.create() != cudaSuccess) rc = MGCD_ERR_CUDA;
+  cudaStream_t s = c->main.stream;
+  if (rc == MGCD_OK && c->mods.grow(mc.size() * sizeof(ModConstHost), c->pool, s) != cudaSuccess) rc = MGCD_ERR_CUDA;
   if (rc == MGCD_OK &&
-      cudaMemcpy(c->mods.p, mc.data(), mc.size() * sizeof(ModConstHost), cudaMemcpyHostToDevice) != cudaSuccess)
+      cudaMemcpyAsync(c->mods.p, mc.data(), mc.size() * sizeof(ModConstHost), cudaMemcpyHostToDevice, s) != cudaSuccess)
     rc = MGCD_ERR_CUDA;
-  // Pairwise inverses of the first INVTAB_N moduli (every pair of the batched path), for
+  // Pairwise inverses of the first INVTAB_N moduli (every pair of the CTA classes), for
   // recovery: 1 GiB at n = 16,384.
   c->invtab_n = (uint32_t)std::min<size_t>(INVTAB_N, c->moduli.size());
-  if (rc == MGCD_OK && c->d_invtab.grow((size_t)c->invtab_n * c->invtab_n * sizeof(uint32_t)) != cudaSuccess)
+  if (rc == MGCD_OK && c->d_invtab.grow((size_t)c->invtab_n * c->invtab_n * sizeof(uint32_t), c->pool, s) != cudaSuccess)
     rc = MGCD_ERR_CUDA;
-  if (rc == MGCD_OK && (launch_build_invtab(c->mods.as<ModConst>(), c->invtab_n, c->d_invtab.as<uint32_t>(),
-                                            c->stream) != cudaSuccess ||
-                        cudaStreamSynchronize(c->stream) != cudaSuccess))
+  if (rc == MGCD_OK && (launch_build_invtab(c->mods.as<ModConst>(), c->invtab_n, c->d_invtab.as<uint32_t>(), s) !=
+                            cudaSuccess ||
+                        cudaStreamSynchronize(s) != cudaSuccess))
     rc = MGCD_ERR_CUDA;
   if (rc != MGCD_OK) {
     mgcd_destroy(c);
@@ -300,23 +279,16 @@ int mgcd_create(int device, int L, mgcd_context** out)
 int mgcd_destroy(mgcd_context* c)
 {
   if (!c) return MGCD_ERR_INVALID_ARG;
+  if (busy(c)) return MGCD_ERR_BUSY;
   cudaSetDevice(c->device);
-  if (c->stream) cudaStreamSynchronize(c->stream);
-  drop_graph(c);
-  for (DevBuf* b : {&c->mods, &c->d_limbs, &c->d_pairs, &c->d_order, &c->d_digits, &c->d_count, &c->d_iters,
-                    &c->d_status, &c->d_queue, &c->d_scratch, &c->d_gsync, &c->d_retry, &c->d_invtab})
-    b->release();
-  for (HostBuf* b : {&c->h_count, &c->h_iters, &c->h_status, &c->h_digits}) b->release();
-  for (int i = 0; i < NSTREAMS; ++i) {
-    if (c->bstream[i]) cudaStreamDestroy(c->bstream[i]);
-    if (c->ev_b[i]) cudaEventDestroy(c->ev_b[i]);
-    if (c->t_b0[i]) cudaEventDestroy(c->t_b0[i]);
-    if (c->t_b1[i]) cudaEventDestroy(c->t_b1[i]);
+  cudaStream_t s = c->main.stream;
+  if (s) {
+    cudaStreamSynchronize(s);
+    c->mods.release(s);
+    c->d_invtab.release(s);
   }
-  if (c->t_run0) cudaEventDestroy(c->t_run0);
-  if (c->t_run1) cudaEventDestroy(c->t_run1);
-  if (c->ev_start) cudaEventDestroy(c->ev_start);
-  if (c->stream) cudaStreamDestroy(c->stream);
+  c->main.destroy(c->pool);
+  if (c->pool) cudaMemPoolDestroy(c->pool);
   delete c;
   return MGCD_OK;
 }
@@ -342,30 +314,33 @@ int mgcd_moduli(const mgcd_context* c, uint32_t* out, size_t n)
   return MGCD_OK;
 }
 
+}  // extern "C"
+
 // ------------------------------------------------------------------------- batch ----
 
-static int schedule(mgcd_context* c, const std::vector<PairDesc>& descs, const std::vector<uint32_t>& subset,
+static int schedule(mgcd_context* c, Plan& P, const std::vector<PairDesc>& descs, const std::vector<uint32_t>& subset,
                     bool plain, std::vector<Bucket>& buckets, std::vector<uint32_t>& grid_pairs, size_t& scratch);
 
-static int plan_batch(mgcd_context* c, size_t np, const uint32_t* limbs, const uint64_t* u_off,
-                      const uint32_t* u_len, const uint64_t* v_off, const uint32_t* v_len, bool plain)
+int mgcd::plan_batch(mgcd_context* c, Plan& P, size_t np, const uint32_t* limbs, const uint64_t* u_off,
+                     const uint32_t* u_len, const uint64_t* v_off, const uint32_t* v_len, bool plain)
 {
   if (!c || (np && (!limbs || !u_off || !u_len || !v_off || !v_len))) return MGCD_ERR_INVALID_ARG;
   CK(cudaSetDevice(c->device));
-  CK(cudaStreamSynchronize(c->stream));   // buffers below may be reallocated
-  drop_graph(c);
-  c->np = np;
-  c->plain = plain;
-  c->ran = false;
-  c->status.assign(np, -1);
-  c->slot.assign(np, -1);
-  c->trivial.assign(np, {});
-  c->descs.clear();
-  c->ref_nq.clear();
-  c->grid_pairs.clear();
-  c->buckets.clear();
+  CK(cudaStreamSynchronize(P.stream));   // buffers below may be reallocated
+  P.drop_graph();
+  P.np = np;
+  P.plain = plain;
+  P.ran = false;
+  P.status.assign(np, -1);
+  P.slot.assign(np, -1);
+  P.trivial.assign(np, {});
+  P.descs.clear();
+  P.ref_nq.clear();
+  P.grid_pairs.clear();
+  P.buckets.clear();
   uint64_t limb_end = 0;
   uint32_t out_off = 0;
+  uint64_t glimbs = 0;
   for (size_t i = 0; i < np; ++i) {
     const uint32_t* u = limbs + u_off[i];
     const uint32_t* v = limbs + v_off[i];
@@ -373,8 +348,8 @@ static int plan_batch(mgcd_context* c, size_t np, const uint32_t* limbs, const u
     limb_end = std::max<uint64_t>(limb_end, std::max(u_off[i] + u_len[i], v_off[i] + v_len[i]));
     if (ul == 0 || vl == 0) {  // gcd(x, 0) = |x|: no modular work
       const uint32_t* x = ul ? u : v;
-      c->trivial[i].assign(x, x + (ul ? ul : vl));
-      c->status[i] = MGCD_OK;
+      P.trivial[i].assign(x, x + (ul ? ul : vl));
+      P.status[i] = MGCD_OK;
       continue;
     }
     PairDesc d;
@@ -387,7 +362,7 @@ static int plan_batch(mgcd_context* c, size_t np, const uint32_t* limbs, const u
     const size_t ubits = (size_t)(d.u_len - 1) * 32 + (32 - __builtin_clz(top));
     const int ref_nq = c->force_nq ? (int)c->force_nq : moduli_needed(c->L, ubits);
     if ((size_t)ref_nq > c->moduli.size()) {
-      c->status[i] = MGCD_ERR_NOT_ENOUGH_MODULI;
+      P.status[i] = MGCD_ERR_NOT_ENOUGH_MODULI;
       continue;
     }
     // Batches may use fewer moduli than the reference formula (less work per iteration);
@@ -399,48 +374,55 @@ static int plan_batch(mgcd_context* c, size_t np, const uint32_t* limbs, const u
     d.nq = (uint32_t)nq;
     d.out_off = out_off;
     out_off += (uint32_t)ref_nq + 1;
-    c->slot[i] = (int)c->descs.size();
-    c->descs.push_back(d);
-    c->ref_nq.push_back((uint32_t)ref_nq);
+    d.g_off = glimbs;                 // gcd <= the smaller operand
+    d.g_cap = d.v_len;
+    d.pad_ = 0;
+    glimbs += d.g_cap;
+    P.slot[i] = (int)P.descs.size();
+    P.descs.push_back(d);
+    P.ref_nq.push_back((uint32_t)ref_nq);
   }
-  c->ndig = out_off;
-  const size_t ng = c->descs.size();
-  c->order.clear();
+  P.ndig = out_off;
+  P.nglimbs = glimbs;
+  const size_t ng = P.descs.size();
+  P.order.clear();
   std::vector<uint32_t> all(ng);
   for (uint32_t k = 0; k < ng; ++k) all[k] = k;
   size_t scratch = 0;
-  int rc = schedule(c, c->descs, all, plain, c->buckets, c->grid_pairs, scratch);
+  int rc = schedule(c, P, P.descs, all, plain, P.buckets, P.grid_pairs, scratch);
   if (rc != MGCD_OK) return rc;
-  c->scratch_words = scratch;
-  c->eff_nq.clear();
-  for (const PairDesc& d : c->descs) c->eff_nq.push_back(d.nq);
+  P.scratch_words = scratch;
+  P.eff_nq.clear();
+  for (const PairDesc& d : P.descs) P.eff_nq.push_back(d.nq);
 
   // Device buffers and upload.
-  CK(c->d_limbs.grow(std::max<uint64_t>(limb_end, 1) * sizeof(uint32_t)));
-  CK(c->d_pairs.grow(std::max<size_t>(ng, 1) * sizeof(PairDesc)));
-  CK(c->d_order.grow(std::max<size_t>(c->order.size(), 1) * sizeof(uint32_t)));
-  CK(c->d_digits.grow(std::max<size_t>(c->ndig, 1) * sizeof(mgcd_pair)));
-  CK(c->d_count.grow(std::max<size_t>(ng, 1) * sizeof(uint32_t)));
-  CK(c->d_iters.grow(std::max<size_t>(ng, 1) * sizeof(uint32_t)));
-  CK(c->d_status.grow(std::max<size_t>(ng, 1) * sizeof(int32_t)));
-  CK(c->d_queue.grow(2 * NSTREAMS * sizeof(uint32_t)));
-  CK(c->d_scratch.grow(std::max<size_t>(scratch, 1) * sizeof(uint32_t)));
-  CK(c->d_gsync.grow(sizeof(GridSync)));
-  c->h2d_bytes = ng ? limb_end * sizeof(uint32_t) + ng * sizeof(PairDesc) + c->order.size() * sizeof(uint32_t) : 0;
+  cudaStream_t s = P.stream;
+  CK(P.d_limbs.grow(std::max<uint64_t>(limb_end, 1) * sizeof(uint32_t), c->pool, s));
+  CK(P.d_pairs.grow(std::max<size_t>(ng, 1) * sizeof(PairDesc), c->pool, s));
+  CK(P.d_order.grow(std::max<size_t>(P.order.size(), 1) * sizeof(uint32_t), c->pool, s));
+  CK(P.d_digits.grow(std::max<size_t>(P.ndig, 1) * sizeof(mgcd_pair), c->pool, s));
+  CK(P.d_count.grow(std::max<size_t>(ng, 1) * sizeof(uint32_t), c->pool, s));
+  CK(P.d_iters.grow(std::max<size_t>(ng, 1) * sizeof(uint32_t), c->pool, s));
+  CK(P.d_status.grow(std::max<size_t>(ng, 1) * sizeof(int32_t), c->pool, s));
+  CK(P.d_queue.grow(2 * NSTREAMS * sizeof(uint32_t), c->pool, s));
+  CK(P.d_scratch.grow(std::max<size_t>(scratch, 1) * sizeof(uint32_t), c->pool, s));
+  CK(P.d_gsync.grow(sizeof(GridSync), c->pool, s));
+  CK(P.d_glimbs.grow(std::max<size_t>(P.nglimbs, 1) * sizeof(uint32_t), c->pool, s));
+  CK(P.d_glen.grow(std::max<size_t>(ng, 1) * sizeof(uint32_t), c->pool, s));
+  P.h2d_bytes = ng ? limb_end * sizeof(uint32_t) + ng * sizeof(PairDesc) + P.order.size() * sizeof(uint32_t) : 0;
   if (ng) {
-    CK(cudaMemcpyAsync(c->d_limbs.p, limbs, limb_end * sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream));
-    CK(cudaMemcpyAsync(c->d_pairs.p, c->descs.data(), ng * sizeof(PairDesc), cudaMemcpyHostToDevice, c->stream));
-    if (!c->order.empty())
-      CK(cudaMemcpyAsync(c->d_order.p, c->order.data(), c->order.size() * sizeof(uint32_t),
-                         cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(P.d_limbs.p, limbs, limb_end * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(P.d_pairs.p, P.descs.data(), ng * sizeof(PairDesc), cudaMemcpyHostToDevice, s));
+    if (!P.order.empty())
+      CK(cudaMemcpyAsync(P.d_order.p, P.order.data(), P.order.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
   }
   return MGCD_OK;
 }
 
 // Groups the pairs `subset` (indices into descs) into size-class buckets (batches) or
-// single-pair launches (plain); appends the processing order to c->order and returns the
+// single-pair launches (plain); appends the processing order to P.order and returns the
 // scratch words needed.
-static int schedule(mgcd_context* c, const std::vector<PairDesc>& descs, const std::vector<uint32_t>& subset,
+static int schedule(mgcd_context* c, Plan& P, const std::vector<PairDesc>& descs, const std::vector<uint32_t>& subset,
                     bool plain, std::vector<Bucket>& buckets, std::vector<uint32_t>& grid_pairs, size_t& scratch)
 {
   buckets.clear();
@@ -455,12 +437,7 @@ static int schedule(mgcd_context* c, const std::vector<PairDesc>& descs, const s
       byb[size_class(nq)].push_back(k);
     }
   }
-  int kThreads[NSTREAMS], kSlots[NSTREAMS];
-  for (int b = 0; b < NSTREAMS; ++b) {
-    kThreads[b] = c->cfg[b].threads;
-    kSlots[b] = c->cfg[b].k;
-  }
-  for (int b = NSTREAMS - 1; b >= 0; --b) {  // largest CTA size first: its pairs are the longest
+  for (int b = NSTREAMS - 1; b >= 0; --b) {  // largest class first: its pairs are the longest
     auto& v = byb[b];
     if (v.empty()) continue;
     std::sort(v.begin(), v.end(), [&](uint32_t x, uint32_t y) {
@@ -469,11 +446,11 @@ static int schedule(mgcd_context* c, const std::vector<PairDesc>& descs, const s
       return a.u_len + a.v_len > bb.u_len + bb.v_len;
     });
     Bucket bk;
-    bk.threads = plain ? 256 : kThreads[b];
-    bk.k = plain ? 1 : kSlots[b];
+    bk.threads = plain ? 256 : c->cfg[b].threads;
+    bk.k = plain ? 1 : c->cfg[b].k;
     bk.csize = 0;
     bk.cls = b;
-    bk.first = (uint32_t)c->order.size();
+    bk.first = (uint32_t)P.order.size();
     bk.n = (uint32_t)v.size();
     bk.nq_max = descs[v[0]].nq;
     bk.scratch_off = scratch;
@@ -498,20 +475,358 @@ static int schedule(mgcd_context* c, const std::vector<PairDesc>& descs, const s
       bk.grid = (int)std::min<size_t>((v.size() + bk.k - 1) / bk.k, (size_t)c->sms * bps);
       scratch += (size_t)bk.grid * 4 * bk.k * bk.nq_max;
     }
-    c->order.insert(c->order.end(), v.begin(), v.end());
+    P.order.insert(P.order.end(), v.begin(), v.end());
     buckets.push_back(bk);
   }
   uint32_t grid_nq_max = 0;
   for (uint32_t k : grid_pairs) grid_nq_max = std::max(grid_nq_max, descs[k].nq);
-  c->grid_scratch_off = scratch;
+  P.grid_scratch_off = scratch;
   scratch += 4 * (size_t)grid_nq_max;
   return MGCD_OK;
 }
 
+// Launches the buckets (one stream each, joined back into P.stream) and then the
+// single-pair launches.  `pairs` is the descriptor array on the device, `queue_base` the
+// first of the bucket work counters (zeroed here).
+static int launch_set(mgcd_context* c, Plan& P, const std::vector<Bucket>& buckets,
+                      const std::vector<uint32_t>& grid_pairs, const std::vector<PairDesc>& descs, PairDesc* pairs,
+                      uint32_t* queue_base, bool time_buckets)
+{
+  CK(cudaMemsetAsync(queue_base, 0, NSTREAMS * sizeof(uint32_t), P.stream));
+  CK(cudaEventRecord(P.ev_start, P.stream));
+  for (size_t b = 0; b < buckets.size(); ++b) {
+    const Bucket& bk = buckets[b];
+    BatchArgs a;
+    a.inv = InvTab{c->d_invtab.as<uint32_t>(), c->invtab_n};
+    a.limbs = P.d_limbs.as<uint32_t>();
+    a.pairs = pairs;
+    a.order = P.d_order.as<uint32_t>() + bk.first;
+    a.npairs = bk.n;
+    a.mods = c->mods.as<ModConst>();
+    a.L = c->L;
+    a.queue = queue_base + b;
+    a.scratch = P.d_scratch.as<uint32_t>() + bk.scratch_off;
+    a.scratch_words = 4 * (size_t)bk.k * bk.nq_max;
+    a.nq_max = bk.nq_max;
+    a.digits = P.d_digits.as<mgcd_pair>();
+    a.count = P.d_count.as<uint32_t>();
+    a.iters = P.d_iters.as<uint32_t>();
+    a.status = P.d_status.as<int32_t>();
+    CK(cudaStreamWaitEvent(P.bstream[b], P.ev_start, 0));
+    if (time_buckets) CK(cudaEventRecord(P.t_b0[b], P.bstream[b]));
+    if (bk.csize)
+      CK(launch_cluster_batch(a, bk.threads, bk.csize, bk.grid, bk.smem, P.bstream[b]));
+    else
+      CK(launch_batch(a, bk.threads, bk.k, bk.grid, bk.smem, P.bstream[b]));
+    if (time_buckets) CK(cudaEventRecord(P.t_b1[b], P.bstream[b]));
+    CK(cudaEventRecord(P.ev_b[b], P.bstream[b]));
+    ++P.launches;
+  }
+  for (size_t b = 0; b < buckets.size(); ++b) CK(cudaStreamWaitEvent(P.stream, P.ev_b[b], 0));
+
+  for (uint32_t k : grid_pairs) {
+    const PairDesc& d = descs[k];
+    GridArgs g;
+    g.inv = InvTab{c->d_invtab.as<uint32_t>(), c->invtab_n};
+    g.limbs = P.d_limbs.as<uint32_t>();
+    g.pair = d;
+    g.mods = c->mods.as<ModConst>();
+    g.L = c->L;
+    g.scratch = P.d_scratch.as<uint32_t>() + P.grid_scratch_off;
+    g.digits = P.d_digits.as<mgcd_pair>();
+    g.count = P.d_count.as<uint32_t>() + k;
+    g.iters = P.d_iters.as<uint32_t>() + k;
+    g.status = P.d_status.as<int32_t>() + k;
+    const bool ref_shape = c->single_policy == MGCD_SINGLE_REFERENCE_SHAPE;
+    if (!ref_shape && d.nq <= (uint32_t)MAX_CLUSTER * 1024) {
+      // thread-block cluster: as many CTAs (<= 16) as keep one modulus per thread
+      const int ctas = (int)std::min<uint32_t>(MAX_CLUSTER, (d.nq + 255) / 256);
+      const uint32_t per = (d.nq + ctas - 1) / ctas;
+      const int threads = per <= 256 ? 256 : per <= 512 ? 512 : 1024;
+      g.per_cta = per;
+      g.sync = nullptr;
+      if (launch_cluster(g, threads, ctas, grid_smem_bytes(per), P.stream) != cudaSuccess) return MGCD_ERR_GRID;
+      ++P.launches;
+      continue;
+    }
+    // cooperative grid: one CTA per SM (or the reference's shape: 256-thread CTAs, 256 moduli)
+    uint32_t per = ref_shape ? 256u : std::max<uint32_t>(32, (d.nq + c->sms - 1) / c->sms);
+    const int threads = (ref_shape || per <= 256) ? 256 : per <= 512 ? 512 : GRID_THREADS;
+    int bps = 0;
+    if (grid_max_blocks_per_sm(threads, grid_smem_bytes(per), &bps) != cudaSuccess || bps < 1) return MGCD_ERR_GRID;
+    uint32_t grid = (d.nq + per - 1) / per;
+    if (grid > (uint32_t)(c->sms * bps)) {
+      per = (d.nq + c->sms * bps - 1) / (c->sms * bps);
+      grid = (d.nq + per - 1) / per;
+      if (grid_max_blocks_per_sm(threads, grid_smem_bytes(per), &bps) != cudaSuccess ||
+          grid > (uint32_t)(c->sms * bps))
+        return MGCD_ERR_GRID;
+    }
+    g.per_cta = per;
+    g.sync = P.d_gsync.as<GridSync>();
+    CK(launch_gridsync_init(g.sync, c->wait_timeout_ns, c->withhold_cta, P.stream));
+    ++P.launches;
+    cudaError_t e = launch_grid(g, threads, (int)grid, grid_smem_bytes(per), P.stream);
+    if (e == cudaErrorCooperativeLaunchTooLarge) return MGCD_ERR_GRID;
+    if (e != cudaSuccess) return MGCD_ERR_CUDA;
+    ++P.launches;
+  }
+  return MGCD_OK;
+}
+
+// Converts every GPU pair's digits to binary limbs on P.stream (after the gcd kernels).
+static int launch_convert(mgcd_context* c, Plan& P)
+{
+  const uint32_t ng = (uint32_t)P.descs.size();
+  const int grid = (int)std::min<uint32_t>(ng, (uint32_t)c->sms * 2);
+  CK(launch_radix(P.d_pairs.as<PairDesc>(), ng, P.d_digits.as<mgcd_pair>(), P.d_count.as<uint32_t>(),
+                  P.d_status.as<int32_t>(), P.d_glimbs.as<uint32_t>(), P.d_glen.as<uint32_t>(), grid, P.stream));
+  ++P.launches;
+  return MGCD_OK;
+}
+
+int mgcd::run_plan(mgcd_context* c, Plan& P)
+{
+  if (!c) return MGCD_ERR_INVALID_ARG;
+  CK(cudaSetDevice(c->device));
+  P.launches = 0;
+  P.retried = 0;
+  const size_t ng = P.descs.size();
+  if (ng == 0) {
+    P.ran = true;
+    P.synced = true;
+    return MGCD_OK;
+  }
+  for (size_t k = 0; k < ng; ++k) P.eff_nq[k] = P.descs[k].nq;
+  if (c->use_graph && P.graphable && !P.plain) {
+    if (!P.graph) {
+      // Record the run once (status reset, queue reset, every bucket kernel on its stream,
+      // joined back into P.stream); each later run is a single graph launch.
+      CK(cudaStreamBeginCapture(P.stream, cudaStreamCaptureModeThreadLocal));
+      int rc = MGCD_OK;
+      if (cudaMemsetAsync(P.d_status.p, 0xFF, ng * sizeof(int32_t), P.stream) != cudaSuccess) rc = MGCD_ERR_CUDA;
+      if (rc == MGCD_OK)
+        rc = launch_set(c, P, P.buckets, P.grid_pairs, P.descs, P.d_pairs.as<PairDesc>(), P.d_queue.as<uint32_t>(),
+                        false);
+      if (rc == MGCD_OK) rc = launch_convert(c, P);
+      cudaGraph_t g = nullptr;
+      const cudaError_t e = cudaStreamEndCapture(P.stream, &g);
+      if (rc == MGCD_OK && e != cudaSuccess) rc = MGCD_ERR_CUDA;
+      if (rc == MGCD_OK && cudaGraphInstantiate(&P.graph, g, 0) != cudaSuccess) {
+        P.graph = nullptr;
+        rc = MGCD_ERR_CUDA;
+      }
+      if (g) cudaGraphDestroy(g);
+      if (rc != MGCD_OK) return rc;
+      P.graph_kernels = P.launches;
+    }
+    CK(cudaEventRecord(P.t_run0, P.stream));
+    CK(cudaGraphLaunch(P.graph, P.stream));
+    P.launches = P.graph_kernels;
+    P.bucket_timed = false;
+  } else {
+    CK(cudaEventRecord(P.t_run0, P.stream));
+    CK(cudaMemsetAsync(P.d_status.p, 0xFF, ng * sizeof(int32_t), P.stream));
+    int rc = launch_set(c, P, P.buckets, P.grid_pairs, P.descs, P.d_pairs.as<PairDesc>(), P.d_queue.as<uint32_t>(),
+                        true);
+    if (rc == MGCD_OK) rc = launch_convert(c, P);
+    if (rc != MGCD_OK) return rc;
+    P.bucket_timed = true;
+  }
+  CK(cudaEventRecord(P.t_run1, P.stream));
+  P.ran = true;
+  P.synced = false;
+  return MGCD_OK;
+}
+
+// Waits for the run; pairs that ran with fewer moduli than the reference count and could
+// not be certified are rerun once with the reference count (same digit slots).
+int mgcd::sync_plan(mgcd_context* c, Plan& P)
+{
+  if (!c || !P.ran) return MGCD_ERR_INVALID_ARG;
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(P.stream));
+  if (P.synced) return MGCD_OK;
+  P.synced = true;
+  const size_t ng = P.descs.size();
+  bool scaled = false;
+  for (size_t k = 0; k < ng && !scaled; ++k) scaled = P.descs[k].nq < P.ref_nq[k];
+  if (!scaled) return MGCD_OK;
+  CK(P.h_status.grow(ng * sizeof(int32_t)));
+  CK(cudaMemcpyAsync(P.h_status.p, P.d_status.p, ng * sizeof(int32_t), cudaMemcpyDeviceToHost, P.stream));
+  CK(cudaStreamSynchronize(P.stream));
+  const int32_t* st = P.h_status.as<int32_t>();
+  std::vector<uint32_t> redo;
+  for (uint32_t k = 0; k < ng; ++k)
+    if (st[k] != ST_OK && st[k] != ST_TIMEOUT && P.descs[k].nq < P.ref_nq[k]) redo.push_back(k);
+  if (redo.empty()) return MGCD_OK;
+  std::vector<PairDesc> rd = P.descs;
+  for (uint32_t k : redo) {
+    rd[k].nq = P.ref_nq[k];
+    P.eff_nq[k] = P.ref_nq[k];
+  }
+  const size_t main_order = P.order.size();
+  std::vector<Bucket> bks;
+  std::vector<uint32_t> gp;
+  size_t scratch = 0;
+  const size_t keep_grid_off = P.grid_scratch_off;
+  int rc = schedule(c, P, rd, redo, false, bks, gp, scratch);
+  if (rc != MGCD_OK) return rc;
+  // device buffers: retry descriptors after the main ones, retry order after the main order
+  cudaStream_t s = P.stream;
+  CK(P.d_retry.grow(ng * sizeof(PairDesc), c->pool, s));
+  if (P.order.size() * sizeof(uint32_t) > P.d_order.bytes) {
+    // keep the main order: grow by copying
+    DevBuf nb;
+    CK(nb.grow(P.order.size() * sizeof(uint32_t), c->pool, s));
+    CK(cudaMemcpyAsync(nb.p, P.d_order.p, main_order * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+    P.drop_graph();
+    P.d_order.release(s);
+    P.d_order = nb;
+  }
+  if (scratch > P.d_scratch.bytes / sizeof(uint32_t)) {
+    P.drop_graph();
+    P.d_scratch.release(s);
+    CK(P.d_scratch.grow(scratch * sizeof(uint32_t), c->pool, s));
+  }
+  CK(cudaMemcpyAsync(P.d_retry.p, rd.data(), ng * sizeof(PairDesc), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(P.d_order.as<uint32_t>() + main_order, P.order.data() + main_order,
+                     (P.order.size() - main_order) * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+  rc = launch_set(c, P, bks, gp, rd, P.d_retry.as<PairDesc>(), P.d_queue.as<uint32_t>() + NSTREAMS, false);
+  P.order.resize(main_order);               // the plan itself is unchanged for later runs
+  P.grid_scratch_off = keep_grid_off;
+  if (rc == MGCD_OK) rc = launch_convert(c, P);   // same digit and limb slots: convert again
+  if (rc != MGCD_OK) return rc;
+  CK(cudaEventRecord(P.t_run1, s));
+  CK(cudaStreamSynchronize(s));
+  P.retried = (int)redo.size();
+  return MGCD_OK;
+}
+
+// Copies the GPU results of the plan to pinned host memory.
+int mgcd::fetch(mgcd_context* c, Plan& P)
+{
+  const size_t ng = P.descs.size();
+  CK(cudaSetDevice(c->device));
+  if (ng == 0) return MGCD_OK;
+  CK(P.h_count.grow(ng * sizeof(uint32_t)));
+  CK(P.h_iters.grow(ng * sizeof(uint32_t)));
+  CK(P.h_status.grow(ng * sizeof(int32_t)));
+  CK(P.h_glen.grow(ng * sizeof(uint32_t)));
+  CK(P.h_glimbs.grow(std::max<size_t>(P.nglimbs, 1) * sizeof(uint32_t)));
+  if (P.plain) CK(P.h_digits.grow(std::max<size_t>(P.ndig, 1) * sizeof(mgcd_pair)));
+  cudaStream_t s = P.stream;
+  // Results as binary limbs (converted on the device); digits only where the caller wants
+  // them (single pairs) or the host converts (very long gcds).
+  CK(cudaMemcpyAsync(P.h_count.p, P.d_count.p, ng * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(P.h_iters.p, P.d_iters.p, ng * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(P.h_status.p, P.d_status.p, ng * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(P.h_glen.p, P.d_glen.p, ng * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(P.h_glimbs.p, P.d_glimbs.p, P.nglimbs * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  uint64_t d2h = ng * 4 * sizeof(uint32_t) + P.nglimbs * sizeof(uint32_t);
+  if (P.plain) {
+    CK(cudaMemcpyAsync(P.h_digits.p, P.d_digits.p, P.ndig * sizeof(mgcd_pair), cudaMemcpyDeviceToHost, s));
+    d2h += P.ndig * sizeof(mgcd_pair);
+  }
+  CK(cudaStreamSynchronize(s));
+  if (!P.plain) {
+    const uint32_t* gl = P.h_glen.as<uint32_t>();
+    const int32_t* st0 = P.h_status.as<int32_t>();
+    bool any = false;
+    for (size_t k = 0; k < ng && !any; ++k) any = gl[k] == RADIX_HOST && st0[k] == ST_OK;
+    if (any) CK(P.h_digits.grow(std::max<size_t>(P.ndig, 1) * sizeof(mgcd_pair)));
+    any = false;
+    for (size_t k = 0; k < ng; ++k) {
+      if (gl[k] != RADIX_HOST || st0[k] != ST_OK) continue;
+      const PairDesc& d = P.descs[k];
+      const size_t n = P.h_count.as<uint32_t>()[k];
+      CK(cudaMemcpyAsync(P.h_digits.as<mgcd_pair>() + d.out_off, P.d_digits.as<mgcd_pair>() + d.out_off,
+                         n * sizeof(mgcd_pair), cudaMemcpyDeviceToHost, s));
+      d2h += n * sizeof(mgcd_pair);
+      any = true;
+    }
+    if (any) CK(cudaStreamSynchronize(s));
+  }
+  P.d2h_bytes = d2h;
+  // work by the cost model
+  const uint32_t* it = P.h_iters.as<uint32_t>();
+  const uint32_t* cnt = P.h_count.as<uint32_t>();
+  const int32_t* st = P.h_status.as<int32_t>();
+  double R = 0, E = 0, M = 0, B = 0;
+  for (size_t k = 0; k < ng; ++k) {
+    const PairDesc& d = P.descs[k];
+    R += (double)d.nq * (d.u_len + d.v_len);
+    B += 4.0 * (d.u_len + d.v_len);
+    if (st[k] != ST_OK) continue;
+    const double I = it[k], K = cnt[k], N = P.eff_nq[k];
+    E += I * N - I * (I + 1) / 2;
+    M += K * (N - I) - K * (K + 1) / 2;
+  }
+  P.work[0] = R; P.work[1] = E; P.work[2] = M; P.work[3] = B;
+  return MGCD_OK;
+}
+
+int mgcd::convert_all(mgcd_context* c, Plan& P, uint32_t* g, const uint64_t* g_off, const uint32_t* g_cap,
+                      uint32_t* g_len, int32_t* status, bool threaded)
+{
+  (void)c;
+  const size_t np = P.np;
+  const mgcd_pair* dig = P.h_digits.as<mgcd_pair>();
+  const uint32_t* cnt = P.h_count.as<uint32_t>();
+  const int32_t* st = P.h_status.as<int32_t>();
+  const uint32_t* gl = P.h_glen.as<uint32_t>();
+  const uint32_t* gv = P.h_glimbs.as<uint32_t>();
+  std::atomic<size_t> next{0};
+  auto work = [&]() {
+    for (;;) {
+      const size_t i = next.fetch_add(1);
+      if (i >= np) break;
+      int s = P.status[i];
+      size_t len = 0;
+      if (P.slot[i] >= 0) {
+        const int k = P.slot[i];
+        s = to_status(st[k]);
+        if (s != MGCD_OK) {
+        } else if (gl[k] != RADIX_HOST) {           // converted on the device
+          len = gl[k];
+          if (len > g_cap[i]) { s = MGCD_ERR_CAPACITY; len = 0; }
+          else if (len) std::memcpy(g + g_off[i], gv + P.descs[k].g_off, len * sizeof(uint32_t));
+        } else if (mixed_radix_to_limbs(dig + P.descs[k].out_off, cnt[k], g + g_off[i], g_cap[i], &len)) {
+          s = MGCD_ERR_CAPACITY;
+        }
+      } else if (s == MGCD_OK) {
+        len = P.trivial[i].size();
+        if (len > g_cap[i]) { s = MGCD_ERR_CAPACITY; len = 0; }
+        else if (len) std::memcpy(g + g_off[i], P.trivial[i].data(), len * sizeof(uint32_t));
+      }
+      g_len[i] = (uint32_t)len;
+      if (status) status[i] = s;
+    }
+  };
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t nt = threaded ? std::min<size_t>(hw, (np + 15) / 16) : 1;
+  if (nt <= 1) {
+    work();
+  } else {
+    std::vector<std::thread> th;
+    for (size_t t = 0; t < nt; ++t) th.emplace_back(work);
+    for (auto& t : th) t.join();
+  }
+  int rc = MGCD_OK;
+  for (size_t i = 0; i < np && rc == MGCD_OK; ++i) {
+    if (status) { if (status[i] != MGCD_OK) rc = status[i]; }
+  }
+  return rc;
+}
+
+extern "C" {
+
 int mgcd_batch_upload(mgcd_context* c, size_t np, const uint32_t* limbs, const uint64_t* u_off,
                       const uint32_t* u_len, const uint64_t* v_off, const uint32_t* v_len)
 {
-  return plan_batch(c, np, limbs, u_off, u_len, v_off, v_len, false);
+  if (!c) return MGCD_ERR_INVALID_ARG;
+  if (busy(c)) return MGCD_ERR_BUSY;
+  return plan_batch(c, c->main, np, limbs, u_off, u_len, v_off, v_len, false);
 }
 
 int mgcd_set_nq_scale(mgcd_context* c, float scale)
@@ -547,14 +862,60 @@ int mgcd_get_cluster_size(const mgcd_context* c, int* ctas)
   return MGCD_OK;
 }
 
+// Tuning table: one line per size class, "class threads k nq_scale cluster_ctas" ('#' starts
+// a comment).  All lines are checked before any is applied.
+int mgcd_load_tuning(mgcd_context* c, const char* path)
+{
+  if (!c || !path) return MGCD_ERR_INVALID_ARG;
+  FILE* f = std::fopen(path, "r");
+  if (!f) return MGCD_ERR_INVALID_ARG;
+  mgcd_context::ClassCfg cfg[NSTREAMS];
+  static_assert(sizeof(cfg) == sizeof(c->cfg), "copy of the whole table");
+  std::memcpy(cfg, c->cfg, sizeof(cfg));
+  char line[256];
+  int rc = MGCD_OK;
+  while (rc == MGCD_OK && std::fgets(line, sizeof line, f)) {
+    const char* s = line;
+    while (*s == ' ' || *s == '\t') ++s;
+    if (*s == '#' || *s == '\n' || *s == '\r' || *s == 0) continue;
+    int cls, threads, k, cs;
+    float sc;
+    if (std::sscanf(s, "%d %d %d %f %d", &cls, &threads, &k, &sc, &cs) != 5 || cls < 0 || cls >= NSTREAMS ||
+        (threads != 256 && threads != 512 && threads != 1024) || !(sc >= 0.5f && sc <= 1.0f) ||
+        (k != 1 && k != 2 && !(k == 4 && threads <= 512)) ||
+        (cls == CLUSTER_CLASS ? (k != 1 || cs < 2 || cs > MAX_CLUSTER) : cs != 0)) {
+      rc = MGCD_ERR_INVALID_ARG;
+      break;
+    }
+    cfg[cls].threads = threads;
+    cfg[cls].k = k;
+    cfg[cls].nq_scale = sc;
+    cfg[cls].csize = cs;
+  }
+  std::fclose(f);
+  if (rc == MGCD_OK) std::memcpy(c->cfg, cfg, sizeof(cfg));
+  return rc;
+}
+
+int mgcd_save_tuning(const mgcd_context* c, const char* path)
+{
+  if (!c || !path) return MGCD_ERR_INVALID_ARG;
+  FILE* f = std::fopen(path, "w");
+  if (!f) return MGCD_ERR_INVALID_ARG;
+  std::fprintf(f, "# modgcd tuning table (modulus width %d): class threads k nq_scale cluster_ctas\n", c->L);
+  for (int i = 0; i < NSTREAMS; ++i)
+    std::fprintf(f, "%d %d %d %.3f %d\n", i, c->cfg[i].threads, c->cfg[i].k, c->cfg[i].nq_scale, c->cfg[i].csize);
+  return std::fclose(f) == 0 ? MGCD_OK : MGCD_ERR_INVALID_ARG;
+}
+
 int mgcd_batch_use_graph(mgcd_context* c, int enable)
 {
   if (!c) return MGCD_ERR_INVALID_ARG;
   c->use_graph = enable != 0;
   if (!c->use_graph) {
     cudaSetDevice(c->device);
-    cudaStreamSynchronize(c->stream);
-    drop_graph(c);
+    cudaStreamSynchronize(c->main.stream);
+    c->main.drop_graph();
   }
   return MGCD_OK;
 }
@@ -570,8 +931,8 @@ int mgcd_set_wait_timeout_ms(mgcd_context* c, unsigned ms)
 {
   if (!c || ms == 0) return MGCD_ERR_INVALID_ARG;
   c->wait_timeout_ns = (unsigned long long)ms * 1000000ull;
-  cudaStreamSynchronize(c->stream);
-  drop_graph(c);
+  cudaStreamSynchronize(c->main.stream);
+  c->main.drop_graph();
   return MGCD_OK;
 }
 
@@ -586,8 +947,8 @@ int mgcd_test_withhold_cta(mgcd_context* c, int cta)
 {
   if (!c) return MGCD_ERR_INVALID_ARG;
   c->withhold_cta = cta < 0 ? 0xFFFFFFFFu : (uint32_t)cta;
-  cudaStreamSynchronize(c->stream);
-  drop_graph(c);
+  cudaStreamSynchronize(c->main.stream);
+  c->main.drop_graph();
   return MGCD_OK;
 }
 
@@ -602,225 +963,32 @@ int mgcd_get_size_class(const mgcd_context* c, int cls, int* threads, int* k, fl
 
 int mgcd_batch_kernel_stats(const mgcd_context* c, int i, int* cls, int* pairs, float* ms)
 {
-  if (!c || !c->ran || !c->bucket_timed || i < 0 || i >= (int)c->buckets.size()) return MGCD_ERR_INVALID_ARG;
-  float t = 0.f;
-  CK(cudaEventElapsedTime(&t, c->t_b0[i], c->t_b1[i]));
-  if (cls) *cls = c->buckets[i].cls;
-  if (pairs) *pairs = (int)c->buckets[i].n;
-  if (ms) *ms = t;
-  return MGCD_OK;
-}
-
-// Launches the buckets (one stream each, joined back into c->stream) and then the
-// cooperative-grid pairs.  `pairs` is the descriptor array on the device, `queue_base`
-// the first of the bucket work counters (zeroed here).
-static int launch_set(mgcd_context* c, const std::vector<Bucket>& buckets, const std::vector<uint32_t>& grid_pairs,
-                      const std::vector<PairDesc>& descs, PairDesc* pairs, uint32_t* queue_base, bool time_buckets)
-{
-  CK(cudaMemsetAsync(queue_base, 0, NSTREAMS * sizeof(uint32_t), c->stream));
-  CK(cudaEventRecord(c->ev_start, c->stream));
-  for (size_t b = 0; b < buckets.size(); ++b) {
-    const Bucket& bk = buckets[b];
-    BatchArgs a;
-    a.inv = InvTab{c->d_invtab.as<uint32_t>(), c->invtab_n};
-    a.limbs = c->d_limbs.as<uint32_t>();
-    a.pairs = pairs;
-    a.order = c->d_order.as<uint32_t>() + bk.first;
-    a.npairs = bk.n;
-    a.mods = c->mods.as<ModConst>();
-    a.L = c->L;
-    a.queue = queue_base + b;
-    a.scratch = c->d_scratch.as<uint32_t>() + bk.scratch_off;
-    a.scratch_words = 4 * (size_t)bk.k * bk.nq_max;
-    a.nq_max = bk.nq_max;
-    a.digits = c->d_digits.as<mgcd_pair>();
-    a.count = c->d_count.as<uint32_t>();
-    a.iters = c->d_iters.as<uint32_t>();
-    a.status = c->d_status.as<int32_t>();
-    CK(cudaStreamWaitEvent(c->bstream[b], c->ev_start, 0));
-    if (time_buckets) CK(cudaEventRecord(c->t_b0[b], c->bstream[b]));
-    if (bk.csize)
-      CK(launch_cluster_batch(a, bk.threads, bk.csize, bk.grid, bk.smem, c->bstream[b]));
-    else
-      CK(launch_batch(a, bk.threads, bk.k, bk.grid, bk.smem, c->bstream[b]));
-    if (time_buckets) CK(cudaEventRecord(c->t_b1[b], c->bstream[b]));
-    CK(cudaEventRecord(c->ev_b[b], c->bstream[b]));
-    ++c->launches;
-  }
-  for (size_t b = 0; b < buckets.size(); ++b) CK(cudaStreamWaitEvent(c->stream, c->ev_b[b], 0));
-
-  if (!grid_pairs.empty()) {
-    for (uint32_t k : grid_pairs) {
-      const PairDesc& d = descs[k];
-      GridArgs g;
-      g.inv = InvTab{c->d_invtab.as<uint32_t>(), c->invtab_n};
-      g.limbs = c->d_limbs.as<uint32_t>();
-      g.pair = d;
-      g.mods = c->mods.as<ModConst>();
-      g.L = c->L;
-      g.scratch = c->d_scratch.as<uint32_t>() + c->grid_scratch_off;
-      g.digits = c->d_digits.as<mgcd_pair>();
-      g.count = c->d_count.as<uint32_t>() + k;
-      g.iters = c->d_iters.as<uint32_t>() + k;
-      g.status = c->d_status.as<int32_t>() + k;
-      const bool ref_shape = c->single_policy == MGCD_SINGLE_REFERENCE_SHAPE;
-      if (!ref_shape && d.nq <= (uint32_t)MAX_CLUSTER * 1024) {
-        // thread-block cluster: as many CTAs (<= 16) as keep one modulus per thread
-        const int ctas = (int)std::min<uint32_t>(MAX_CLUSTER, (d.nq + 255) / 256);
-        const uint32_t per = (d.nq + ctas - 1) / ctas;
-        const int threads = per <= 256 ? 256 : per <= 512 ? 512 : 1024;
-        g.per_cta = per;
-        g.sync = nullptr;
-        if (launch_cluster(g, threads, ctas, grid_smem_bytes(per), c->stream) != cudaSuccess) return MGCD_ERR_GRID;
-        ++c->launches;
-        continue;
-      }
-      // cooperative grid: one CTA per SM (or the reference's shape: 256-thread CTAs, 256 moduli)
-      uint32_t per = ref_shape ? 256u : std::max<uint32_t>(32, (d.nq + c->sms - 1) / c->sms);
-      const int threads = (ref_shape || per <= 256) ? 256 : per <= 512 ? 512 : GRID_THREADS;
-      int bps = 0;
-      if (grid_max_blocks_per_sm(threads, grid_smem_bytes(per), &bps) != cudaSuccess || bps < 1) return MGCD_ERR_GRID;
-      uint32_t grid = (d.nq + per - 1) / per;
-      if (grid > (uint32_t)(c->sms * bps)) {
-        per = (d.nq + c->sms * bps - 1) / (c->sms * bps);
-        grid = (d.nq + per - 1) / per;
-        if (grid_max_blocks_per_sm(threads, grid_smem_bytes(per), &bps) != cudaSuccess ||
-            grid > (uint32_t)(c->sms * bps))
-          return MGCD_ERR_GRID;
-      }
-      g.per_cta = per;
-      g.sync = c->d_gsync.as<GridSync>();
-      CK(launch_gridsync_init(g.sync, c->wait_timeout_ns, c->withhold_cta, c->stream));
-      ++c->launches;
-      cudaError_t e = launch_grid(g, threads, (int)grid, grid_smem_bytes(per), c->stream);
-      if (e == cudaErrorCooperativeLaunchTooLarge) return MGCD_ERR_GRID;
-      if (e != cudaSuccess) return MGCD_ERR_CUDA;
-      ++c->launches;
-    }
-  }
-  return MGCD_OK;
-}
-
-static int run_plan(mgcd_context* c)
-{
   if (!c) return MGCD_ERR_INVALID_ARG;
-  CK(cudaSetDevice(c->device));
-  c->launches = 0;
-  c->retried = 0;
-  const size_t ng = c->descs.size();
-  if (ng == 0) {
-    c->ran = true;
-    return MGCD_OK;
-  }
-  if (c->use_graph && !c->plain) {
-    if (!c->graph) {
-      // Record the run once (status reset, queue reset, every bucket kernel on its stream,
-      // joined back into c->stream); each later run is a single graph launch.
-      CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-      int rc = MGCD_OK;
-      if (cudaMemsetAsync(c->d_status.p, 0xFF, ng * sizeof(int32_t), c->stream) != cudaSuccess) rc = MGCD_ERR_CUDA;
-      if (rc == MGCD_OK)
-        rc = launch_set(c, c->buckets, c->grid_pairs, c->descs, c->d_pairs.as<PairDesc>(), c->d_queue.as<uint32_t>(),
-                        false);
-      cudaGraph_t g = nullptr;
-      const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
-      if (rc == MGCD_OK && e != cudaSuccess) rc = MGCD_ERR_CUDA;
-      if (rc == MGCD_OK && cudaGraphInstantiate(&c->graph, g, 0) != cudaSuccess) {
-        c->graph = nullptr;
-        rc = MGCD_ERR_CUDA;
-      }
-      if (g) cudaGraphDestroy(g);
-      if (rc != MGCD_OK) return rc;
-      c->graph_kernels = c->launches;
-    }
-    CK(cudaEventRecord(c->t_run0, c->stream));
-    CK(cudaGraphLaunch(c->graph, c->stream));
-    c->launches = c->graph_kernels;
-    c->bucket_timed = false;
-  } else {
-    CK(cudaEventRecord(c->t_run0, c->stream));
-    CK(cudaMemsetAsync(c->d_status.p, 0xFF, ng * sizeof(int32_t), c->stream));
-    int rc = launch_set(c, c->buckets, c->grid_pairs, c->descs, c->d_pairs.as<PairDesc>(), c->d_queue.as<uint32_t>(),
-                        true);
-    if (rc != MGCD_OK) return rc;
-    c->bucket_timed = true;
-  }
-  CK(cudaEventRecord(c->t_run1, c->stream));
-  c->ran = true;
-  c->synced = false;
-  return MGCD_OK;
-}
-
-// Waits for the run; pairs that ran with fewer moduli than the reference count and could
-// not be certified are rerun once with the reference count (same digit slots).
-static int sync_plan(mgcd_context* c)
-{
-  if (!c || !c->ran) return MGCD_ERR_INVALID_ARG;
-  CK(cudaSetDevice(c->device));
-  CK(cudaStreamSynchronize(c->stream));
-  if (c->synced) return MGCD_OK;
-  c->synced = true;
-  const size_t ng = c->descs.size();
-  bool scaled = false;
-  for (size_t k = 0; k < ng && !scaled; ++k) scaled = c->descs[k].nq < c->ref_nq[k];
-  if (!scaled) return MGCD_OK;
-  CK(c->h_status.grow(ng * sizeof(int32_t)));
-  CK(cudaMemcpy(c->h_status.p, c->d_status.p, ng * sizeof(int32_t), cudaMemcpyDeviceToHost));
-  const int32_t* st = c->h_status.as<int32_t>();
-  std::vector<uint32_t> redo;
-  for (uint32_t k = 0; k < ng; ++k)
-    if (st[k] != ST_OK && st[k] != ST_TIMEOUT && c->descs[k].nq < c->ref_nq[k]) redo.push_back(k);
-  if (redo.empty()) return MGCD_OK;
-  std::vector<PairDesc> rd = c->descs;
-  for (uint32_t k : redo) rd[k].nq = c->ref_nq[k];
-  const size_t main_order = c->order.size();
-  std::vector<Bucket> bks;
-  std::vector<uint32_t> gp;
-  size_t scratch = 0;
-  const size_t keep_grid_off = c->grid_scratch_off;
-  int rc = schedule(c, rd, redo, false, bks, gp, scratch);
-  if (rc != MGCD_OK) return rc;
-  // device buffers: retry descriptors after the main ones, retry order after the main order
-  CK(c->d_retry.grow(ng * sizeof(PairDesc)));
-  if (c->order.size() * sizeof(uint32_t) > c->d_order.bytes) {
-    // keep the main order: grow by copying
-    DevBuf nb;
-    CK(nb.grow(c->order.size() * sizeof(uint32_t)));
-    CK(cudaMemcpy(nb.p, c->d_order.p, main_order * sizeof(uint32_t), cudaMemcpyDeviceToDevice));
-    drop_graph(c);
-    c->d_order.release();
-    c->d_order = nb;
-  }
-  if (scratch > c->d_scratch.bytes / sizeof(uint32_t)) {
-    drop_graph(c);
-    c->d_scratch.release();
-    CK(c->d_scratch.grow(scratch * sizeof(uint32_t)));
-  }
-  CK(cudaMemcpyAsync(c->d_retry.p, rd.data(), ng * sizeof(PairDesc), cudaMemcpyHostToDevice, c->stream));
-  CK(cudaMemcpyAsync(c->d_order.as<uint32_t>() + main_order, c->order.data() + main_order,
-                     (c->order.size() - main_order) * sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream));
-  rc = launch_set(c, bks, gp, rd, c->d_retry.as<PairDesc>(), c->d_queue.as<uint32_t>() + NSTREAMS, false);
-  c->order.resize(main_order);               // the plan itself is unchanged for later runs
-  c->grid_scratch_off = keep_grid_off;
-  if (rc != MGCD_OK) return rc;
-  CK(cudaEventRecord(c->t_run1, c->stream));
-  CK(cudaStreamSynchronize(c->stream));
-  c->retried = (int)redo.size();
+  const Plan& P = c->main;
+  if (!P.ran || !P.bucket_timed || i < 0 || i >= (int)P.buckets.size()) return MGCD_ERR_INVALID_ARG;
+  float t = 0.f;
+  CK(cudaEventElapsedTime(&t, P.t_b0[i], P.t_b1[i]));
+  if (cls) *cls = P.buckets[i].cls;
+  if (pairs) *pairs = (int)P.buckets[i].n;
+  if (ms) *ms = t;
   return MGCD_OK;
 }
 
 int mgcd_batch_elapsed_ms(const mgcd_context* c, float* run_ms, float* dominant_ms, int* dominant_threads)
 {
-  if (!c || !c->ran) return MGCD_ERR_INVALID_ARG;
+  if (!c) return MGCD_ERR_INVALID_ARG;
+  const Plan& P = c->main;
+  if (!P.ran) return MGCD_ERR_INVALID_ARG;
   float r = 0.f, best = 0.f;
   int bt = 0;
-  if (!c->descs.empty()) {
-    CK(cudaEventElapsedTime(&r, c->t_run0, c->t_run1));
-    for (size_t b = 0; b < c->buckets.size(); ++b) {
-      float t = 0.f;
-      CK(cudaEventElapsedTime(&t, c->t_b0[b], c->t_b1[b]));
-      if (t > best) { best = t; bt = c->buckets[b].threads; }
-    }
+  if (!P.descs.empty()) {
+    CK(cudaEventElapsedTime(&r, P.t_run0, P.t_run1));
+    if (P.bucket_timed)
+      for (size_t b = 0; b < P.buckets.size(); ++b) {
+        float t = 0.f;
+        CK(cudaEventElapsedTime(&t, P.t_b0[b], P.t_b1[b]));
+        if (t > best) { best = t; bt = P.buckets[b].threads; }
+      }
   }
   if (run_ms) *run_ms = r;
   if (dominant_ms) *dominant_ms = best;
@@ -831,17 +999,19 @@ int mgcd_batch_elapsed_ms(const mgcd_context* c, float* run_ms, float* dominant_
 int mgcd_batch_transfer_bytes(const mgcd_context* c, uint64_t* h2d, uint64_t* d2h)
 {
   if (!c) return MGCD_ERR_INVALID_ARG;
-  if (h2d) *h2d = c->h2d_bytes;
-  if (d2h) *d2h = c->d2h_bytes;
+  if (h2d) *h2d = c->main.h2d_bytes;
+  if (d2h) *d2h = c->main.d2h_bytes;
   return MGCD_OK;
 }
 
 int mgcd_int_peak(mgcd_context* c, double* ops)
 {
   if (!c || !ops) return MGCD_ERR_INVALID_ARG;
+  if (busy(c)) return MGCD_ERR_BUSY;
   CK(cudaSetDevice(c->device));
-  uint32_t* sink = nullptr;
-  CK(cudaMalloc(&sink, sizeof(uint32_t)));
+  cudaStream_t s = c->main.stream;
+  DevBuf sink;
+  CK(sink.grow(sizeof(uint32_t), c->pool, s));
   const int blocks = c->sms * 8, iters = 1 << 16;
   cudaEvent_t a, b;
   cudaEventCreate(&a);
@@ -849,9 +1019,9 @@ int mgcd_int_peak(mgcd_context* c, double* ops)
   float best = 1e30f;
   int rc = MGCD_OK;
   for (int rep = 0; rep < 4 && rc == MGCD_OK; ++rep) {
-    cudaEventRecord(a, c->stream);
-    if (launch_int_peak(sink, blocks, iters, c->stream) != cudaSuccess) rc = MGCD_ERR_CUDA;
-    cudaEventRecord(b, c->stream);
+    cudaEventRecord(a, s);
+    if (launch_int_peak(sink.as<uint32_t>(), blocks, iters, s) != cudaSuccess) rc = MGCD_ERR_CUDA;
+    cudaEventRecord(b, s);
     if (cudaEventSynchronize(b) != cudaSuccess) rc = MGCD_ERR_CUDA;
     float ms = 0.f;
     cudaEventElapsedTime(&ms, a, b);
@@ -859,136 +1029,72 @@ int mgcd_int_peak(mgcd_context* c, double* ops)
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
-  cudaFree(sink);
+  sink.release(s);
   if (rc != MGCD_OK) return rc;
   *ops = (double)blocks * 256.0 * iters * 8.0 / (best * 1e-3);
   return MGCD_OK;
 }
 
-int mgcd_batch_run(mgcd_context* c) { return run_plan(c); }
+int mgcd_batch_run(mgcd_context* c)
+{
+  if (!c) return MGCD_ERR_INVALID_ARG;
+  if (busy(c)) return MGCD_ERR_BUSY;
+  return run_plan(c, c->main);
+}
 
-int mgcd_batch_sync(mgcd_context* c) { return sync_plan(c); }
+int mgcd_batch_sync(mgcd_context* c)
+{
+  if (!c) return MGCD_ERR_INVALID_ARG;
+  return sync_plan(c, c->main);
+}
 
 int mgcd_batch_retried(const mgcd_context* c, int* pairs)
 {
   if (!c || !pairs) return MGCD_ERR_INVALID_ARG;
-  *pairs = c->retried;
+  *pairs = c->main.retried;
   return MGCD_OK;
 }
 
 int mgcd_batch_launches(const mgcd_context* c, int* launches)
 {
   if (!c || !launches) return MGCD_ERR_INVALID_ARG;
-  *launches = c->launches;
-  return MGCD_OK;
-}
-
-// Copies the GPU results of the plan to pinned host memory.
-static int fetch(mgcd_context* c)
-{
-  const size_t ng = c->descs.size();
-  CK(cudaSetDevice(c->device));
-  if (ng == 0) return MGCD_OK;
-  CK(c->h_count.grow(ng * sizeof(uint32_t)));
-  CK(c->h_iters.grow(ng * sizeof(uint32_t)));
-  CK(c->h_status.grow(ng * sizeof(int32_t)));
-  CK(c->h_digits.grow(std::max<size_t>(c->ndig, 1) * sizeof(mgcd_pair)));
-  CK(cudaMemcpyAsync(c->h_count.p, c->d_count.p, ng * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
-  CK(cudaMemcpyAsync(c->h_iters.p, c->d_iters.p, ng * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
-  CK(cudaMemcpyAsync(c->h_status.p, c->d_status.p, ng * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
-  CK(cudaMemcpyAsync(c->h_digits.p, c->d_digits.p, c->ndig * sizeof(mgcd_pair), cudaMemcpyDeviceToHost, c->stream));
-  CK(cudaStreamSynchronize(c->stream));
-  c->d2h_bytes = ng * (2 * sizeof(uint32_t) + sizeof(int32_t)) + c->ndig * sizeof(mgcd_pair);
-  // work by the cost model
-  const uint32_t* it = c->h_iters.as<uint32_t>();
-  const uint32_t* cnt = c->h_count.as<uint32_t>();
-  const int32_t* st = c->h_status.as<int32_t>();
-  double R = 0, E = 0, M = 0, B = 0;
-  for (size_t k = 0; k < ng; ++k) {
-    const PairDesc& d = c->descs[k];
-    R += (double)d.nq * (d.u_len + d.v_len);
-    B += 4.0 * (d.u_len + d.v_len);
-    if (st[k] != ST_OK) continue;
-    const double I = it[k], K = cnt[k], N = c->eff_nq[k];
-    E += I * N - I * (I + 1) / 2;
-    M += K * (N - I) - K * (K + 1) / 2;
-  }
-  c->work[0] = R; c->work[1] = E; c->work[2] = M; c->work[3] = B;
+  *launches = c->main.launches;
   return MGCD_OK;
 }
 
 int mgcd_batch_work(const mgcd_context* c, double* r, double* e, double* m, double* b)
 {
   if (!c) return MGCD_ERR_INVALID_ARG;
-  if (r) *r = c->work[0];
-  if (e) *e = c->work[1];
-  if (m) *m = c->work[2];
-  if (b) *b = c->work[3];
+  const double* w = c->main.work;
+  if (r) *r = w[0];
+  if (e) *e = w[1];
+  if (m) *m = w[2];
+  if (b) *b = w[3];
   return MGCD_OK;
-}
-
-static int convert_all(mgcd_context* c, uint32_t* g, const uint64_t* g_off, const uint32_t* g_cap,
-                       uint32_t* g_len, int32_t* status)
-{
-  const size_t np = c->np;
-  const mgcd_pair* dig = c->h_digits.as<mgcd_pair>();
-  const uint32_t* cnt = c->h_count.as<uint32_t>();
-  const int32_t* st = c->h_status.as<int32_t>();
-  std::atomic<size_t> next{0};
-  auto work = [&]() {
-    for (;;) {
-      const size_t i = next.fetch_add(1);
-      if (i >= np) break;
-      int s = c->status[i];
-      size_t len = 0;
-      if (c->slot[i] >= 0) {
-        const int k = c->slot[i];
-        s = to_status(st[k]);
-        if (s == MGCD_OK && mixed_radix_to_limbs(dig + c->descs[k].out_off, cnt[k], g + g_off[i], g_cap[i], &len))
-          s = MGCD_ERR_CAPACITY;
-      } else if (s == MGCD_OK) {
-        len = c->trivial[i].size();
-        if (len > g_cap[i]) { s = MGCD_ERR_CAPACITY; len = 0; }
-        else if (len) std::memcpy(g + g_off[i], c->trivial[i].data(), len * sizeof(uint32_t));
-      }
-      g_len[i] = (uint32_t)len;
-      if (status) status[i] = s;
-    }
-  };
-  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-  const size_t nt = std::min<size_t>(hw, (np + 15) / 16);
-  if (nt <= 1) {
-    work();
-  } else {
-    std::vector<std::thread> th;
-    for (size_t t = 0; t < nt; ++t) th.emplace_back(work);
-    for (auto& t : th) t.join();
-  }
-  int rc = MGCD_OK;
-  for (size_t i = 0; i < np && rc == MGCD_OK; ++i) {
-    if (status) { if (status[i] != MGCD_OK) rc = status[i]; }
-  }
-  return rc;
 }
 
 int mgcd_batch_download(mgcd_context* c, uint32_t* g, const uint64_t* g_off, const uint32_t* g_cap,
                         uint32_t* g_len, int32_t* status)
 {
-  if (!c || !c->ran || (c->np && (!g || !g_off || !g_cap || !g_len || !status))) return MGCD_ERR_INVALID_ARG;
-  int rc = sync_plan(c);
+  if (!c) return MGCD_ERR_INVALID_ARG;
+  Plan& P = c->main;
+  if (!P.ran || (P.np && (!g || !g_off || !g_cap || !g_len || !status))) return MGCD_ERR_INVALID_ARG;
+  int rc = sync_plan(c, P);
   if (rc != MGCD_OK) return rc;
-  rc = fetch(c);
+  rc = fetch(c, P);
   if (rc != MGCD_OK) return rc;
-  return convert_all(c, g, g_off, g_cap, g_len, status);
+  return convert_all(c, P, g, g_off, g_cap, g_len, status, true);
 }
 
 int mgcd_gcd_batch(mgcd_context* c, size_t np, const uint32_t* limbs, const uint64_t* u_off,
                    const uint32_t* u_len, const uint64_t* v_off, const uint32_t* v_len, uint32_t* g,
                    const uint64_t* g_off, const uint32_t* g_cap, uint32_t* g_len, int32_t* status)
 {
-  int rc = plan_batch(c, np, limbs, u_off, u_len, v_off, v_len, false);
+  if (!c) return MGCD_ERR_INVALID_ARG;
+  if (busy(c)) return MGCD_ERR_BUSY;
+  int rc = plan_batch(c, c->main, np, limbs, u_off, u_len, v_off, v_len, false);
   if (rc != MGCD_OK) return rc;
-  rc = run_plan(c);
+  rc = run_plan(c, c->main);
   if (rc != MGCD_OK) return rc;
   return mgcd_batch_download(c, g, g_off, g_cap, g_len, status);
 }
@@ -998,6 +1104,7 @@ int mgcd_gcd_batch(mgcd_context* c, size_t np, const uint32_t* limbs, const uint
 static int single(mgcd_context* c, const uint32_t* u, size_t uSz, const uint32_t* v, size_t vSz)
 {
   if (!c || (uSz && !u) || (vSz && !v)) return MGCD_ERR_INVALID_ARG;
+  if (busy(c)) return MGCD_ERR_BUSY;
   // Pack both operands contiguously (the plan reads one limb array).
   static thread_local std::vector<uint32_t> buf;
   buf.resize(uSz + vSz);
@@ -1005,13 +1112,14 @@ static int single(mgcd_context* c, const uint32_t* u, size_t uSz, const uint32_t
   if (vSz) std::memcpy(buf.data() + uSz, v, vSz * sizeof(uint32_t));
   const uint64_t uo = 0, vo = uSz;
   const uint32_t ul = (uint32_t)uSz, vl = (uint32_t)vSz;
-  int rc = plan_batch(c, 1, buf.data(), &uo, &ul, &vo, &vl, true);
+  Plan& P = c->main;
+  int rc = plan_batch(c, P, 1, buf.data(), &uo, &ul, &vo, &vl, true);
   if (rc != MGCD_OK) return rc;
-  rc = run_plan(c);
+  rc = run_plan(c, P);
   if (rc != MGCD_OK) return rc;
-  rc = sync_plan(c);
+  rc = sync_plan(c, P);
   if (rc != MGCD_OK) return rc;
-  return fetch(c);
+  return fetch(c, P);
 }
 
 int mgcd_gcd_digits(mgcd_context* c, const uint32_t* u, size_t uSz, const uint32_t* v, size_t vSz,
@@ -1022,12 +1130,13 @@ int mgcd_gcd_digits(mgcd_context* c, const uint32_t* u, size_t uSz, const uint32
   if (strip(u, uSz) == 0 || strip(v, vSz) == 0) return MGCD_ERR_INVALID_ARG;
   int rc = single(c, u, uSz, v, vSz);
   if (rc != MGCD_OK) return rc;
-  if (c->slot[0] < 0) return c->status[0];
-  const int32_t st = c->h_status.as<int32_t>()[0];
+  const Plan& P = c->main;
+  if (P.slot[0] < 0) return P.status[0];
+  const int32_t st = P.h_status.as<int32_t>()[0];
   if (st != ST_OK) return to_status(st);
-  const uint32_t n = c->h_count.as<uint32_t>()[0];
+  const uint32_t n = P.h_count.as<uint32_t>()[0];
   if (n > cap) return MGCD_ERR_CAPACITY;
-  std::memcpy(digits, c->h_digits.as<mgcd_pair>() + c->descs[0].out_off, n * sizeof(mgcd_pair));
+  std::memcpy(digits, P.h_digits.as<mgcd_pair>() + P.descs[0].out_off, n * sizeof(mgcd_pair));
   *count = n;
   return MGCD_OK;
 }
@@ -1043,7 +1152,7 @@ int mgcd_gcd(mgcd_context* c, const uint32_t* u, size_t uSz, const uint32_t* v, 
   const uint32_t cap = (uint32_t)std::min<size_t>(g_cap, 0xFFFFFFFFu);
   uint32_t len = 0;
   int32_t st = 0;
-  rc = convert_all(c, g, &off, &cap, &len, &st);
+  rc = convert_all(c, c->main, g, &off, &cap, &len, &st, false);
   *g_len = len;
   return rc;
 }

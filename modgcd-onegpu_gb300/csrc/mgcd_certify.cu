@@ -1,0 +1,127 @@
+// mgcd_certify.cu -- exhaustive certification of the float quotient steps of inv_mod on
+// the device it runs on (the reference certifies its quoRem<QUASI> the same way, per
+// device, certifyQuoRemQuasi.cu:25-48).
+//
+// Each Euclid step of inv_mod estimates Q = floor(r0 / r1) from a float reciprocal and
+// corrects it with one exact integer step, which is right iff the estimate is Q or Q - 1:
+//   phase A (2^22 <= r1 < r0 < 2^32): est = fma_rz(ru(r0), rcp(ru(r1)), -2^-9), Q = rz(est);
+//   phase C (2 <= r1 < r0 < 2^22):    qf = fma_rz(r0, rcp(r1), 2^23 - 1/2) - 2^23,
+//                                      rem = fma_rn(-qf, r1, r0), one correction.
+// For a fixed r1 both estimates are non-decreasing in r0 (every operation is monotone and
+// rcp(r1) is fixed), while the true quotient is constant (= k) on [k r1, (k+1) r1 - 1].  So
+// the estimate lies in {k - 1, k} on the whole interval iff it does at the two ends:
+// checking both ends of every interval, for every r1, covers every (r0, r1) of the phase.
+// Phase A: ~6e10 end points; phase C: ~1.3e8 (where the whole step -- quotient, exact
+// remainder, correction -- is also checked at the end points).
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/modgcd.h"
+#include "mgcd_device.cuh"
+#include "mgcd_plan.h"
+
+namespace mgcd {
+
+namespace {
+
+struct CertOut {
+  unsigned long long checked;
+  unsigned long long failures;
+  uint32_t first_r0, first_r1;
+};
+
+__device__ __forceinline__ uint32_t est_a(uint32_t r0, uint32_t r1)
+{
+  const float est = __fmaf_rz(__uint2float_ru(r0), rcp_approx(__uint2float_ru(r1)), -0x1p-9f);
+  return __float2uint_rz(est);
+}
+
+// Phase C step as inv_mod runs it; returns false if it does not yield (Q, r0 mod r1).
+__device__ __forceinline__ bool step_c_ok(uint32_t r0, uint32_t r1, uint32_t k)
+{
+  const float f0 = (float)r0, f1 = (float)r1;
+  const float rc = rcp_approx(f1);
+  float qm = __fmaf_rz(f0, rc, 8388607.5f);
+  const float qf = qm - 8388608.0f;
+  if (qf < (float)(k - 1) || qf > (float)k) return false;     // estimate in {k - 1, k}
+  float rem = __fmaf_rn(-qf, f1, f0);
+  if (rem >= f1) { rem -= f1; qm += 1.0f; }
+  const uint32_t Q = __float_as_uint(qm) - 0x4B000000u;
+  return Q == k && rem == (float)(r0 - k * r1);
+}
+
+__device__ void fail(CertOut* o, uint32_t r0, uint32_t r1)
+{
+  if (atomicAdd(&o->failures, 1ull) == 0ull) {
+    o->first_r0 = r0;
+    o->first_r1 = r1;
+  }
+}
+
+__global__ void __launch_bounds__(256) certify_kernel(CertOut* out)
+{
+  const uint32_t stride = gridDim.x * blockDim.x;
+  unsigned long long n = 0;
+  // phase C: 2 <= r1 < r0 < 2^22
+  constexpr uint32_t C_TOP = (1u << 22) - 1u;
+  for (uint32_t r1 = 2u + blockIdx.x * blockDim.x + threadIdx.x; r1 < (1u << 22); r1 += stride) {
+    for (uint32_t k = 1; k <= C_TOP / r1; ++k) {
+      const uint32_t lo = k == 1 ? r1 + 1u : k * r1;
+      const uint32_t hi = min((k + 1) * r1 - 1u, C_TOP);
+      if (lo > hi) continue;
+      n += 2;
+      if (!step_c_ok(lo, r1, k)) fail(out, lo, r1);
+      if (!step_c_ok(hi, r1, k)) fail(out, hi, r1);
+    }
+  }
+  // phase A: 2^22 <= r1 < r0 < 2^32
+  constexpr uint64_t A_TOP = 0xFFFFFFFFull;
+  for (uint64_t r1w = (1ull << 22) + blockIdx.x * blockDim.x + threadIdx.x; r1w < A_TOP; r1w += stride) {
+    const uint32_t r1 = (uint32_t)r1w;
+    const uint32_t kmax = (uint32_t)(A_TOP / r1w);
+    for (uint32_t k = 1; k <= kmax; ++k) {
+      const uint64_t lo = k == 1 ? r1w + 1 : (uint64_t)k * r1w;
+      const uint64_t hi = min((uint64_t)(k + 1) * r1w - 1, A_TOP);
+      if (lo > hi) continue;
+      n += 2;
+      const uint32_t el = est_a((uint32_t)lo, r1), eh = est_a((uint32_t)hi, r1);
+      if (el + 1u < k || el > k) fail(out, (uint32_t)lo, r1);
+      if (eh + 1u < k || eh > k) fail(out, (uint32_t)hi, r1);
+    }
+  }
+  atomicAdd(&out->checked, n);
+}
+
+}  // namespace
+
+}  // namespace mgcd
+
+extern "C" int mgcd_certify_inverse(mgcd_context* c, uint64_t* checked, uint64_t* failures, uint32_t* first_r0,
+                                    uint32_t* first_r1)
+{
+  using namespace mgcd;
+  if (!c || !checked || !failures) return MGCD_ERR_INVALID_ARG;
+  if (c->serving) return MGCD_ERR_BUSY;
+  if (cudaSetDevice(c->device) != cudaSuccess) return MGCD_ERR_CUDA;
+  cudaStream_t s = c->main.stream;
+  DevBuf buf;
+  if (buf.grow(sizeof(CertOut), c->pool, s) != cudaSuccess) return MGCD_ERR_CUDA;
+  CertOut h = {};
+  int rc = MGCD_OK;
+  if (cudaMemsetAsync(buf.p, 0, sizeof(CertOut), s) != cudaSuccess) rc = MGCD_ERR_CUDA;
+  if (rc == MGCD_OK) {
+    certify_kernel<<<c->sms * 8, 256, 0, s>>>(buf.as<CertOut>());
+    if (cudaGetLastError() != cudaSuccess) rc = MGCD_ERR_CUDA;
+  }
+  if (rc == MGCD_OK && (cudaMemcpyAsync(&h, buf.p, sizeof(CertOut), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                        cudaStreamSynchronize(s) != cudaSuccess))
+    rc = MGCD_ERR_CUDA;
+  buf.release(s);
+  cudaStreamSynchronize(s);
+  if (rc != MGCD_OK) return rc;
+  *checked = h.checked;
+  *failures = h.failures;
+  if (first_r0) *first_r0 = h.first_r0;
+  if (first_r1) *first_r1 = h.first_r1;
+  return MGCD_OK;
+}

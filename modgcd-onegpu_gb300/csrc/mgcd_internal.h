@@ -17,7 +17,19 @@ struct PairDesc {
   uint32_t u_len, v_len;
   uint32_t nq;       // moduli used (multiple of 256)
   uint32_t out_off;  // first digit slot in the digit array; nq + 1 slots are reserved
+  uint64_t g_off;    // first limb of the binary gcd in the result-limb array
+  uint32_t g_cap;    // limbs reserved there (the smaller operand's length)
+  uint32_t pad_;
 };
+
+// Device-side mixed-radix conversion (mgcd_radix_dev.cu): pairs with up to RADIX_MAX
+// digits are converted on the GPU; glen = RADIX_HOST marks a pair left to the host
+// (more digits, or a failed pair).
+constexpr uint32_t RADIX_MAX = 4096;
+constexpr uint32_t RADIX_HOST = 0xFFFFFFFFu;
+size_t radix_smem_bytes();
+cudaError_t launch_radix(const PairDesc* pairs, uint32_t npairs, const mgcd_pair* digits, const uint32_t* count,
+                         const int32_t* status, uint32_t* glimbs, uint32_t* glen, int grid, cudaStream_t s);
 
 // Per-pair results written by the kernels.
 enum : int32_t {

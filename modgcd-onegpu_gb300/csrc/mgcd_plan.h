@@ -1,0 +1,138 @@
+// mgcd_plan.h -- host-side state of the library: the context (device, moduli table,
+// inverse table, launch configuration) and plans (one batch's buffers, streams and
+// schedule).  A context owns one plan for its own calls; the request server owns one plan
+// per in-flight wave, all sharing the context's resident tables.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "../../include/modgcd.h"
+#include "mgcd_internal.h"
+
+namespace mgcd {
+
+// Device buffer from the context's stream-ordered memory pool: growing it neither blocks
+// the host nor serialises the other streams (plain cudaMalloc/cudaFree would).
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaError_t grow(size_t want, cudaMemPool_t pool, cudaStream_t s);
+  void release(cudaStream_t s);
+  template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+// Pinned host buffer (grow-only, doubling).  A buffer it outgrows is kept until release():
+// cudaFreeHost waits for all work on the device, which would stall a server behind every
+// kernel in flight.
+struct HostBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  std::vector<void*> retired;
+  cudaError_t grow(size_t want);
+  void release();
+  template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+struct Bucket {
+  int threads, k;      // CTA size, pairs per CTA in lockstep
+  int csize;           // CTAs per thread-block cluster (0: one CTA per pair)
+  int cls;             // size class
+  uint32_t first, n, nq_max;
+  int grid;            // CTAs (csize = 0) or clusters
+  size_t smem;
+  size_t scratch_off;  // words
+};
+
+// Size classes of the batched path, one persistent kernel (and stream) each: pairs with at
+// most 1,024 / 4,096 / 16,384 moduli run one per CTA; larger pairs one per cluster.
+constexpr int NSTREAMS = MGCD_NUM_SIZE_CLASSES;
+constexpr int CLUSTER_CLASS = 3;
+constexpr uint32_t CTA_MAX_NQ = 16384;
+constexpr size_t INVTAB_N = 16384;        // moduli covered by the pairwise inverse table
+
+inline int size_class(uint32_t nq) { return nq <= 1024 ? 0 : nq <= 4096 ? 1 : nq <= CTA_MAX_NQ ? 2 : CLUSTER_CLASS; }
+
+struct Plan {
+  cudaStream_t stream = nullptr;
+  cudaStream_t bstream[NSTREAMS] = {};
+  cudaEvent_t ev_start = nullptr, ev_b[NSTREAMS] = {};
+  // timing: the whole run on `stream`, and each bucket launch on its stream
+  cudaEvent_t t_run0 = nullptr, t_run1 = nullptr, t_b0[NSTREAMS] = {}, t_b1[NSTREAMS] = {};
+
+  size_t np = 0;                       // pairs in the plan
+  std::vector<int32_t> status;         // per pair: MGCD_OK / error code / -1 = computed on the GPU
+  std::vector<int> slot;               // per pair: index into GPU arrays, or -1
+  std::vector<std::vector<uint32_t>> trivial;  // per pair: host-decided result (zero operand)
+  std::vector<PairDesc> descs;         // GPU pairs
+  std::vector<uint32_t> order;
+  std::vector<Bucket> buckets;
+  std::vector<uint32_t> grid_pairs;    // GPU indices run as single-pair launches
+  std::vector<uint32_t> ref_nq, eff_nq; // per GPU pair: reference count, count of the final run
+  size_t ndig = 0, scratch_words = 0, grid_scratch_off = 0;
+  size_t nglimbs = 0;                  // result limbs reserved (sum of g_cap)
+  bool plain = false;                  // single-pair latency policy
+  bool graphable = true;               // may be recorded into a CUDA graph (context setting)
+
+  DevBuf d_limbs, d_pairs, d_order, d_digits, d_count, d_iters, d_status, d_queue, d_scratch, d_gsync, d_retry;
+  DevBuf d_glimbs, d_glen;             // binary gcds converted on the device
+  HostBuf h_count, h_iters, h_status, h_digits, h_glimbs, h_glen;
+  int launches = 0, retried = 0;
+  bool ran = false, synced = false, bucket_timed = false;
+  double work[4] = {0, 0, 0, 0};
+  uint64_t h2d_bytes = 0, d2h_bytes = 0;
+
+  // CUDA graph of the plan's GPU work; dropped whenever a buffer it uses moves
+  cudaGraphExec_t graph = nullptr;
+  int graph_kernels = 0;
+
+  cudaError_t create();
+  void destroy(cudaMemPool_t pool);
+  void drop_graph();
+  size_t device_bytes() const;
+};
+
+}  // namespace mgcd
+
+struct mgcd_context {
+  int device = 0, L = 32, sms = 0;
+  size_t smem_optin = 0;               // largest dynamic shared memory per CTA
+  cudaMemPool_t pool = nullptr;
+  std::vector<uint32_t> moduli;
+  mgcd::DevBuf mods;
+  mgcd::DevBuf d_invtab;               // pairwise inverse table (InvTab)
+  uint32_t invtab_n = 0;
+  mgcd::Plan main;                     // the plan of the context's own calls
+  bool serving = false;                // a request server runs on this context
+
+  // Per size class of the batched path: CTA size, pairs per CTA in lockstep, fraction of
+  // the reference moduli count, CTAs per cluster (cluster class only).
+  struct ClassCfg { int threads, k; float nq_scale; int csize; };
+  ClassCfg cfg[mgcd::NSTREAMS] = {{256, 4, 1.0f, 0}, {512, 4, 1.0f, 0}, {1024, 2, 1.0f, 0}, {1024, 1, 1.0f, 8}};
+  bool use_graph = false;
+  int single_policy = MGCD_SINGLE_AUTO;  // launch shape of pairs that span several CTAs
+  unsigned long long wait_timeout_ns = 2000000000ull;   // bound of every cross-CTA wait
+  uint32_t withhold_cta = 0xFFFFFFFFu;                  // test hook (mgcd_test_withhold_cta)
+  uint32_t force_nq = 0;                                // test hook (mgcd_test_force_moduli)
+};
+
+namespace mgcd {
+
+// Plan operations (mgcd_capi.cpp).  All return MGCD_* codes.
+//   plan_batch   validate, order and size the pairs on the host, copy the batch to the
+//                device on P.stream (asynchronous when `limbs` is pinned);
+//   run_plan     launch the GPU work (asynchronous);
+//   sync_plan    wait; rerun uncertified pairs of a scaled run with the reference count;
+//   fetch        copy the digits back (pinned) and account the work;
+//   convert_all  digits -> binary gcds for every pair of the plan.
+int plan_batch(mgcd_context* c, Plan& P, size_t np, const uint32_t* limbs, const uint64_t* u_off,
+               const uint32_t* u_len, const uint64_t* v_off, const uint32_t* v_len, bool plain);
+int run_plan(mgcd_context* c, Plan& P);
+int sync_plan(mgcd_context* c, Plan& P);
+int fetch(mgcd_context* c, Plan& P);
+int convert_all(mgcd_context* c, Plan& P, uint32_t* g, const uint64_t* g_off, const uint32_t* g_cap,
+                uint32_t* g_len, int32_t* status, bool threaded);
+int to_status(int32_t st);
+
+}  // namespace mgcd

@@ -1,0 +1,121 @@
+#!/usr/bin/env python
+"""Autotuner of the batched path: picks, per size class, the launch configuration that
+gives the shortest device time for that class's pairs, and writes the tuning table that
+mgcd_load_tuning reads.
+
+Size classes (by the reference's moduli count of the pair): 0 = <= 1,024 moduli, 1 =
+<= 4,096, 2 = <= 16,384 (one CTA per pair), 3 = larger (one thread-block cluster per pair).
+Candidates: CTA size 256/512/1024, pairs per CTA in lockstep k = 1/2/4 (k = 4 needs
+<= 512 threads), fraction of the reference moduli count 1.0 ... 0.7 (results stay exact:
+uncertified pairs are rerun, and the rerun is part of the timed run); for class 3 the CTA
+size and the cluster size (4/8/16 CTAs).  The classes of a batch run concurrently and
+share the SMs, so classes 0-2 are tuned by coordinate descent on the whole mixed
+1k-64k-bit batch (largest class first, the others held at their current best); class 3 is
+timed alone on 300k-bit pairs.  Every time is the median of `reps` runs and every result
+is checked against Python's gcd.
+
+  python modgcd-onegpu_gb300/tune.py [--out PATH] [--log PATH] [--L 32]
+"""
+import argparse
+import importlib
+import json
+import math
+import os
+import statistics
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+
+mg = importlib.import_module("modgcd-onegpu_gb300")
+wl = importlib.import_module("modgcd-onegpu_gb300.workloads")
+
+SCALES = (1.0, 0.9, 0.8, 0.7)
+
+
+def class_of(u, v, L):
+    nq = mg.moduli_needed(max(u.bit_length(), v.bit_length()), L)
+    return 0 if nq <= 1024 else 1 if nq <= 4096 else 2 if nq <= 16384 else 3
+
+
+def time_config(dev, packed, exp, reps):
+    dev.batch_upload(*packed)
+    ms = []
+    for _ in range(reps + 1):
+        dev.batch_run()
+        dev.batch_sync()
+        ms.append(dev.batch_elapsed_ms()[0])
+    g, go, gn, st = dev.batch_download()
+    got = [mg.from_limbs(g[int(o): int(o) + int(n)]) for o, n in zip(go, gn)]
+    if not (st == 0).all() or got != exp:
+        raise RuntimeError("tuning run gave a wrong or failed result")
+    return statistics.median(ms[1:])
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--L", type=int, default=32)
+    ap.add_argument("--pairs", type=int, default=4096)
+    ap.add_argument("--seed", type=int, default=3)
+    ap.add_argument("--big-pairs", type=int, default=24)
+    ap.add_argument("--big-bits", type=int, default=300000)
+    ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--out", default=None)
+    ap.add_argument("--log", default=None)
+    args = ap.parse_args()
+
+    us, vs, _ = wl.mixed_batch(args.pairs, seed=args.seed)
+    by = {c: ([], []) for c in range(4)}
+    for u, v in zip(us, vs):
+        c = class_of(u, v, args.L)
+        by[c][0].append(u)
+        by[c][1].append(v)
+    bu, bv, _ = wl.serve_requests(args.big_pairs, 1.0, seed=args.seed + 1, big_frac=1.0, big_bits=args.big_bits)
+    by[3] = (bu, bv)
+
+    dev = mg.Device(0, args.L)
+    log = []
+    best = {}
+    full = mg.pack_pairs(us, vs)
+    full_exp = [math.gcd(u, v) for u, v in zip(us, vs)]
+    for c in (2, 1, 0, 3):
+        cu, cv = by[c]
+        if not cu:
+            continue
+        if c < 3:   # whole batch, other classes at their current setting
+            packed, exp = full, full_exp
+            cands = [(t, k, s, 0) for t in (256, 512, 1024) for k in (1, 2, 4) if not (k == 4 and t > 512)
+                     for s in SCALES]
+        else:
+            packed, exp = mg.pack_pairs(cu, cv), [math.gcd(u, v) for u, v in zip(cu, cv)]
+            cands = [(t, 1, 1.0, cs) for t in (512, 1024) for cs in (4, 8, 16)]
+        for t, k, s, cs in cands:
+            dev.set_size_class(c, t, k, s)
+            if cs:
+                dev.set_cluster_size(cs)
+            try:
+                ms = time_config(dev, packed, exp, args.reps)
+            except mg.GcdError as e:       # e.g. a launch shape that does not fit
+                log.append({"class": c, "threads": t, "k": k, "nq_scale": s, "cluster": cs, "error": str(e)})
+                continue
+            log.append({"class": c, "pairs": len(cu), "timed_pairs": len(exp), "threads": t, "k": k,
+                        "nq_scale": s, "cluster": cs, "ms": ms})
+            print(json.dumps(log[-1]), flush=True)
+            if c not in best or ms < best[c][0]:
+                best[c] = (ms, t, k, s, cs)
+        _, t, k, s, cs = best[c]
+        dev.set_size_class(c, t, k, s)
+        if cs:
+            dev.set_cluster_size(cs)
+    out = args.out or os.path.join(HERE, "tuning", "gb300_L%d.txt" % args.L)
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    dev.save_tuning(out)
+    if args.log:
+        with open(args.log, "w") as f:
+            json.dump({"best": {str(c): b for c, b in best.items()}, "runs": log}, f, indent=1)
+    print(open(out).read())
+    dev.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -66,6 +66,31 @@ def mixed_batch(n=4096, seed=3, lo_bits=1024, hi_bits=65536):
     return us, vs, kinds
 
 
+def serve_requests(n, rate, seed=5, big_frac=0.01, big_bits=1 << 20, lo_bits=1024, hi_bits=65536):
+    """Open-loop serving load: n requests with Poisson arrivals at `rate` per second
+    (exponential gaps, seeded), sizes from the mixed-batch distribution plus a `big_frac`
+    share of big_bits-bit requests (planted gcd of U[0, 50%]).  Returns (us, vs, arrival_s).
+    The big requests sit at evenly spread positions so every prefix has its share."""
+    rng = random.Random(seed)
+    us, vs, arr = [], [], []
+    t = 0.0
+    n_big = int(round(n * big_frac))
+    big_at = {int((k + 0.5) * n / n_big) for k in range(n_big)} if n_big else set()
+    for i in range(n):
+        t += rng.expovariate(rate)
+        arr.append(t)
+        if i in big_at:
+            gb = int(rng.uniform(0.0, 0.5) * big_bits)
+            g = _rand_bits(rng, gb) if gb > 0 else 1
+            us.append(g * _rand_bits(rng, big_bits - gb))
+            vs.append(g * _rand_bits(rng, big_bits - gb))
+        else:
+            u, v, _ = mixed_pair(rng, lo_bits, hi_bits)
+            us.append(u)
+            vs.append(v)
+    return us, vs, arr
+
+
 def skewed_batch(n_big=64, big_bits=1 << 20, n_small=16384, seed=4):
     rng = random.Random(seed)
     us, vs = [], []

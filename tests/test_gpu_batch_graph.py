@@ -2,6 +2,7 @@
 pair, pulled from a persistent queue) and batches replayed from a recorded CUDA graph.
 Every result is compared with Python's exact gcd; graph replays must equal direct runs."""
 import math
+import os
 import random
 
 import numpy as np
@@ -111,3 +112,33 @@ def test_graph_replay_with_fewer_moduli_and_retries(mgcd):
             dev.batch_run()
             dev.batch_sync()
             assert _results(mgcd, dev) == exp
+
+
+def test_tuning_table_roundtrip_and_bad_tables(mgcd, tmp_path):
+    with mgcd.Device(0, 32) as dev:
+        dev.set_size_class(1, 256, 2, 0.9)
+        dev.set_cluster_size(4)
+        path = tmp_path / "table.txt"
+        dev.save_tuning(str(path))
+        dev.set_size_class(1, 512, 4, 1.0)
+        dev.set_cluster_size(8)
+        dev.load_tuning(str(path))
+        t, k, s = dev.get_size_class(1)
+        assert (t, k) == (256, 2) and abs(s - 0.9) < 1e-6
+        assert dev.get_cluster_size() == 4
+        before = [dev.get_size_class(c) for c in range(4)]
+        for bad in ("1 256 2 0.9 0\n2 1024 4 1.0 0\n",      # k = 4 needs <= 512 threads
+                    "3 1024 1 1.0 0\n",                       # class 3 needs a cluster size
+                    "0 256 4 0.4 0\n",                        # scale below 0.5
+                    "0 256 4\n"):                             # short line
+            p = tmp_path / "bad.txt"
+            p.write_text(bad)
+            with pytest.raises(mgcd.GcdError):
+                dev.load_tuning(str(p))
+            assert [dev.get_size_class(c) for c in range(4)] == before   # nothing applied
+        default = mgcd.default_tuning_path(dev)
+        if os.path.exists(default):
+            dev.load_tuning(default)
+            rng = random.Random(46)
+            us, vs = _skewed(rng, 1, 200000, 300)
+            assert dev.gcd_batch(us, vs) == [math.gcd(u, v) for u, v in zip(us, vs)]

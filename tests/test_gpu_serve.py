@@ -1,0 +1,87 @@
+"""The request server (continuous batching under an HBM admission budget).
+
+- Each result is the same alone (one request on an idle server) and in the mix (the same
+  request among a Poisson stream of others of mixed sizes), and equals Python's gcd.
+- The admission budget is never exceeded and an oversize request is refused.
+- While a server runs, the context's own calls are refused; afterwards they work again.
+"""
+import importlib
+import math
+import random
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+wl = importlib.import_module("modgcd-onegpu_gb300.workloads")
+
+
+def _cap(u, v):
+    return max(u.bit_length(), v.bit_length()) // 32 + 2
+
+
+def test_same_alone_and_in_the_mix(mgcd):
+    us, vs, arr = wl.serve_requests(400, 20000.0, seed=7, big_frac=0.01, big_bits=150000, hi_bits=16384)
+    us += [0, 12345, 7 * 2**5000]          # zero operands and a tiny pair ride along
+    vs += [99, 0, 7 * 3**3000]
+    arr += [arr[-1] + 1e-4] * 3
+    exp = [math.gcd(u, v) for u, v in zip(us, vs)]
+    with mgcd.Device(0, 32) as dev:
+        with mgcd.Server(dev) as srv:
+            alone = [srv.gcd(u, v) for u, v in zip(us, vs)]
+            mix, st, lat, makespan = srv.replay(us, vs, arr)
+            stats = srv.stats()
+        assert alone == exp
+        assert mix == exp
+        assert (st == 0).all()
+        assert (lat > 0).all() and makespan >= max(arr)
+        assert stats["completed"] == 2 * len(us)
+        # in the mix, requests share waves: far fewer waves than requests
+        assert stats["waves"] < 2 * len(us)
+
+
+def test_admission_budget(mgcd):
+    rng = random.Random(8)
+    budget = 600_000
+    with mgcd.Device(0, 32) as dev:
+        with mgcd.Server(dev, budget_bytes=budget) as srv:
+            big = rng.getrandbits(400000) | 1
+            with pytest.raises(mgcd.GcdError) as e:
+                srv.submit(big, big + 2)
+            assert mgcd.STATUS_NAMES[e.value.status] == "MGCD_ERR_BUDGET"
+            us = [rng.getrandbits(rng.randint(1000, 20000)) | 1 for _ in range(300)]
+            vs = [rng.getrandbits(rng.randint(1000, 20000)) | 1 for _ in range(300)]
+            tickets = [srv.submit(u, v) for u, v in zip(us, vs)]
+            got = [srv.take(t, _cap(u, v))[0] for t, u, v in zip(tickets, us, vs)]
+            stats = srv.stats()
+        assert got == [math.gcd(u, v) for u, v in zip(us, vs)]
+        assert 0 < stats["peak_admitted_bytes"] <= budget
+        assert stats["waves"] > 1
+
+
+def test_take_timeout_keeps_the_ticket(mgcd):
+    rng = random.Random(9)
+    g = rng.getrandbits(60000) | 1
+    u, v = g * (rng.getrandbits(200000) | 1), g * (rng.getrandbits(200000) | 1)
+    with mgcd.Device(0, 32) as dev:
+        with mgcd.Server(dev) as srv:
+            t = srv.submit(u, v)
+            with pytest.raises(mgcd.GcdError) as e:
+                srv.take(t, _cap(u, v), timeout_ms=1)
+            assert mgcd.STATUS_NAMES[e.value.status] == "MGCD_ERR_TIMEOUT"
+            assert srv.take(t, _cap(u, v))[0] == math.gcd(u, v)
+            with pytest.raises(mgcd.GcdError):      # released
+                srv.poll(t)
+
+
+def test_context_refuses_direct_calls_while_serving(mgcd):
+    with mgcd.Device(0, 32) as dev:
+        srv = mgcd.Server(dev)
+        with pytest.raises(mgcd.GcdError) as e:
+            dev.gcd(6, 4)
+        assert mgcd.STATUS_NAMES[e.value.status] == "MGCD_ERR_BUSY"
+        with pytest.raises(mgcd.GcdError):
+            mgcd.Server(dev)
+        srv.close()
+        assert dev.gcd(6, 4) == 2

@@ -30,6 +30,9 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# Many streams run at once (size classes, server waves): give them separate hardware
+# queues.  Read when the CUDA context is created, so set before torch touches the GPU.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 TRAFFIC_FILE = os.path.join(ROOT, "profiles", "ncu_traffic.json")
@@ -167,13 +170,24 @@ def serve_leg(mg, wl, po, dev, rates, n_req, nthreads, seed=5):
     rows = []
     with mg.Server(dev, budget_bytes=8 << 30) as srv:
         for rate in rates:
+            n_tr = len(srv.trace())
             g, go, gn, st, lat, mk = srv.replay_packed(*packed, np.asarray(arr1) / rate)
+            tr = srv.trace()[n_tr:]
             ok = bool((st == 0).all()) and results_equal(mg, g, go, gn, gx, gxo, gxn)
             ms = lat * 1e3
+            waves = {}
+            for lane in range(4):
+                t = tr[tr["lane"] == lane]
+                if len(t):
+                    waves[str(lane)] = {"waves": int(len(t)), "requests": int(t["requests"].sum()),
+                                        "launch_ms_max": float(1e3 * (t["t_launched"] - t["t_admit"]).max()),
+                                        "gpu_ms_p50": float(1e3 * np.median(t["t_gpu_done"] - t["t_launched"])),
+                                        "gpu_ms_max": float(1e3 * (t["t_gpu_done"] - t["t_launched"]).max()),
+                                        "answer_ms_max": float(1e3 * (t["t_answered"] - t["t_gpu_done"]).max())}
             row = {"rate_req_s": rate, "requests": n_req, "gcds_per_s": n_req / mk, "makespan_s": mk,
                    "p50_ms": float(np.percentile(ms, 50)), "p99_ms": float(np.percentile(ms, 99)),
                    "p50_ms_small": float(np.percentile(ms[~big], 50)), "p99_ms_small": float(np.percentile(ms[~big], 99)),
-                   "bit_exact": ok}
+                   "bit_exact": ok, "waves_by_lane": waves}
             if big.any():
                 row.update({"n_1M": int(big.sum()), "p50_ms_1M": float(np.percentile(ms[big], 50)),
                             "max_ms_1M": float(ms[big].max())})
@@ -255,7 +269,7 @@ def run_ours(args, rank, local, world, pg):
     clocks = Clocks(local)
     barrier(pg)
     clocks.start()
-    run_ms, dom_ms = [], []
+    run_ms, dom_ms, kern_ms = [], [], []
     wall0 = time.perf_counter()
     for _ in range(args.steps):
         flush.fill_(1)
@@ -265,6 +279,7 @@ def run_ours(args, rank, local, world, pg):
         r, d, dom_t = dev.batch_elapsed_ms()
         run_ms.append(r)
         dom_ms.append(d)
+        kern_ms.append(dev.batch_kernel_stats())   # per bucket kernel: (class, pairs, ms), CUDA events
     wall = time.perf_counter() - wall0
     tot_s = reduce_max(pg, sum(run_ms) / 1e3)
     clk = clocks.stop()
@@ -306,13 +321,23 @@ def run_ours(args, rank, local, world, pg):
     ops = OPS_RESIDUE * work["residue_steps"] + OPS_EUCLID * work["euclid_updates"] + \
         OPS_RECOVERY * work["recovery_updates"]
     run_s = statistics.mean(run_ms) / 1e3
-    achieved = ops / run_s
     alg_bytes = work["operand_bytes"]
-    traffic = None
+    # dominant kernel: the bucket kernel with the longest mean device time
+    nb = len(kern_ms[0])
+    mean_ms = [statistics.mean(k[b][2] for k in kern_ms) for b in range(nb)]
+    dom = max(range(nb), key=lambda b: mean_ms[b])
+    dom_cls, dom_pairs = kern_ms[0][dom][0], kern_ms[0][dom][1]
+    kw = dev.batch_kernel_work(dom)
+    dom_ops = OPS_RESIDUE * kw["residue_steps"] + OPS_EUCLID * kw["euclid_updates"] + \
+        OPS_RECOVERY * kw["recovery_updates"]
+    achieved = dom_ops / (mean_ms[dom] / 1e3)
+    traffic = None   # DRAM bytes of one dominant launch, scaled from a captured launch of the same kernel
     try:
         with open(TRAFFIC_FILE) as f:
-            traffic = json.load(f).get("bytes_per_run")
-    except (OSError, ValueError):
+            tf = json.load(f)
+        if tf.get("size_class") == dom_cls:
+            traffic = tf["bytes_per_pair"] * dom_pairs
+    except (OSError, ValueError, KeyError):
         pass
     line = {
         "metric": "GCDs/s (mixed 1k-64k-bit batch, bit-exact vs mpz_gcd)",
@@ -336,9 +361,12 @@ def run_ours(args, rank, local, world, pg):
         "tuning": tuning,
         "roofline": {"bound": "int", "achieved": achieved / 1e9, "peak": int_peak / 1e9, "unit": "Gop/s",
                      "frac": achieved / int_peak, "traffic": traffic,
-                     "kernel": "all launches of one step (%d persistent bucket kernels)" % launches,
-                     "model": "ops = 9*residue_steps + 257*euclid_updates + 124*recovery_updates",
+                     "kernel": "dominant bucket kernel: size class %d, %d pairs, %.1f ms per launch (CUDA events "
+                               "on its stream)" % (dom_cls, dom_pairs, mean_ms[dom]),
+                     "model": "ops = 9*residue_steps + 257*euclid_updates + 124*recovery_updates of that kernel's "
+                              "pairs (the reference formulation's integer ops)",
                      "peak_source": "in-repo IMAD microbenchmark (mgcd_int_peak), measured live",
+                     "whole_step": {"achieved": ops / run_s / 1e9, "frac": ops / run_s / int_peak},
                      "hbm": {"achieved_gbs": alg_bytes / run_s / 1e9, "peak_gbs": peaks.get("hbm_gbs"),
                              "frac": alg_bytes / run_s / 1e9 / peaks.get("hbm_gbs", 6800.0),
                              "peak_source": peaks_kind}},

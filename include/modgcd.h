@@ -176,6 +176,9 @@ int mgcd_batch_use_graph(mgcd_context *ctx, int enable);
    size class, pair count and device time (the time includes waiting for SMs that other
    concurrently running classes hold). */
 int mgcd_batch_kernel_stats(const mgcd_context *ctx, int i, int *cls, int *pairs, float *ms);
+/* Work of kernel i of the last downloaded batch by the cost model of mgcd_batch_work. */
+int mgcd_batch_kernel_work(const mgcd_context *ctx, int i, double *residue_steps, double *euclid_updates,
+                           double *recovery_updates, double *operand_bytes);
 /* Pairs the last run had to rerun with the reference's moduli count. */
 int mgcd_batch_retried(const mgcd_context *ctx, int *pairs);
 /* Kernel launches the last mgcd_batch_run issued. */
@@ -238,6 +241,16 @@ int mgcd_serve_replay(mgcd_server *server, size_t npairs, const uint32_t *limbs,
 /* Waves launched, kernel launches, peak admitted bytes, requests answered. */
 int mgcd_serve_stats(mgcd_server *server, uint64_t *waves, uint64_t *launches, uint64_t *peak_bytes,
                      uint64_t *completed);
+/* One record per wave (the first 2^20 waves), times in seconds since the server started:
+   formed from the queue, its GPU work enqueued, its completion seen by the server thread,
+   its requests answered (digits copied back and converted). */
+typedef struct mgcd_wave_trace {
+  int32_t lane;            /* size class */
+  uint32_t requests;
+  double t_admit, t_launched, t_gpu_done, t_answered;
+} mgcd_wave_trace;
+/* Copies up to cap records; *n receives the number recorded so far. */
+int mgcd_serve_trace(mgcd_server *server, mgcd_wave_trace *out, size_t cap, size_t *n);
 
 /* ------------------------------------------------------------ allocation-free call ----
    No counterpart in the reference.  For callers that cannot allocate device memory when

@@ -70,6 +70,8 @@ SIGNATURES = {
     "mgcd_batch_kernel_stats": (_c.c_int, [_P, _c.c_int, _c.POINTER(_c.c_int), _c.POINTER(_c.c_int),
                                            _c.POINTER(_c.c_float)]),
     "mgcd_batch_retried": (_c.c_int, [_P, _c.POINTER(_c.c_int)]),
+    "mgcd_batch_kernel_work": (_c.c_int, [_P, _c.c_int, _c.POINTER(_c.c_double), _c.POINTER(_c.c_double),
+                                          _c.POINTER(_c.c_double), _c.POINTER(_c.c_double)]),
     "mgcd_set_cluster_size": (_c.c_int, [_P, _c.c_int]),
     "mgcd_get_cluster_size": (_c.c_int, [_P, _c.POINTER(_c.c_int)]),
     "mgcd_batch_use_graph": (_c.c_int, [_P, _c.c_int]),
@@ -87,6 +89,7 @@ SIGNATURES = {
                                      _c.POINTER(_c.c_double)]),
     "mgcd_serve_stats": (_c.c_int, [_P, _c.POINTER(_c.c_uint64), _c.POINTER(_c.c_uint64),
                                     _c.POINTER(_c.c_uint64), _c.POINTER(_c.c_uint64)]),
+    "mgcd_serve_trace": (_c.c_int, [_P, _P, _c.c_size_t, _c.POINTER(_c.c_size_t)]),
 }
 
 _lib = None
@@ -372,6 +375,14 @@ class Device:
             out.append((c.value, n.value, ms.value))
             i += 1
 
+    def batch_kernel_work(self, i):
+        """Cost-model work of kernel i of the last downloaded batch."""
+        r, e, m, b = (ctypes.c_double() for _ in range(4))
+        _check(self._lib.mgcd_batch_kernel_work(self._h, int(i), ctypes.byref(r), ctypes.byref(e), ctypes.byref(m),
+                                                ctypes.byref(b)))
+        return {"residue_steps": r.value, "euclid_updates": e.value, "recovery_updates": m.value,
+                "operand_bytes": b.value}
+
     def batch_retried(self):
         n = ctypes.c_int()
         _check(self._lib.mgcd_batch_retried(self._h, ctypes.byref(n)))
@@ -479,6 +490,17 @@ class Server:
         g, g_off, g_len, st, lat, mk = self.replay_packed(*pack_pairs(us, vs), arrival_s)
         res = [from_limbs(g[int(o): int(o) + int(n)]) for o, n in zip(g_off, g_len)]
         return res, st, lat, mk
+
+    WAVE_TRACE = np.dtype([("lane", "<i4"), ("requests", "<u4"), ("t_admit", "<f8"), ("t_launched", "<f8"),
+                           ("t_gpu_done", "<f8"), ("t_answered", "<f8")])
+
+    def trace(self):
+        """Per-wave records (mgcd_serve_trace) as a numpy structured array."""
+        n = ctypes.c_size_t()
+        _check(self._lib.mgcd_serve_trace(self._h, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value, dtype=self.WAVE_TRACE)
+        _check(self._lib.mgcd_serve_trace(self._h, out.ctypes.data if n.value else None, n.value, ctypes.byref(n)))
+        return out[: n.value]
 
     def stats(self):
         w, l, p, c = (ctypes.c_uint64() for _ in range(4))

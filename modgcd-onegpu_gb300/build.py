@@ -66,8 +66,8 @@ def build(verbose=False, force=False):
     for f in ("mgcd_kernels.cu", "mgcd_noalloc.cu", "mgcd_radix_dev.cu", "mgcd_certify.cu"):
         src = os.path.join(CSRC, f)
         obj = os.path.join(BUILD, f + ".o")
-        cmd = [NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-v",
-                               "-c", src, "-o", obj]
+        cmd = [NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-v"] + \
+            os.environ.get("MGCD_NVCC_FLAGS", "").split() + ["-c", src, "-o", obj]
         units.append((obj, [src] + hdrs, cmd))
     for f in ("mgcd_capi.cpp", "mgcd_serve.cpp", "mgcd_moduli.cpp", "mgcd_radix.cpp", "GmpCudaDevice.cpp"):
         src = os.path.join(CSRC, f)

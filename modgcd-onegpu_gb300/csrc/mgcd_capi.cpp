@@ -78,11 +78,11 @@ void HostBuf::release()
   bytes = 0;
 }
 
-cudaError_t Plan::create()
+cudaError_t Plan::create(int priority)
 {
-  if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) return cudaErrorUnknown;
+  if (cudaStreamCreateWithPriority(&stream, cudaStreamNonBlocking, priority) != cudaSuccess) return cudaErrorUnknown;
   for (int i = 0; i < NSTREAMS; ++i)
-    if (cudaStreamCreateWithFlags(&bstream[i], cudaStreamNonBlocking) != cudaSuccess ||
+    if (cudaStreamCreateWithPriority(&bstream[i], cudaStreamNonBlocking, priority) != cudaSuccess ||
         cudaEventCreateWithFlags(&ev_b[i], cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreate(&t_b0[i]) != cudaSuccess || cudaEventCreate(&t_b1[i]) != cudaSuccess)
       return cudaErrorUnknown;
@@ -215,6 +215,10 @@ int mgcd_create(int device, int L, mgcd_context** out)
 {
   if (!out || (L != 22 && L != 27 && L != 32)) return MGCD_ERR_INVALID_ARG;
   *out = nullptr;
+  // Batches and servers keep many streams busy at once; with the default 8 hardware
+  // connections unrelated streams share queues and wait on each other.  Only takes effect
+  // if the process has not created its CUDA context yet; a caller's setting is kept.
+  setenv("CUDA_DEVICE_MAX_CONNECTIONS", "32", 0);
   int n = 0;
   mgcd_device_count(&n);
   if (device < 0) {
@@ -456,7 +460,7 @@ static int schedule(mgcd_context* c, Plan& P, const std::vector<PairDesc>& descs
     bk.scratch_off = scratch;
     if (b == CLUSTER_CLASS) {
       // one pair per cluster; more CTAs per cluster when a pair's share exceeds shared memory
-      int cs = c->cfg[b].csize;
+      int cs = P.cluster_ctas ? P.cluster_ctas : c->cfg[b].csize;
       while (cs < MAX_CLUSTER && cluster_batch_smem_bytes(cs, bk.nq_max) > c->smem_optin) cs *= 2;
       cs = std::min(cs, MAX_CLUSTER);
       bk.csize = cs;
@@ -753,16 +757,26 @@ int mgcd::fetch(mgcd_context* c, Plan& P)
   const uint32_t* cnt = P.h_count.as<uint32_t>();
   const int32_t* st = P.h_status.as<int32_t>();
   double R = 0, E = 0, M = 0, B = 0;
+  std::vector<double> pw(4 * ng, 0.0);    // per pair: R, E, M, B
   for (size_t k = 0; k < ng; ++k) {
     const PairDesc& d = P.descs[k];
-    R += (double)d.nq * (d.u_len + d.v_len);
-    B += 4.0 * (d.u_len + d.v_len);
-    if (st[k] != ST_OK) continue;
-    const double I = it[k], K = cnt[k], N = P.eff_nq[k];
-    E += I * N - I * (I + 1) / 2;
-    M += K * (N - I) - K * (K + 1) / 2;
+    double* w = &pw[4 * k];
+    w[0] = (double)d.nq * (d.u_len + d.v_len);
+    w[3] = 4.0 * (d.u_len + d.v_len);
+    if (st[k] == ST_OK) {
+      const double I = it[k], K = cnt[k], N = P.eff_nq[k];
+      w[1] = I * N - I * (I + 1) / 2;
+      w[2] = K * (N - I) - K * (K + 1) / 2;
+    }
+    R += w[0]; E += w[1]; M += w[2]; B += w[3];
   }
   P.work[0] = R; P.work[1] = E; P.work[2] = M; P.work[3] = B;
+  P.bucket_work.assign(4 * P.buckets.size(), 0.0);
+  for (size_t b = 0; b < P.buckets.size(); ++b)
+    for (uint32_t i = 0; i < P.buckets[b].n; ++i) {
+      const uint32_t k = P.order[P.buckets[b].first + i];
+      for (int x = 0; x < 4; ++x) P.bucket_work[4 * b + x] += pw[4 * k + x];
+    }
   return MGCD_OK;
 }
 
@@ -971,6 +985,20 @@ int mgcd_batch_kernel_stats(const mgcd_context* c, int i, int* cls, int* pairs, 
   if (cls) *cls = P.buckets[i].cls;
   if (pairs) *pairs = (int)P.buckets[i].n;
   if (ms) *ms = t;
+  return MGCD_OK;
+}
+
+int mgcd_batch_kernel_work(const mgcd_context* c, int i, double* residue_steps, double* euclid_updates,
+                           double* recovery_updates, double* operand_bytes)
+{
+  if (!c) return MGCD_ERR_INVALID_ARG;
+  const Plan& P = c->main;
+  if (i < 0 || 4 * (size_t)i + 3 >= P.bucket_work.size()) return MGCD_ERR_INVALID_ARG;
+  const double* w = &P.bucket_work[4 * (size_t)i];
+  if (residue_steps) *residue_steps = w[0];
+  if (euclid_updates) *euclid_updates = w[1];
+  if (recovery_updates) *recovery_updates = w[2];
+  if (operand_bytes) *operand_bytes = w[3];
   return MGCD_OK;
 }
 

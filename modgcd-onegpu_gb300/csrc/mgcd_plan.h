@@ -74,20 +74,22 @@ struct Plan {
   size_t nglimbs = 0;                  // result limbs reserved (sum of g_cap)
   bool plain = false;                  // single-pair latency policy
   bool graphable = true;               // may be recorded into a CUDA graph (context setting)
+  int cluster_ctas = 0;                // CTAs per cluster of size class 3 (0: the context's setting)
 
   DevBuf d_limbs, d_pairs, d_order, d_digits, d_count, d_iters, d_status, d_queue, d_scratch, d_gsync, d_retry;
   DevBuf d_glimbs, d_glen;             // binary gcds converted on the device
   HostBuf h_count, h_iters, h_status, h_digits, h_glimbs, h_glen;
   int launches = 0, retried = 0;
   bool ran = false, synced = false, bucket_timed = false;
-  double work[4] = {0, 0, 0, 0};
+  double work[4] = {0, 0, 0, 0};       // residue steps, loop updates, recovery updates, operand bytes
+  std::vector<double> bucket_work;     // the same per bucket kernel (4 per bucket)
   uint64_t h2d_bytes = 0, d2h_bytes = 0;
 
   // CUDA graph of the plan's GPU work; dropped whenever a buffer it uses moves
   cudaGraphExec_t graph = nullptr;
   int graph_kernels = 0;
 
-  cudaError_t create();
+  cudaError_t create(int priority = 0);   // streams at this priority (lower = more urgent)
   void destroy(cudaMemPool_t pool);
   void drop_graph();
   size_t device_bytes() const;

@@ -69,7 +69,11 @@ struct Wave {
   std::vector<uint64_t> uo, vo, goff;
   std::vector<uint32_t> ul, vl, gcap, glen, gbuf;
   std::vector<int32_t> st;
+  size_t trace = 0;                    // index of this wave's record in the server trace
 };
+
+constexpr size_t MAX_TRACE = size_t(1) << 20;   // wave records kept
+constexpr int SERVE_CLUSTER_CTAS = 8;            // CTAs per cluster for class-3 requests
 
 size_t strip(const uint32_t* x, size_t n)
 {
@@ -92,6 +96,8 @@ struct mgcd_server {
   std::thread th;
   bool stop = false;
   uint64_t n_waves = 0, n_launches = 0, n_done = 0;
+  double t0 = 0;                       // server start (trace clock origin)
+  std::vector<mgcd_wave_trace> trace;
 };
 
 namespace {
@@ -153,10 +159,15 @@ void serve_loop(mgcd_server* S)
       if (!w.busy) continue;
       const cudaError_t q = cudaEventQuery(w.done);
       if (q == cudaErrorNotReady) continue;
+      const double t_gpu = now_s();
       lk.unlock();
       const int rc = q == cudaSuccess ? finish_wave(S, w) : MGCD_ERR_CUDA;
       const double t = now_s();
       lk.lock();
+      if (w.trace < S->trace.size()) {
+        S->trace[w.trace].t_gpu_done = t_gpu - S->t0;
+        S->trace[w.trace].t_answered = t - S->t0;
+      }
       for (size_t i = 0; i < w.reqs.size(); ++i) {
         Request* r = w.reqs[i];
         if (rc == MGCD_OK) {
@@ -198,11 +209,16 @@ void serve_loop(mgcd_server* S)
       S->peak_bytes = std::max(S->peak_bytes, S->in_flight);
       w->bytes = bytes;
       w->busy = true;
+      const double t_admit = now_s() - S->t0;
       lk.unlock();
       const int rc = start_wave(S, *w);
+      const double t_launched = now_s() - S->t0;
       lk.lock();
       ++S->n_waves;
       S->n_launches += (uint64_t)w->plan.launches;
+      w->trace = S->trace.size();
+      if (S->trace.size() < MAX_TRACE)
+        S->trace.push_back(mgcd_wave_trace{lane, (uint32_t)w->reqs.size(), t_admit, t_launched, 0.0, 0.0});
       if (rc != MGCD_OK) {   // answer the wave's requests with the failure
         cudaStreamSynchronize(w->plan.stream);
         const double t = now_s();
@@ -314,15 +330,22 @@ int mgcd_serve_start(mgcd_context* c, size_t budget_bytes, mgcd_server** out)
   auto* S = new mgcd_server();
   S->c = c;
   S->budget = budget_bytes;
+  S->t0 = now_s();
   std::vector<int> lanes;
   for (int l = 0; l < NLANES; ++l) lanes.insert(lanes.end(), LANE_SLOTS[l], l);
   S->waves.resize(lanes.size());
+  // The short requests' lanes get the most urgent stream priority, so that CTAs of their
+  // waves are scheduled first whenever SMs free up; class-3 requests (seconds each) the least.
+  int least = 0, greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&least, &greatest);
   int rc = MGCD_OK;
   for (size_t i = 0; i < S->waves.size() && rc == MGCD_OK; ++i) {
     Wave& w = S->waves[i];
     w.lane = lanes[i];
     w.plan.graphable = false;
-    if (w.plan.create() != cudaSuccess || cudaEventCreateWithFlags(&w.done, cudaEventDisableTiming) != cudaSuccess)
+    if (w.lane == CLUSTER_CLASS) w.plan.cluster_ctas = SERVE_CLUSTER_CTAS;
+    if (w.plan.create(w.lane == CLUSTER_CLASS ? least : greatest) != cudaSuccess ||
+        cudaEventCreateWithFlags(&w.done, cudaEventDisableTiming) != cudaSuccess)
       rc = MGCD_ERR_CUDA;
   }
   if (rc != MGCD_OK) {
@@ -433,6 +456,16 @@ int mgcd_serve_replay(mgcd_server* S, size_t n, const uint32_t* limbs, const uin
   }
   if (makespan_s) *makespan_s = last - t0;
   return rc;
+}
+
+int mgcd_serve_trace(mgcd_server* S, mgcd_wave_trace* out, size_t cap, size_t* n)
+{
+  if (!S || !n || (cap && !out)) return MGCD_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> g(S->mu);
+  *n = S->trace.size();
+  const size_t k = std::min(cap, S->trace.size());
+  if (k) std::memcpy(out, S->trace.data(), k * sizeof(mgcd_wave_trace));
+  return MGCD_OK;
 }
 
 int mgcd_serve_stats(mgcd_server* S, uint64_t* waves, uint64_t* launches, uint64_t* peak_bytes,

@@ -459,20 +459,28 @@ static int schedule(mgcd_context* c, Plan& P, const std::vector<PairDesc>& descs
     bk.nq_max = descs[v[0]].nq;
     bk.scratch_off = scratch;
     if (b == CLUSTER_CLASS) {
-      // one pair per cluster; more CTAs per cluster when a pair's share exceeds shared memory
+      // k pairs per cluster; more CTAs per cluster when a CTA's share of the moduli would
+      // not fit its shared memory (16 KB kept for the kernel's static shared memory)
+      if (P.cluster_k) {
+        bk.k = P.cluster_k;
+        if (bk.k > 1 && bk.threads > 512) bk.threads = 512;
+      }
       int cs = P.cluster_ctas ? P.cluster_ctas : c->cfg[b].csize;
-      while (cs < MAX_CLUSTER && cluster_batch_smem_bytes(cs, bk.nq_max) > c->smem_optin) cs *= 2;
+      const size_t room = c->smem_optin - 16384;
+      while (cs < MAX_CLUSTER && cluster_batch_smem_bytes(cs, bk.nq_max, bk.k) > room) cs *= 2;
       cs = std::min(cs, MAX_CLUSTER);
       bk.csize = cs;
-      bk.k = 1;
-      bk.smem = cluster_batch_smem_bytes(cs, bk.nq_max);
+      bk.smem = cluster_batch_smem_bytes(cs, bk.nq_max, bk.k);
       int nc = 0;
-      if (bk.smem > c->smem_optin || cluster_batch_max_clusters(bk.threads, cs, bk.smem, &nc) != cudaSuccess ||
-          nc < 1)
+      if (bk.smem > room || cluster_batch_max_clusters(bk.threads, bk.k, cs, bk.smem, &nc) != cudaSuccess || nc < 1)
         return MGCD_ERR_GRID;
-      bk.grid = (int)std::min<size_t>(v.size(), (size_t)nc);
-      scratch += (size_t)bk.grid * 4 * bk.nq_max;
+      bk.grid = (int)std::min<size_t>((v.size() + bk.k - 1) / bk.k, (size_t)nc);
+      scratch += (size_t)bk.grid * 4 * bk.k * bk.nq_max;
     } else {
+      // fewer pairs per CTA when k of the bucket's largest pairs would not fit shared memory
+      // (16 KB kept for the kernel's static shared memory)
+      while (bk.k > 1 && batch_smem_bytes(bk.threads, bk.k, bk.nq_max) > c->smem_optin - 16384) bk.k /= 2;
+      if (bk.k == 4 && bk.threads > 512) bk.threads = 512;
       bk.smem = batch_smem_bytes(bk.threads, bk.k, bk.nq_max);
       int bps = 0;
       if (batch_max_blocks_per_sm(bk.threads, bk.k, bk.smem, &bps) != cudaSuccess || bps < 1) return MGCD_ERR_GRID;
@@ -519,7 +527,7 @@ static int launch_set(mgcd_context* c, Plan& P, const std::vector<Bucket>& bucke
     CK(cudaStreamWaitEvent(P.bstream[b], P.ev_start, 0));
     if (time_buckets) CK(cudaEventRecord(P.t_b0[b], P.bstream[b]));
     if (bk.csize)
-      CK(launch_cluster_batch(a, bk.threads, bk.csize, bk.grid, bk.smem, P.bstream[b]));
+      CK(launch_cluster_batch(a, bk.threads, bk.k, bk.csize, bk.grid, bk.smem, P.bstream[b]));
     else
       CK(launch_batch(a, bk.threads, bk.k, bk.grid, bk.smem, P.bstream[b]));
     if (time_buckets) CK(cudaEventRecord(P.t_b1[b], P.bstream[b]));
@@ -850,12 +858,21 @@ int mgcd_set_nq_scale(mgcd_context* c, float scale)
   return MGCD_OK;
 }
 
+// Launch configurations that exist: CTA size 256/512/1024; k = 1, 2, 4 with <= 512 threads,
+// or 8 with 512 threads (not in the cluster class); in the cluster class k = 2 also needs
+// <= 512 threads.
+static bool valid_class_cfg(int cls, int threads, int k, float nq_scale)
+{
+  if (cls < 0 || cls >= NSTREAMS || !(nq_scale >= 0.5f && nq_scale <= 1.0f)) return false;
+  if (threads != 256 && threads != 512 && threads != 1024) return false;
+  if (k == 8) return threads == 512 && cls != CLUSTER_CLASS;
+  if (k != 1 && k != 2 && !(k == 4 && threads <= 512)) return false;
+  return !(cls == CLUSTER_CLASS && k == 2 && threads > 512);
+}
+
 int mgcd_set_size_class(mgcd_context* c, int cls, int threads, int k, float nq_scale)
 {
-  if (!c || cls < 0 || cls >= NSTREAMS || !(nq_scale >= 0.5f && nq_scale <= 1.0f)) return MGCD_ERR_INVALID_ARG;
-  if (threads != 256 && threads != 512 && threads != 1024) return MGCD_ERR_INVALID_ARG;
-  if (k != 1 && k != 2 && !(k == 4 && threads <= 512)) return MGCD_ERR_INVALID_ARG;
-  if (cls == CLUSTER_CLASS && k != 1) return MGCD_ERR_INVALID_ARG;
+  if (!c || !valid_class_cfg(cls, threads, k, nq_scale)) return MGCD_ERR_INVALID_ARG;
   c->cfg[cls].threads = threads;
   c->cfg[cls].k = k;
   c->cfg[cls].nq_scale = nq_scale;
@@ -894,10 +911,8 @@ int mgcd_load_tuning(mgcd_context* c, const char* path)
     if (*s == '#' || *s == '\n' || *s == '\r' || *s == 0) continue;
     int cls, threads, k, cs;
     float sc;
-    if (std::sscanf(s, "%d %d %d %f %d", &cls, &threads, &k, &sc, &cs) != 5 || cls < 0 || cls >= NSTREAMS ||
-        (threads != 256 && threads != 512 && threads != 1024) || !(sc >= 0.5f && sc <= 1.0f) ||
-        (k != 1 && k != 2 && !(k == 4 && threads <= 512)) ||
-        (cls == CLUSTER_CLASS ? (k != 1 || cs < 2 || cs > MAX_CLUSTER) : cs != 0)) {
+    if (std::sscanf(s, "%d %d %d %f %d", &cls, &threads, &k, &sc, &cs) != 5 || !valid_class_cfg(cls, threads, k, sc) ||
+        (cls == CLUSTER_CLASS ? (cs < 2 || cs > MAX_CLUSTER) : cs != 0)) {
       rc = MGCD_ERR_INVALID_ARG;
       break;
     }

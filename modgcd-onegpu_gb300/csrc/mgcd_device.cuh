@@ -134,70 +134,6 @@ __device__ __forceinline__ uint32_t inv_mod(uint32_t x, uint32_t q, uint32_t qin
   return inv;
 }
 
-// N independent inverses x[i]^{-1} mod q[i] (in place) with the steps of inv_mod run side
-// by side: each phase loops while any instance still needs it and advances only those, so
-// one thread keeps N dependency chains in flight (the single inverse is a latency-bound
-// chain of ~20 dependent quotient steps).  Same arithmetic, bounds and self-check as
-// inv_mod.
-template <int N>
-__device__ __forceinline__ void inv_mod_n(uint32_t (&x)[N], const uint32_t (&q)[N], const uint32_t (&qinv)[N])
-{
-  uint32_t r0[N], r1[N], s0[N], s1[N], par[N];
-#pragma unroll
-  for (int i = 0; i < N; ++i) { r0[i] = q[i]; r1[i] = x[i]; s0[i] = 0u; s1[i] = 1u; par[i] = 0u; }
-  for (;;) {   // phase A
-    bool any = false;
-#pragma unroll
-    for (int i = 0; i < N; ++i) any |= r1[i] >= (1u << 22);
-    if (!any) break;
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-      if (r1[i] < (1u << 22)) continue;
-      const float est = __fmaf_rz(__uint2float_ru(r0[i]), rcp_approx(__uint2float_ru(r1[i])), -0x1p-9f);
-      uint32_t Q = __float2uint_rz(est);
-      uint32_t r = r0[i] - Q * r1[i];
-      if (r >= r1[i]) { r -= r1[i]; Q += 1; }
-      const uint32_t s = s0[i] + Q * s1[i];
-      r0[i] = r1[i]; r1[i] = r; s0[i] = s1[i]; s1[i] = s; par[i] ^= 1u;
-    }
-  }
-  float f0[N], f1[N];
-#pragma unroll
-  for (int i = 0; i < N; ++i) {   // phase B
-    if (r1[i] > 1u && r0[i] >= (1u << 22)) {
-      const uint32_t Q = r0[i] / r1[i];
-      const uint32_t r = r0[i] - Q * r1[i];
-      const uint32_t s = s0[i] + Q * s1[i];
-      r0[i] = r1[i]; r1[i] = r; s0[i] = s1[i]; s1[i] = s; par[i] ^= 1u;
-    }
-    f0[i] = (float)r0[i];
-    f1[i] = r1[i] > 1u ? (float)r1[i] : 1.0f;
-  }
-  for (int guard = 64; --guard;) {   // phase C
-    bool any = false;
-#pragma unroll
-    for (int i = 0; i < N; ++i) any |= f1[i] > 1.0f;
-    if (!any) break;
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-      if (!(f1[i] > 1.0f)) continue;
-      const float rc = rcp_approx(f1[i]);
-      float qm = __fmaf_rz(f0[i], rc, 8388607.5f);
-      const float qf = qm - 8388608.0f;
-      float rem = __fmaf_rn(-qf, f1[i], f0[i]);
-      if (rem >= f1[i]) { rem -= f1[i]; qm += 1.0f; }
-      const uint32_t Q = __float_as_uint(qm) - 0x4B000000u;
-      const uint32_t s = s0[i] + Q * s1[i];
-      f0[i] = f1[i]; f1[i] = rem; s0[i] = s1[i]; s1[i] = s; par[i] ^= 1u;
-    }
-  }
-#pragma unroll
-  for (int i = 0; i < N; ++i) {
-    const uint32_t inv = par[i] ? q[i] - s1[i] : s1[i];
-    x[i] = (redc((uint64_t)inv * x[i], q[i], qinv[i]) != redc(1ull, q[i], qinv[i])) ? inv_mod_slow(x[i], q[i]) : inv;
-  }
-}
-
 // Key of the reduction loop's pivot choice (postMinPair, GmpCudaDevice-getGcdKernel.cu:152-154):
 // high word |value| (0x80000000 for MOD_INFINITY), low word modulus - (value >= 0).
 __device__ __forceinline__ void t_key(uint32_t t, uint32_t q, uint32_t& hi, uint32_t& lo)
@@ -281,54 +217,6 @@ __device__ __forceinline__ void t_update_k(uint32_t (&t)[K], uint32_t q, uint32_
     if ((need >> s) & 1u) t[s] = mont_mul(p[s] > q ? p[s] - q : p[s], y, q, qinv);
   }
   if (need & 1u) t[0] = mont_mul(p[0] > q ? p[0] - q : p[0], Z, q, qinv);
-}
-
-// t_update_k for N moduli at once (q[n], one K-slot group each): the N batch inversions
-// share one inv_mod_n call, so a thread keeps N independent chains in flight.  An empty
-// group (mask[n] = 0, or no slot needing an inverse) inverts the Montgomery one instead.
-template <int K, int N>
-__device__ __forceinline__ void t_update_kn(uint32_t (&t)[N][K], const uint32_t (&q)[N], const uint32_t (&qinv)[N],
-                                            const uint32_t (&r1)[N], const uint32_t (&p)[K], const int32_t (&b)[K],
-                                            const uint32_t (&mask)[N])
-{
-  uint32_t x[N][K], P[N][K], Z[N], need[N];
-  bool any = false;
-#pragma unroll
-  for (int n = 0; n < N; ++n) {
-    need[n] = 0u;
-#pragma unroll
-    for (int s = 0; s < K; ++s) {
-      x[n][s] = r1[n];
-      if (!((mask[n] >> s) & 1u)) continue;
-      const uint32_t ts = t[n][s];
-      if (ts >= T_MARK) { t[n][s] = (ts == T_INF) ? 0u : ts; continue; }
-      if (q[n] == p[s]) { t[n][s] = T_RETIRED; continue; }
-      const uint32_t d = mod_sub(ts, from_signed(b[s], q[n]), q[n]);
-      if (d == 0u) { t[n][s] = T_INF; continue; }
-      x[n][s] = redc((uint64_t)d, q[n], qinv[n]);
-      need[n] |= 1u << s;
-    }
-    any |= need[n] != 0u;
-  }
-  if (!any) return;
-#pragma unroll
-  for (int n = 0; n < N; ++n) {
-    P[n][0] = x[n][0];
-#pragma unroll
-    for (int s = 1; s < K; ++s) P[n][s] = mont_mul(P[n][s - 1], x[n][s], q[n], qinv[n]);
-    Z[n] = P[n][K - 1];
-  }
-  inv_mod_n<N>(Z, q, qinv);
-#pragma unroll
-  for (int n = 0; n < N; ++n) {
-#pragma unroll
-    for (int s = K - 1; s >= 1; --s) {
-      const uint32_t y = mont_mul(Z[n], P[n][s - 1], q[n], qinv[n]);
-      Z[n] = mont_mul(Z[n], x[n][s], q[n], qinv[n]);
-      if ((need[n] >> s) & 1u) t[n][s] = mont_mul(p[s] > q[n] ? p[s] - q[n] : p[s], y, q[n], qinv[n]);
-    }
-    if (need[n] & 1u) t[n][0] = mont_mul(p[0] > q[n] ? p[0] - q[n] : p[0], Z[n], q[n], qinv[n]);
-  }
 }
 
 // Initial state t = u/v mod q from the residues.

@@ -107,10 +107,11 @@ cudaError_t launch_batch(const BatchArgs& a, int threads, int k, int grid, size_
 cudaError_t launch_cluster(const GridArgs& a, int threads, int ctas, size_t smem, cudaStream_t s);
 
 // Persistent batched kernel for pairs larger than one CTA: `clusters` thread-block
-// clusters of `csize` CTAs each pull pairs from the queue.  a.scratch_words = 4 * nq_max.
-size_t cluster_batch_smem_bytes(int csize, uint32_t nq_max);
-cudaError_t cluster_batch_max_clusters(int threads, int csize, size_t smem, int* clusters);
-cudaError_t launch_cluster_batch(const BatchArgs& a, int threads, int csize, int clusters, size_t smem,
+// clusters of `csize` CTAs each pull pairs from the queue, k pairs per cluster in lockstep
+// (k = 1: any CTA size; k = 2, 4: 256 or 512 threads).  a.scratch_words = 4 * k * nq_max.
+size_t cluster_batch_smem_bytes(int csize, uint32_t nq_max, int k);
+cudaError_t cluster_batch_max_clusters(int threads, int k, int csize, size_t smem, int* clusters);
+cudaError_t launch_cluster_batch(const BatchArgs& a, int threads, int k, int csize, int clusters, size_t smem,
                                  cudaStream_t s);
 
 // Resets the grid exchange state on the device (capturable in a CUDA graph).

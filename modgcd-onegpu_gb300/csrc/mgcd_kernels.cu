@@ -268,6 +268,220 @@ __global__ void __launch_bounds__(T, MINB) batchk_kernel(const BatchArgs a)
   }
 }
 
+// ------------------------------------------- K pairs per thread-block cluster, lockstep ----
+//
+// The cluster analogue of batchk_kernel for pairs larger than one CTA (size class 3).  A
+// cluster of C CTAs holds K pairs; CTA r owns global moduli [r * per, (r + 1) * per) of every
+// pair (per = ceil(nq_max / C), the same slice for all slots, so a thread's K updates share
+// one modulus and one inverse).  Pivot keys: each CTA reduces its K minima (one
+// __syncthreads), warp 0 stores them into every CTA of the cluster (DSMEM), one cluster
+// barrier, then every warp reduces the C values per slot.  Queue pops are made by CTA 0 and
+// broadcast the same way.  Set-up and finish of one slot run the cluster single-pair code
+// on the CTA's slice while the other slots wait.
+
+template <int K>
+struct ClusterSlotKeys {
+  unsigned long long key[2][K][MAX_CLUSTER];   // per slot: each CTA's minimum, double-buffered
+  uint32_t next;                               // queue index broadcast by CTA 0
+  uint32_t nloc[K];                            // this CTA's moduli of each slot's pair
+};
+
+template <int T, int K>
+__device__ __forceinline__ void cluster_min_keys(uint32_t (&kh)[K], uint32_t (&kl)[K], SlotSmem<K>& ss,
+                                                 ClusterSlotKeys<K>& ck, uint32_t& kparity, uint32_t& cparity)
+{
+  block_min_keys<T, K>(kh, kl, ss, kparity);
+  const uint32_t lane = threadIdx.x & 31u, me = cluster_rank(), nc = cluster_size();
+  if (threadIdx.x < 32u && lane < nc) {
+#pragma unroll
+    for (int s = 0; s < K; ++s)
+      st_cluster_u64(&ck.key[cparity][s][me], lane, ((unsigned long long)kh[s] << 32) | kl[s]);
+  }
+  cluster_sync_all();
+#pragma unroll
+  for (int s = 0; s < K; ++s) {
+    const unsigned long long k = lane < nc ? ck.key[cparity][s][lane] : ~0ull;
+    kh[s] = (uint32_t)(k >> 32);
+    kl[s] = (uint32_t)k;
+    warp_min_key(kh[s], kl[s]);
+  }
+  cparity ^= 1u;
+}
+
+template <int T, int K>
+__global__ void __launch_bounds__(T) cluster_batchk_kernel(const BatchArgs a)
+{
+  extern __shared__ __align__(16) uint32_t smem[];
+  __shared__ SlotSmem<K> ss;
+  __shared__ ClusterSlotKeys<K> ck;
+  __shared__ ClusterSmem cs;                          // single-slot exchanges (set-up, finish)
+  __shared__ RedSmem rs;
+  const uint32_t C = cluster_size(), r = cluster_rank();
+  const uint32_t per = (a.nq_max + C - 1) / C;        // slice of every slot's moduli
+  const uint32_t j0 = r * per;
+  uint32_t* const tS = smem;                          // K x per states
+  uint32_t* const acc2 = smem + (size_t)K * per;      // residues of v during set-up
+  uint32_t* const chunk = acc2 + per;
+  uint32_t* const scr = a.scratch + (size_t)(blockIdx.x / C) * a.scratch_words;   // per slot u0, v0, hist
+  const uint32_t NQS = a.nq_max;
+  const int L = a.L;
+  GridSync* const gcs = reinterpret_cast<GridSync*>(&cs);
+  // parities of the double-buffered exchanges: slot keys in the CTA (ss) and across the
+  // cluster (ck), single keys in the CTA (rs) and across the cluster (cs)
+  uint32_t kparity = 0, cparity = 0, bparity = 0, rparity = 0, repoch = 0;
+  uint32_t valid = 0, active = 0, redux = 0;
+  int rem[K], ubits[K], vbits[K];
+  uint32_t iters[K], p[K], kh[K], kl[K];
+  int32_t b[K];
+
+  cluster_sync_all();
+  auto load = [&](int s) -> bool {
+    if (r == 0 && threadIdx.x < C) {
+      const uint32_t k = __shfl_sync(0xFFFFFFFFu >> (32 - C), threadIdx.x == 0 ? atomicAdd(a.queue, 1u) : 0u, 0);
+      const uint32_t ad = (uint32_t)__cvta_generic_to_shared(&ck.next);
+      uint32_t ra;
+      asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(ad), "r"(threadIdx.x));
+      asm volatile("st.shared::cluster.u32 [%0], %1;" :: "r"(ra), "r"(k) : "memory");
+    }
+    cluster_sync_all();
+    const uint32_t k = ck.next;
+    cluster_sync_all();                               // everyone has read next before it changes
+    if (k >= a.npairs) return false;
+    if (threadIdx.x == 0) {
+      ss.pi[s] = a.order[k];
+      ss.d[s] = a.pairs[ss.pi[s]];
+      const uint32_t nq = ss.d[s].nq;
+      ck.nloc[s] = j0 >= nq ? 0u : (nq - j0 < per ? nq - j0 : per);
+    }
+    __syncthreads();
+    const PairDesc& d = ss.d[s];
+    const uint32_t nloc = ck.nloc[s];
+    uint32_t* ts = tS + (size_t)s * per;
+    uint32_t* u0 = scr + (size_t)s * 4 * NQS;
+    const ModConst* my = a.mods + j0;
+    residues<T>(a.limbs + d.u_off, d.u_len, my, nloc, ts, chunk);
+    residues<T>(a.limbs + d.v_off, d.v_len, my, nloc, acc2, chunk);
+    uint32_t h0 = 0xFFFFFFFFu, l0 = 0xFFFFFFFFu;
+    for (uint32_t j = threadIdx.x; j < nloc; j += T) {
+      const ModConst c = my[j];
+      const uint32_t u = ts[j], v = acc2[j];
+      u0[j0 + j] = u;
+      u0[NQS + j0 + j] = v;
+      const uint32_t t = t_init(u, v, c.q, c.qinv);
+      ts[j] = t;
+      uint32_t h, l;
+      t_key(t, c.q, h, l);
+      if (key_less(h, l, h0, l0)) { h0 = h; l0 = l; }
+    }
+    if (threadIdx.x == 32u * s) {
+      ss.lu[s] = (double)(((int)d.u_len - 1) * 32 + (32 - __clz(a.limbs[d.u_off + d.u_len - 1])));
+      ss.lv[s] = (double)(((int)d.v_len - 1) * 32 + (32 - __clz(a.limbs[d.v_off + d.v_len - 1])));
+    }
+    block_min_key<T>(h0, l0, rs, bparity);
+    cluster_min_key<T>(h0, l0, cs, rparity);
+    uint32_t p0;
+    int32_t b0;
+    key_pair(h0, l0, p0, b0);
+    put(p, s, p0);
+    put(b, s, b0);
+    put(rem, s, (int)d.nq);
+    put(ubits, s, ((int)d.u_len + 1) * 32);
+    put(vbits, s, ((int)d.v_len + 1) * 32);
+    put(iters, s, 0u);
+    return true;
+  };
+
+#pragma unroll 1
+  for (int s = 0; s < K; ++s)
+    if (load(s)) { valid |= 1u << s; active |= 1u << s; }
+
+  for (;;) {
+    const uint32_t done = valid & ~active;
+#pragma unroll 1
+    for (int s = 0; s < K; ++s) {
+      if (!((done >> s) & 1u)) continue;
+      const uint32_t pi = ss.pi[s];
+      const uint32_t it = pick(iters, s);
+      if (threadIdx.x == 0 && r == 0) a.iters[pi] = it;
+      if ((redux >> s) & 1u) {
+        if (threadIdx.x == 0 && r == 0) { a.status[pi] = ST_REDUX; a.count[pi] = 0; }
+      } else {
+        uint32_t* u0 = scr + (size_t)s * 4 * NQS;
+        finish_pair<T, SYNC_CLUSTER>(a.mods, ss.d[s], L, j0, ck.nloc[s], tS + (size_t)s * per, rs, rparity, repoch,
+                                     gcs, u0 + j0, u0 + NQS + j0, reinterpret_cast<const int2*>(u0 + 2 * (size_t)NQS),
+                                     it, pick(rem, s), ss.lu[s], ss.lv[s], a.digits, a.count + pi, a.status + pi,
+                                     a.inv);
+      }
+      cluster_sync_all();                             // the slot's scratch is free in every CTA
+      valid &= ~(1u << s);
+      redux &= ~(1u << s);
+      if (load(s)) { valid |= 1u << s; active |= 1u << s; }
+    }
+    if (!valid) break;
+
+#pragma unroll
+    for (int s = 0; s < K; ++s) {
+      if (!((active >> s) & 1u)) continue;
+      if (b[s] == MOD_INFINITY) { active &= ~(1u << s); continue; }
+      if (threadIdx.x == 32u * s) {
+        if (r == 0) {
+          int2* hist = reinterpret_cast<int2*>(scr + (size_t)s * 4 * NQS + 2 * (size_t)NQS);
+          hist[iters[s]] = make_int2((int)p[s], b[s]);
+        }
+        const uint32_t ab = b[s] < 0 ? 0u - (uint32_t)b[s] : (uint32_t)b[s];
+        double sum = ss.lu[s];
+        if (ab != 0u) {
+          const double y = ss.lv[s] + (double)log2f((float)ab);
+          const double m = y > sum ? y : sum, dd = y > sum ? y - sum : sum - y;
+          sum = m + (dd < 40.0 ? (double)log2f(1.0f + exp2f(-(float)dd)) : 0.0);
+        }
+        ss.lu[s] = ss.lv[s];
+        ss.lv[s] = sum - (double)log2f((float)p[s]) + 1e-4;
+      }
+      ++iters[s];
+      rem[s] -= 1;
+      const uint32_t ab = b[s] < 0 ? 0u - (uint32_t)b[s] : (uint32_t)b[s];
+      const int tbits = ubits[s] - (L - 1) + __ffs((int)ab);
+      ubits[s] = vbits[s];
+      vbits[s] = tbits;
+      if (rem[s] * (L - 2) <= ubits[s]) { redux |= 1u << s; active &= ~(1u << s); }
+    }
+    if (!active) continue;
+
+    uint32_t nmax = 0;
+#pragma unroll
+    for (int s = 0; s < K; ++s) {
+      if ((active >> s) & 1u) nmax = max(nmax, ck.nloc[s]);
+      kh[s] = kl[s] = 0xFFFFFFFFu;
+    }
+    for (uint32_t j = threadIdx.x; j < nmax; j += T) {
+      uint32_t m = 0, tv[K];
+#pragma unroll
+      for (int s = 0; s < K; ++s) {
+        const bool on = ((active >> s) & 1u) && j < ck.nloc[s];
+        m |= (uint32_t)on << s;
+        tv[s] = on ? tS[(size_t)s * per + j] : T_RETIRED;
+      }
+      if (!m) continue;
+      const ModConst c = a.mods[j0 + j];
+      t_update_k<K>(tv, c.q, c.qinv, c.r1, p, b, m);
+#pragma unroll
+      for (int s = 0; s < K; ++s) {
+        if (!((m >> s) & 1u)) continue;
+        tS[(size_t)s * per + j] = tv[s];
+        uint32_t h, l;
+        t_key(tv[s], c.q, h, l);
+        if (key_less(h, l, kh[s], kl[s])) { kh[s] = h; kl[s] = l; }
+      }
+    }
+    cluster_min_keys<T, K>(kh, kl, ss, ck, kparity, cparity);
+#pragma unroll
+    for (int s = 0; s < K; ++s)
+      if ((active >> s) & 1u) key_pair(kh[s], kl[s], p[s], b[s]);
+  }
+  cluster_sync_all();   // no CTA leaves while others may still address its shared memory
+}
+
 // One pair over a cooperative grid of GRID_THREADS-thread CTAs; CTA c owns moduli
 // [c * per_cta, min(nq, (c + 1) * per_cta)).
 template <int T>
@@ -444,6 +658,7 @@ static const void* batch_fn_for(int threads, int k)
       default: return nullptr;
     }
   }
+  if (k == 8 && threads == 512) return reinterpret_cast<const void*>(&batchk_kernel<512, 8>);
   return nullptr;
 }
 
@@ -511,14 +726,35 @@ static cudaError_t prepare_cluster_fn(const void* fn, int csize, size_t smem)
   return e;
 }
 
-size_t cluster_batch_smem_bytes(int csize, uint32_t nq_max)
+static const void* cluster_batch_fn_k(int threads, int k)
 {
-  return grid_smem_bytes((nq_max + csize - 1) / csize);
+  if (k == 1) return cluster_batch_fn(threads);
+  if (k == 2) {
+    switch (threads) {
+      case 256: return reinterpret_cast<const void*>(&cluster_batchk_kernel<256, 2>);
+      case 512: return reinterpret_cast<const void*>(&cluster_batchk_kernel<512, 2>);
+      default: return nullptr;
+    }
+  }
+  if (k == 4) {
+    switch (threads) {
+      case 256: return reinterpret_cast<const void*>(&cluster_batchk_kernel<256, 4>);
+      case 512: return reinterpret_cast<const void*>(&cluster_batchk_kernel<512, 4>);
+      default: return nullptr;
+    }
+  }
+  return nullptr;
 }
 
-cudaError_t cluster_batch_max_clusters(int threads, int csize, size_t smem, int* clusters)
+size_t cluster_batch_smem_bytes(int csize, uint32_t nq_max, int k)
 {
-  const void* fn = cluster_batch_fn(threads);
+  const size_t per = (nq_max + csize - 1) / csize;
+  return sizeof(uint32_t) * ((size_t)(k > 1 ? k + 1 : 2) * per + CHUNK);
+}
+
+cudaError_t cluster_batch_max_clusters(int threads, int k, int csize, size_t smem, int* clusters)
+{
+  const void* fn = cluster_batch_fn_k(threads, k);
   cudaError_t e = prepare_cluster_fn(fn, csize, smem);
   if (e != cudaSuccess) return e;
   cudaLaunchAttribute attr[1];
@@ -537,9 +773,10 @@ cudaError_t launch_cluster(const GridArgs& a, int threads, int ctas, size_t smem
   return cudaLaunchKernelExC(&cfg, fn, args);
 }
 
-cudaError_t launch_cluster_batch(const BatchArgs& a, int threads, int csize, int clusters, size_t smem, cudaStream_t s)
+cudaError_t launch_cluster_batch(const BatchArgs& a, int threads, int k, int csize, int clusters, size_t smem,
+                                 cudaStream_t s)
 {
-  const void* fn = cluster_batch_fn(threads);
+  const void* fn = cluster_batch_fn_k(threads, k);
   cudaError_t e = prepare_cluster_fn(fn, csize, smem);
   if (e != cudaSuccess) return e;
   cudaLaunchAttribute attr[1];

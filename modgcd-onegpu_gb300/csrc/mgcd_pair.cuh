@@ -289,27 +289,7 @@ __device__ void run_pair(const uint32_t* __restrict__ limbs, const PairDesc& d, 
     }
     kh = 0xFFFFFFFFu;
     kl = 0xFFFFFFFFu;
-    uint32_t j = threadIdx.x;
-#ifndef MGCD_PAIR_MODS
-#define MGCD_PAIR_MODS 1
-#endif
-    for (; MGCD_PAIR_MODS && j + T < nloc; j += 2 * T) {   // two moduli at a time: two inversion chains in flight
-      const uint32_t j1 = j + T;
-      const ModConst c0 = my[j], c1 = my[j1];
-      uint32_t tv[2][1] = {{st[j]}, {st[j1]}};
-      const uint32_t q2[2] = {c0.q, c1.q}, qi2[2] = {c0.qinv, c1.qinv}, r12[2] = {c0.r1, c1.r1};
-      const uint32_t pp[1] = {p}, mk[2] = {1u, 1u};
-      const int32_t bb[1] = {b};
-      t_update_kn<1, 2>(tv, q2, qi2, r12, pp, bb, mk);
-      st[j] = tv[0][0];
-      st[j1] = tv[1][0];
-      uint32_t h, l;
-      t_key(tv[0][0], c0.q, h, l);
-      if (key_less(h, l, kh, kl)) { kh = h; kl = l; }
-      t_key(tv[1][0], c1.q, h, l);
-      if (key_less(h, l, kh, kl)) { kh = h; kl = l; }
-    }
-    for (; j < nloc; j += T) {
+    for (uint32_t j = threadIdx.x; j < nloc; j += T) {
       const ModConst c = my[j];
       const uint32_t t = t_update(st[j], c.q, c.qinv, p, b);
       st[j] = t;

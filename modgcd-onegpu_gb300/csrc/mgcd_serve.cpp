@@ -343,7 +343,10 @@ int mgcd_serve_start(mgcd_context* c, size_t budget_bytes, mgcd_server** out)
     Wave& w = S->waves[i];
     w.lane = lanes[i];
     w.plan.graphable = false;
-    if (w.lane == CLUSTER_CLASS) w.plan.cluster_ctas = SERVE_CLUSTER_CTAS;
+    if (w.lane == CLUSTER_CLASS) {   // one request per wave: one pair per cluster
+      w.plan.cluster_ctas = SERVE_CLUSTER_CTAS;
+      w.plan.cluster_k = 1;
+    }
     if (w.plan.create(w.lane == CLUSTER_CLASS ? least : greatest) != cudaSuccess ||
         cudaEventCreateWithFlags(&w.done, cudaEventDisableTiming) != cudaSuccess)
       rc = MGCD_ERR_CUDA;

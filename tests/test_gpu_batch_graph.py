@@ -142,3 +142,38 @@ def test_tuning_table_roundtrip_and_bad_tables(mgcd, tmp_path):
             rng = random.Random(46)
             us, vs = _skewed(rng, 1, 200000, 300)
             assert dev.gcd_batch(us, vs) == [math.gcd(u, v) for u, v in zip(us, vs)]
+
+
+@pytest.mark.parametrize("threads,k,ctas,scale", [(512, 2, 8, 1.0), (512, 4, 16, 1.0), (256, 4, 8, 1.0),
+                                                  (512, 2, 4, 0.6)])
+def test_cluster_class_k_pairs_per_cluster(mgcd, threads, k, ctas, scale):
+    """Class-3 pairs k to a cluster in lockstep (shared inverses); slots refill from the
+    queue; with a low moduli fraction some pairs fail certification and are rerun."""
+    rng = random.Random(48 + 3 * k + ctas)
+    us, vs = _skewed(rng, 5, 230000, 40)
+    v = rng.getrandbits(120000) | 1                 # v | u
+    us.append(v * (rng.getrandbits(100000) | 1))
+    vs.append(v)
+    us.append(rng.getrandbits(240000) | 1)          # (almost surely) coprime
+    vs.append(rng.getrandbits(239000) | 1)
+    with mgcd.Device(0, 32) as dev:
+        dev.set_size_class(3, threads, k, scale)
+        dev.set_cluster_size(ctas)
+        assert dev.gcd_batch(us, vs) == [math.gcd(a, b) for a, b in zip(us, vs)]
+
+
+@pytest.mark.parametrize("k", [4, 8])
+def test_pairs_per_cta_step_down_when_shared_memory_is_short(mgcd, k):
+    """A size-class-2 pair near 16,384 moduli with k pairs per CTA would need more than one
+    CTA's shared memory; the bucket runs with fewer pairs per CTA instead of failing."""
+    rng = random.Random(60 + k)
+    us, vs = _skewed(rng, 0, 0, 30)
+    for nb in (175000, 150000, 60000):
+        a, b = _pair(rng, nb, rng.randint(1, nb // 3))
+        us.append(a)
+        vs.append(b)
+    with mgcd.Device(0, 32) as dev:
+        for cls in (1, 2):
+            dev.set_size_class(cls, 512, k, 1.0)
+        assert mgcd.moduli_needed(175000) > 15000
+        assert dev.gcd_batch(us, vs) == [math.gcd(a, b) for a, b in zip(us, vs)]

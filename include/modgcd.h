@@ -151,10 +151,9 @@ int mgcd_test_force_moduli(mgcd_context *ctx, unsigned nq);
    <= 1,024 moduli, 1 = <= 4,096, 2 = <= 16,384 (one CTA per pair), 3 = larger (one
    thread-block cluster per k pairs).  threads: CTA size (256, 512, 1024); k: pairs one CTA
    (class 3: one cluster) runs in lockstep, sharing one modular inverse per modulus and
-   iteration (1, 2, 4 with threads <= 512, or 8 with threads = 512 outside class 3; in class
-   3, k = 2 also needs threads <= 512; a bucket whose k largest pairs would not fit one
-   CTA's shared memory runs with fewer pairs per CTA); nq_scale as above.  The autotuner
-   writes these. */
+   iteration (1, 2, 4, or 8 with threads = 512; in class 3, k = 1, or 2 and 4 with
+   threads <= 512; a bucket whose k largest pairs would not fit one CTA's shared memory runs
+   with fewer pairs per CTA); nq_scale as above.  The autotuner writes these. */
 #define MGCD_NUM_SIZE_CLASSES 4
 int mgcd_set_size_class(mgcd_context *ctx, int cls, int threads, int k, float nq_scale);
 int mgcd_get_size_class(const mgcd_context *ctx, int cls, int *threads, int *k, float *nq_scale);

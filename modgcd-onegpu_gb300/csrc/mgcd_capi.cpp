@@ -480,7 +480,6 @@ static int schedule(mgcd_context* c, Plan& P, const std::vector<PairDesc>& descs
       // fewer pairs per CTA when k of the bucket's largest pairs would not fit shared memory
       // (16 KB kept for the kernel's static shared memory)
       while (bk.k > 1 && batch_smem_bytes(bk.threads, bk.k, bk.nq_max) > c->smem_optin - 16384) bk.k /= 2;
-      if (bk.k == 4 && bk.threads > 512) bk.threads = 512;
       bk.smem = batch_smem_bytes(bk.threads, bk.k, bk.nq_max);
       int bps = 0;
       if (batch_max_blocks_per_sm(bk.threads, bk.k, bk.smem, &bps) != cudaSuccess || bps < 1) return MGCD_ERR_GRID;
@@ -858,16 +857,16 @@ int mgcd_set_nq_scale(mgcd_context* c, float scale)
   return MGCD_OK;
 }
 
-// Launch configurations that exist: CTA size 256/512/1024; k = 1, 2, 4 with <= 512 threads,
-// or 8 with 512 threads (not in the cluster class); in the cluster class k = 2 also needs
-// <= 512 threads.
+// Launch configurations that exist: CTA size 256/512/1024 with k = 1, 2, 4, or k = 8 with
+// 512 threads; in the cluster class k = 1, or k = 2, 4 with <= 512 threads.
 static bool valid_class_cfg(int cls, int threads, int k, float nq_scale)
 {
   if (cls < 0 || cls >= NSTREAMS || !(nq_scale >= 0.5f && nq_scale <= 1.0f)) return false;
   if (threads != 256 && threads != 512 && threads != 1024) return false;
   if (k == 8) return threads == 512 && cls != CLUSTER_CLASS;
-  if (k != 1 && k != 2 && !(k == 4 && threads <= 512)) return false;
-  return !(cls == CLUSTER_CLASS && k == 2 && threads > 512);
+  if (k != 1 && k != 2 && k != 4) return false;
+  if (cls == CLUSTER_CLASS) return k == 1 || threads <= 512;
+  return true;
 }
 
 int mgcd_set_size_class(mgcd_context* c, int cls, int threads, int k, float nq_scale)

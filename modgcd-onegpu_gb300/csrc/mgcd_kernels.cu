@@ -655,6 +655,7 @@ static const void* batch_fn_for(int threads, int k)
     switch (threads) {
       case 256: return reinterpret_cast<const void*>(&batchk_kernel<256, 4>);
       case 512: return reinterpret_cast<const void*>(&batchk_kernel<512, 4>);
+      case 1024: return reinterpret_cast<const void*>(&batchk_kernel<1024, 4>);   // 64 registers, 32 warps/SM
       default: return nullptr;
     }
   }

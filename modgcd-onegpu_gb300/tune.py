@@ -5,8 +5,8 @@ mgcd_load_tuning reads.
 
 Size classes (by the reference's moduli count of the pair): 0 = <= 1,024 moduli, 1 =
 <= 4,096, 2 = <= 16,384 (one CTA per pair), 3 = larger (one thread-block cluster per pair).
-Candidates: CTA size 256/512/1024, pairs per CTA in lockstep k = 1/2/4/8 (k = 4 needs
-<= 512 threads, k = 8 exactly 512), fraction of the reference moduli count 1.0 ... 0.7
+Candidates: CTA size 256/512/1024, pairs per CTA in lockstep k = 1/2/4/8 (k = 8 needs
+512 threads), fraction of the reference moduli count 1.0 ... 0.7
 (results stay exact: uncertified pairs are rerun, and the rerun is part of the timed run);
 for class 3 the CTA size, the pairs per cluster (1/2/4) and the cluster size (4/8/16
 CTAs).  The classes of a batch run concurrently and share the SMs, so classes 0-2 are
@@ -85,8 +85,8 @@ def main():
             continue
         if c < 3:   # whole batch, other classes at their current setting
             packed, exp = full, full_exp
-            cands = [(t, k, s, 0) for t in (256, 512, 1024) for k in (1, 2, 4) if not (k == 4 and t > 512)
-                     for s in SCALES] + [(512, 8, s, 0) for s in SCALES]
+            cands = [(t, k, s, 0) for t in (256, 512, 1024) for k in (1, 2, 4) for s in SCALES] + \
+                    [(512, 8, s, 0) for s in SCALES]
         else:
             packed, exp = mg.pack_pairs(cu, cv), [math.gcd(u, v) for u, v in zip(cu, cv)]
             cands = [(t, 1, 1.0, cs) for t in (512, 1024) for cs in (4, 8, 16)] + \

@@ -127,7 +127,7 @@ def test_tuning_table_roundtrip_and_bad_tables(mgcd, tmp_path):
         assert (t, k) == (256, 2) and abs(s - 0.9) < 1e-6
         assert dev.get_cluster_size() == 4
         before = [dev.get_size_class(c) for c in range(4)]
-        for bad in ("1 256 2 0.9 0\n2 1024 4 1.0 0\n",      # k = 4 needs <= 512 threads
+        for bad in ("1 256 2 0.9 0\n2 1024 8 1.0 0\n",      # k = 8 needs 512 threads
                     "3 1024 1 1.0 0\n",                       # class 3 needs a cluster size
                     "0 256 4 0.4 0\n",                        # scale below 0.5
                     "0 256 4\n"):                             # short line
@@ -162,18 +162,18 @@ def test_cluster_class_k_pairs_per_cluster(mgcd, threads, k, ctas, scale):
         assert dev.gcd_batch(us, vs) == [math.gcd(a, b) for a, b in zip(us, vs)]
 
 
-@pytest.mark.parametrize("k", [4, 8])
-def test_pairs_per_cta_step_down_when_shared_memory_is_short(mgcd, k):
+@pytest.mark.parametrize("threads,k", [(512, 4), (512, 8), (1024, 4)])
+def test_pairs_per_cta_step_down_when_shared_memory_is_short(mgcd, threads, k):
     """A size-class-2 pair near 16,384 moduli with k pairs per CTA would need more than one
     CTA's shared memory; the bucket runs with fewer pairs per CTA instead of failing."""
-    rng = random.Random(60 + k)
+    rng = random.Random(60 + k + threads)
     us, vs = _skewed(rng, 0, 0, 30)
-    for nb in (175000, 150000, 60000):
+    for nb in (175000, 150000, 60000, 20000, 9000):
         a, b = _pair(rng, nb, rng.randint(1, nb // 3))
         us.append(a)
         vs.append(b)
     with mgcd.Device(0, 32) as dev:
-        for cls in (1, 2):
-            dev.set_size_class(cls, 512, k, 1.0)
+        for cls in (0, 1, 2):
+            dev.set_size_class(cls, threads, k, 1.0)
         assert mgcd.moduli_needed(175000) > 15000
         assert dev.gcd_batch(us, vs) == [math.gcd(a, b) for a, b in zip(us, vs)]

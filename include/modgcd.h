@@ -151,9 +151,9 @@ int mgcd_test_force_moduli(mgcd_context *ctx, unsigned nq);
    <= 1,024 moduli, 1 = <= 4,096, 2 = <= 16,384 (one CTA per pair), 3 = larger (one
    thread-block cluster per k pairs).  threads: CTA size (256, 512, 1024); k: pairs one CTA
    (class 3: one cluster) runs in lockstep, sharing one modular inverse per modulus and
-   iteration (1, 2, 4, or 8 with threads = 512; in class 3, k = 1, or 2 and 4 with
-   threads <= 512; a bucket whose k largest pairs would not fit one CTA's shared memory runs
-   with fewer pairs per CTA); nq_scale as above.  The autotuner writes these. */
+   iteration (1, 2, 4, or 8 with threads = 512 outside class 3; a bucket whose k largest
+   pairs would not fit one CTA's shared memory runs with fewer pairs per CTA); nq_scale as
+   above.  The autotuner writes these. */
 #define MGCD_NUM_SIZE_CLASSES 4
 int mgcd_set_size_class(mgcd_context *ctx, int cls, int threads, int k, float nq_scale);
 int mgcd_get_size_class(const mgcd_context *ctx, int cls, int *threads, int *k, float *nq_scale);
@@ -161,6 +161,11 @@ int mgcd_get_size_class(const mgcd_context *ctx, int cls, int *threads, int *k, 
    when a pair's share of moduli would not fit one CTA's shared memory). */
 int mgcd_set_cluster_size(mgcd_context *ctx, int ctas);
 int mgcd_get_cluster_size(const mgcd_context *ctx, int *ctas);
+/* The same for any size class: classes 0-2 run one pair (k pairs) per CTA by default
+   (ctas = 0); with ctas in 2..16 their pairs are spread over clusters of that many CTAs,
+   which shortens the longest pairs of a batch (k <= 4 then). */
+int mgcd_set_class_cluster(mgcd_context *ctx, int cls, int ctas);
+int mgcd_get_class_cluster(const mgcd_context *ctx, int cls, int *ctas);
 /* Tuning table (the autotuner's output, modgcd-onegpu_gb300/tune.py): a text file with one
    line per size class, "class threads k nq_scale cluster_ctas" (cluster_ctas 0 except for
    class 3), '#' comments.  Load checks every line before applying any (MGCD_ERR_INVALID_ARG

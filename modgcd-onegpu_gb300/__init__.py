@@ -75,6 +75,8 @@ SIGNATURES = {
     "mgcd_set_cluster_size": (_c.c_int, [_P, _c.c_int]),
     "mgcd_get_cluster_size": (_c.c_int, [_P, _c.POINTER(_c.c_int)]),
     "mgcd_batch_use_graph": (_c.c_int, [_P, _c.c_int]),
+    "mgcd_set_class_cluster": (_c.c_int, [_P, _c.c_int, _c.c_int]),
+    "mgcd_get_class_cluster": (_c.c_int, [_P, _c.c_int, _c.POINTER(_c.c_int)]),
     "mgcd_certify_inverse": (_c.c_int, [_P, _c.POINTER(_c.c_uint64), _c.POINTER(_c.c_uint64),
                                         _c.POINTER(_c.c_uint32), _c.POINTER(_c.c_uint32)]),
     "mgcd_load_tuning": (_c.c_int, [_P, _c.c_char_p]),
@@ -339,6 +341,15 @@ class Device:
 
     def save_tuning(self, path):
         _check(self._lib.mgcd_save_tuning(self._h, os.fsencode(path)))
+
+    def set_class_cluster(self, cls, ctas):
+        """CTAs per cluster for size class cls (0: one CTA per pair, classes 0-2 only)."""
+        _check(self._lib.mgcd_set_class_cluster(self._h, int(cls), int(ctas)))
+
+    def get_class_cluster(self, cls):
+        n = ctypes.c_int()
+        _check(self._lib.mgcd_get_class_cluster(self._h, int(cls), ctypes.byref(n)))
+        return n.value
 
     def batch_use_graph(self, enable=True):
         """Record each upload's GPU work into a CUDA graph and replay it on every run."""

@@ -458,14 +458,12 @@ static int schedule(mgcd_context* c, Plan& P, const std::vector<PairDesc>& descs
     bk.n = (uint32_t)v.size();
     bk.nq_max = descs[v[0]].nq;
     bk.scratch_off = scratch;
-    if (b == CLUSTER_CLASS) {
+    if (!plain && (b == CLUSTER_CLASS || c->cfg[b].csize > 0)) {
       // k pairs per cluster; more CTAs per cluster when a CTA's share of the moduli would
       // not fit its shared memory (16 KB kept for the kernel's static shared memory)
-      if (P.cluster_k) {
-        bk.k = P.cluster_k;
-        if (bk.k > 1 && bk.threads > 512) bk.threads = 512;
-      }
-      int cs = P.cluster_ctas ? P.cluster_ctas : c->cfg[b].csize;
+      if (b == CLUSTER_CLASS && P.cluster_k) bk.k = P.cluster_k;
+      if (bk.k > 4) bk.k = 4;
+      int cs = (b == CLUSTER_CLASS && P.cluster_ctas) ? P.cluster_ctas : c->cfg[b].csize;
       const size_t room = c->smem_optin - 16384;
       while (cs < MAX_CLUSTER && cluster_batch_smem_bytes(cs, bk.nq_max, bk.k) > room) cs *= 2;
       cs = std::min(cs, MAX_CLUSTER);
@@ -858,15 +856,13 @@ int mgcd_set_nq_scale(mgcd_context* c, float scale)
 }
 
 // Launch configurations that exist: CTA size 256/512/1024 with k = 1, 2, 4, or k = 8 with
-// 512 threads; in the cluster class k = 1, or k = 2, 4 with <= 512 threads.
+// 512 threads (not in the cluster class).
 static bool valid_class_cfg(int cls, int threads, int k, float nq_scale)
 {
   if (cls < 0 || cls >= NSTREAMS || !(nq_scale >= 0.5f && nq_scale <= 1.0f)) return false;
   if (threads != 256 && threads != 512 && threads != 1024) return false;
   if (k == 8) return threads == 512 && cls != CLUSTER_CLASS;
-  if (k != 1 && k != 2 && k != 4) return false;
-  if (cls == CLUSTER_CLASS) return k == 1 || threads <= 512;
-  return true;
+  return k == 1 || k == 2 || k == 4;
 }
 
 int mgcd_set_size_class(mgcd_context* c, int cls, int threads, int k, float nq_scale)
@@ -892,6 +888,22 @@ int mgcd_get_cluster_size(const mgcd_context* c, int* ctas)
   return MGCD_OK;
 }
 
+int mgcd_set_class_cluster(mgcd_context* c, int cls, int ctas)
+{
+  if (!c || cls < 0 || cls >= NSTREAMS || ctas > MAX_CLUSTER || ctas < 0 || ctas == 1 ||
+      (cls == CLUSTER_CLASS && ctas == 0))
+    return MGCD_ERR_INVALID_ARG;
+  c->cfg[cls].csize = ctas;
+  return MGCD_OK;
+}
+
+int mgcd_get_class_cluster(const mgcd_context* c, int cls, int* ctas)
+{
+  if (!c || !ctas || cls < 0 || cls >= NSTREAMS) return MGCD_ERR_INVALID_ARG;
+  *ctas = c->cfg[cls].csize;
+  return MGCD_OK;
+}
+
 // Tuning table: one line per size class, "class threads k nq_scale cluster_ctas" ('#' starts
 // a comment).  All lines are checked before any is applied.
 int mgcd_load_tuning(mgcd_context* c, const char* path)
@@ -911,7 +923,7 @@ int mgcd_load_tuning(mgcd_context* c, const char* path)
     int cls, threads, k, cs;
     float sc;
     if (std::sscanf(s, "%d %d %d %f %d", &cls, &threads, &k, &sc, &cs) != 5 || !valid_class_cfg(cls, threads, k, sc) ||
-        (cls == CLUSTER_CLASS ? (cs < 2 || cs > MAX_CLUSTER) : cs != 0)) {
+        cs < 0 || cs == 1 || cs > MAX_CLUSTER || (cls == CLUSTER_CLASS && cs == 0) || (cs > 0 && k > 4)) {
       rc = MGCD_ERR_INVALID_ARG;
       break;
     }

@@ -734,6 +734,7 @@ static const void* cluster_batch_fn_k(int threads, int k)
     switch (threads) {
       case 256: return reinterpret_cast<const void*>(&cluster_batchk_kernel<256, 2>);
       case 512: return reinterpret_cast<const void*>(&cluster_batchk_kernel<512, 2>);
+      case 1024: return reinterpret_cast<const void*>(&cluster_batchk_kernel<1024, 2>);
       default: return nullptr;
     }
   }
@@ -741,6 +742,7 @@ static const void* cluster_batch_fn_k(int threads, int k)
     switch (threads) {
       case 256: return reinterpret_cast<const void*>(&cluster_batchk_kernel<256, 4>);
       case 512: return reinterpret_cast<const void*>(&cluster_batchk_kernel<512, 4>);
+      case 1024: return reinterpret_cast<const void*>(&cluster_batchk_kernel<1024, 4>);
       default: return nullptr;
     }
   }

@@ -7,9 +7,11 @@ Size classes (by the reference's moduli count of the pair): 0 = <= 1,024 moduli,
 <= 4,096, 2 = <= 16,384 (one CTA per pair), 3 = larger (one thread-block cluster per pair).
 Candidates: CTA size 256/512/1024, pairs per CTA in lockstep k = 1/2/4/8 (k = 8 needs
 512 threads), fraction of the reference moduli count 1.0 ... 0.7
-(results stay exact: uncertified pairs are rerun, and the rerun is part of the timed run);
-for class 3 the CTA size, the pairs per cluster (1/2/4) and the cluster size (4/8/16
-CTAs).  The classes of a batch run concurrently and share the SMs, so classes 0-2 are
+(results stay exact: uncertified pairs are rerun, and the rerun is part of the timed run),
+and for classes 0-2 also clusters of 2 or 4 CTAs per k pairs (the longest pairs of a batch
+bound its time when each runs on one SM); for class 3 the CTA size, the pairs per cluster
+(1/2/4) and the cluster size (4/8/16 CTAs).  The classes of a batch run concurrently and
+share the SMs, so classes 0-2 are
 tuned by coordinate descent on the whole mixed
 1k-64k-bit batch (largest class first, the others held at their current best); class 3 is
 timed alone on 300k-bit pairs.  Every time is the median of `reps` runs and every result
@@ -86,15 +88,15 @@ def main():
         if c < 3:   # whole batch, other classes at their current setting
             packed, exp = full, full_exp
             cands = [(t, k, s, 0) for t in (256, 512, 1024) for k in (1, 2, 4) for s in SCALES] + \
-                    [(512, 8, s, 0) for s in SCALES]
+                    [(512, 8, s, 0) for s in SCALES] + \
+                    [(t, k, s, cs) for t in (512, 1024) for k in (2, 4) for s in SCALES[:3] for cs in (2, 4)]
         else:
             packed, exp = mg.pack_pairs(cu, cv), [math.gcd(u, v) for u, v in zip(cu, cv)]
             cands = [(t, 1, 1.0, cs) for t in (512, 1024) for cs in (4, 8, 16)] + \
-                    [(512, k, 1.0, cs) for k in (2, 4) for cs in (4, 8, 16)]
+                    [(t, k, 1.0, cs) for t in (512, 1024) for k in (2, 4) for cs in (4, 8, 16)]
         for t, k, s, cs in cands:
             dev.set_size_class(c, t, k, s)
-            if cs:
-                dev.set_cluster_size(cs)
+            dev.set_class_cluster(c, cs)
             try:
                 ms = time_config(dev, packed, exp, args.reps)
             except mg.GcdError as e:       # e.g. a launch shape that does not fit
@@ -107,8 +109,7 @@ def main():
                 best[c] = (ms, t, k, s, cs)
         _, t, k, s, cs = best[c]
         dev.set_size_class(c, t, k, s)
-        if cs:
-            dev.set_cluster_size(cs)
+        dev.set_class_cluster(c, cs)
     out = args.out or os.path.join(HERE, "tuning", "gb300_L%d.txt" % args.L)
     os.makedirs(os.path.dirname(out), exist_ok=True)
     dev.save_tuning(out)

@@ -1,6 +1,7 @@
 """Batches holding pairs larger than one CTA (size class 3: one thread-block cluster per
 pair, pulled from a persistent queue) and batches replayed from a recorded CUDA graph.
 Every result is compared with Python's exact gcd; graph replays must equal direct runs."""
+import importlib
 import math
 import os
 import random
@@ -61,8 +62,9 @@ def test_cluster_size_rejects_out_of_range(mgcd):
         for bad in (0, 1, 17):
             with pytest.raises(mgcd.GcdError):
                 dev.set_cluster_size(bad)
-        with pytest.raises(mgcd.GcdError):
-            dev.set_size_class(3, 1024, 2, 1.0)
+        for bad in ((3, 1024, 8, 1.0), (0, 768, 1, 1.0), (1, 256, 3, 1.0), (2, 512, 2, 0.4)):
+            with pytest.raises(mgcd.GcdError):
+                dev.set_size_class(*bad)
 
 
 def test_graph_replay_matches_direct(mgcd):
@@ -177,3 +179,23 @@ def test_pairs_per_cta_step_down_when_shared_memory_is_short(mgcd, threads, k):
             dev.set_size_class(cls, threads, k, 1.0)
         assert mgcd.moduli_needed(175000) > 15000
         assert dev.gcd_batch(us, vs) == [math.gcd(a, b) for a, b in zip(us, vs)]
+
+
+@pytest.mark.parametrize("cls_cfg", [{2: (1024, 4, 0.8, 4), 1: (1024, 4, 0.9, 2)}, {0: (512, 2, 1.0, 2), 2: (512, 4, 1.0, 8)}])
+def test_size_classes_on_clusters(mgcd, cls_cfg):
+    """Pairs of classes 0-2 spread over clusters of CTAs (k pairs per cluster)."""
+    rng = random.Random(70 + len(cls_cfg))
+    us, vs, _ = importlib.import_module("modgcd-onegpu_gb300.workloads").mixed_batch(300, seed=71)
+    exp = [math.gcd(a, b) for a, b in zip(us, vs)]
+    with mgcd.Device(0, 32) as dev:
+        for c, (t, k, s, cs) in cls_cfg.items():
+            dev.set_size_class(c, t, k, s)
+            dev.set_class_cluster(c, cs)
+            assert dev.get_class_cluster(c) == cs
+        assert dev.gcd_batch(us, vs) == exp
+        dev.batch_use_graph(True)
+        dev.batch_upload(*mgcd.pack_pairs(us, vs))
+        for _ in range(2):
+            dev.batch_run()
+            dev.batch_sync()
+            assert _results(mgcd, dev) == exp

@@ -548,7 +548,8 @@ static int launch_set(mgcd_context* c, Plan& P, const std::vector<Bucket>& bucke
     g.status = P.d_status.as<int32_t>() + k;
     const bool ref_shape = c->single_policy == MGCD_SINGLE_REFERENCE_SHAPE;
     if (!ref_shape && d.nq <= (uint32_t)MAX_CLUSTER * 1024) {
-      // thread-block cluster: as many CTAs (<= 16) as keep one modulus per thread
+      // thread-block cluster: as many CTAs (<= 16) as keep one modulus per thread (two per
+      // thread measured 1.7x slower at 23,552 moduli than the grid)
       const int ctas = (int)std::min<uint32_t>(MAX_CLUSTER, (d.nq + 255) / 256);
       const uint32_t per = (d.nq + ctas - 1) / ctas;
       const int threads = per <= 256 ? 256 : per <= 512 ? 512 : 1024;

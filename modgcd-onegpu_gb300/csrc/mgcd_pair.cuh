@@ -90,6 +90,13 @@ static __device__ __forceinline__ unsigned long long globaltimer_ns()
   return t;
 }
 
+// Arrival that publishes this thread's earlier writes (the atomic min, CTA 0's slot reset)
+// to any thread that acquires the counter: one fire-and-forget reduction, no fence.
+static __device__ __forceinline__ void red_release_add_u32(unsigned int* p, unsigned int v)
+{
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
+
 static __device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p)
 {
   unsigned int v;
@@ -150,7 +157,24 @@ __device__ __forceinline__ bool reduce_min(uint32_t& hi, uint32_t& lo, RedSmem& 
                                            GridSync* gs, uint32_t& epoch)
 {
   if constexpr (MODE == SYNC_CLUSTER) {
-    cluster_min_key<T>(hi, lo, *reinterpret_cast<ClusterSmem*>(gs), parity);
+    ClusterSmem& cs = *reinterpret_cast<ClusterSmem*>(gs);
+    const uint32_t nc = cluster_size();
+    if (nc * (T / 32) <= 64) {
+      cluster_min_key<T>(hi, lo, cs, parity);
+      return true;
+    }
+    // Large clusters: the CTA's minimum first (one __syncthreads), then one key per CTA
+    // into every CTA (slot [me][0] of the buffer chosen by the exchange count), one cluster
+    // barrier, and a 16-entry reduction instead of one over every warp of the cluster.
+    block_min_key<T>(hi, lo, rs, parity);
+    const uint32_t cb = epoch & 1u, lane = threadIdx.x & 31u, me = cluster_rank();
+    if (threadIdx.x < 32u && lane < nc) st_cluster_u64(&cs.key[cb][me][0], lane, ((unsigned long long)hi << 32) | lo);
+    cluster_sync_all();
+    const unsigned long long k = lane < nc ? cs.key[cb][lane][0] : ~0ull;
+    hi = (uint32_t)(k >> 32);
+    lo = (uint32_t)k;
+    warp_min_key(hi, lo);
+    epoch += 1u;
     return true;
   }
   block_min_key<T>(hi, lo, rs, parity);
@@ -163,8 +187,7 @@ __device__ __forceinline__ bool reduce_min(uint32_t& hi, uint32_t& lo, RedSmem& 
       if (blockIdx.x != gs->withhold_cta) {
         atomicMin(&gs->slot[s], ((unsigned long long)hi << 32) | lo);
         if (blockIdx.x == 0) gs->slot[(epoch + 1u) % 3u] = ~0ull;
-        __threadfence();
-        atomicAdd(&gs->arrive, 1u);
+        red_release_add_u32(&gs->arrive, 1u);
       }
       const unsigned int target = (epoch + 1u) * gridDim.x;
       const unsigned long long t0 = globaltimer_ns();

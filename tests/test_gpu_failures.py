@@ -23,7 +23,7 @@ def _pair(rng, nbits, gbits):
 
 def test_grid_wait_runs_out_and_context_survives(mgcd):
     rng = random.Random(31)
-    u, v = _pair(rng, 250000, 60000)          # > 16,384 moduli: cooperative grid
+    u, v = _pair(rng, 420000, 60000)          # > 16,384 moduli: cooperative grid
     with mgcd.Device(0, 32) as dev:
         dev.set_wait_timeout_ms(200)
         dev.test_withhold_cta(1)

@@ -128,12 +128,14 @@ def test_other_modulus_widths(mgcd, oracle, L):
         assert dev.gcd_batch(us, vs) == [math.gcd(a, b) for a, b in zip(us, vs)]
 
 
-def test_large_pairs_cooperative_grid(device):
-    """Pairs too large for one CTA run on the cooperative grid (plain path above 2,048
-    moduli, batch path above 16,384)."""
+def test_large_pairs_clusters_and_grid(device):
+    """Pairs too large for one CTA: single pairs on a cluster (up to 16,384 moduli) or the
+    cooperative grid; in a batch, on clusters from the size-class-3 queue."""
     rng = random.Random(16)
     u, v = rand_pair(rng, 65536, 16384)
-    assert device.gcd(u, v) == math.gcd(u, v)                       # plain, grid mode
+    assert device.gcd(u, v) == math.gcd(u, v)                       # plain, cluster
+    u3, v3 = rand_pair(rng, 420000, 100000)
+    assert device.gcd(u3, v3) == math.gcd(u3, v3)                   # plain, grid
     u2, v2 = rand_pair(rng, 262144, 65536)
     assert device.gcd_batch([u2, u], [v2, v]) == [math.gcd(u2, v2), math.gcd(u, v)]
 
@@ -154,11 +156,13 @@ def test_single_pair_launch_shapes_agree(mgcd, oracle):
             assert dev.gcd_digits(u, v) == dig
             dev.set_single_pair_policy(1)
             assert dev.gcd_digits(u, v) == dig
-        u, v = rand_pair(rng, 300000, 80000)                  # > 16 x 1024 moduli: grid
-        g = math.gcd(u, v)
-        for pol in (0, 1):
-            dev.set_single_pair_policy(pol)
-            assert dev.gcd(u, v) == g
+        # 26,880 and 34,816 moduli: the cooperative grid
+        for nbits in (300000, 400000):
+            u, v = rand_pair(rng, nbits, 80000)
+            g = math.gcd(u, v)
+            for pol in (0, 1):
+                dev.set_single_pair_policy(pol)
+                assert dev.gcd(u, v) == g
 
 
 def test_not_enough_moduli(mgcd):

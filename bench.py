@@ -421,15 +421,18 @@ def run_sweep(args, rank, local):
             if ok is None:
                 continue
             # the same pair in the reference's launch shape (256-thread CTAs, grid-wide exchange)
-            dev.set_single_pair_policy(1)
-            ref_ms = []
-            for _ in range(max(1, args.reps - 1)):
-                ok = ok and dev.gcd(u, v) == expect
-                ref_ms.append(dev.batch_elapsed_ms()[0])
+            pol_ms = {}
+            for pol in (1, 2):   # the reference's launch shape; the grid of 8-CTA clusters
+                dev.set_single_pair_policy(pol)
+                pol_ms[pol] = []
+                for _ in range(max(1, args.reps - 1)):
+                    ok = ok and dev.gcd(u, v) == expect
+                    pol_ms[pol].append(dev.batch_elapsed_ms()[0])
             dev.set_single_pair_policy(0)
             rows.append({"L": L, "bits": n, "moduli": mg.moduli_needed(n, L), "device_ms": statistics.median(dev_ms),
                          "wall_ms": statistics.median(wall), "p99_wall_ms": max(wall),
-                         "reference_shape_ms": statistics.median(ref_ms), "gmp_ms": 1e3 * min(gsec),
+                         "reference_shape_ms": statistics.median(pol_ms[1]),
+                         "cluster_grid_ms": statistics.median(pol_ms[2]), "gmp_ms": 1e3 * min(gsec),
                          "bit_exact": bool(ok)})
             print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
         dev.close()

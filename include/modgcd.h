@@ -135,6 +135,12 @@ int mgcd_set_nq_scale(mgcd_context *ctx, float scale);
                                    exchange per iteration (GmpCudaDevice-gcd.cu:80-96). */
 #define MGCD_SINGLE_AUTO            0
 #define MGCD_SINGLE_REFERENCE_SHAPE 1
+/*   MGCD_SINGLE_CLUSTER_GRID      above 16 x 1024 moduli: a cooperative grid of 8-CTA
+                                   clusters; keys meet in each cluster through DSMEM and one
+                                   leader per cluster joins the global exchange (fewer global
+                                   atomics, two more barriers per iteration: measured 20 %
+                                   slower than the default on GB300). */
+#define MGCD_SINGLE_CLUSTER_GRID    2
 int mgcd_set_single_pair_policy(mgcd_context *ctx, int policy);
 /* Bound of every wait a cooperative-grid pair makes on the other CTAs (default 2,000 ms).
    When it runs out, every CTA returns and the pair fails with MGCD_ERR_TIMEOUT; the

@@ -7,9 +7,11 @@ Mirrors the reference's host object GmpCuda::GmpCudaDevice (GmpCuda.h:87-119):
     dev.gcd(u, v)                 GmpCudaDevice::gcd           (GmpCudaDevice-gcd.cu:57-132)
     dev.max_grid_size             getMaxGridSize               (GmpCuda.h:118)
 
-plus batches (``gcd_batch`` and the upload/run/download steps).  Errors raise
-``GcdError`` with the reference's messages.  Every computation runs on the GPU through
-libmodgcd.so; there is no CPU path, and importing fails loudly if the library is missing.
+plus batches (``gcd_batch`` and the upload/run/download steps, CUDA-graph replay, the
+tuning table), the request server (``Server``: continuous batching under an HBM admission
+budget) and the exhaustive inverse certification.  Errors raise ``GcdError`` with the
+reference's messages.  Every computation runs on the GPU through libmodgcd.so; there is
+no CPU path, and loading fails loudly if the library is missing.
 """
 import ctypes
 import os

@@ -559,8 +559,34 @@ static int launch_set(mgcd_context* c, Plan& P, const std::vector<Bucket>& bucke
       ++P.launches;
       continue;
     }
-    // cooperative grid: one CTA per SM (or the reference's shape: 256-thread CTAs, 256 moduli)
-    uint32_t per = ref_shape ? 256u : std::max<uint32_t>(32, (d.nq + c->sms - 1) / c->sms);
+    if (c->single_policy == MGCD_SINGLE_CLUSTER_GRID) {
+      // cooperative grid of 8-CTA clusters, at most one CTA per SM
+      constexpr int CS = 8;
+      int nclu = c->sms / CS;
+      uint32_t per = std::max<uint32_t>(32, (d.nq + nclu * CS - 1) / (nclu * CS));
+      const int threads = per <= 256 ? 256 : per <= 512 ? 512 : 1024;
+      int maxc = 0;
+      if (cgrid_max_clusters(threads, CS, grid_smem_bytes(per), &maxc) != cudaSuccess || maxc < 1) return MGCD_ERR_GRID;
+      if (maxc < nclu) {
+        nclu = maxc;
+        per = (d.nq + nclu * CS - 1) / (nclu * CS);
+        if (per > 1024 * 4) return MGCD_ERR_GRID;
+      }
+      nclu = (int)((d.nq + per * CS - 1) / (per * CS));
+      g.per_cta = per;
+      g.sync = P.d_gsync.as<GridSync>();
+      CK(launch_gridsync_init(g.sync, c->wait_timeout_ns, c->withhold_cta, P.stream));
+      ++P.launches;
+      const int thr = per <= 256 ? 256 : per <= 512 ? 512 : 1024;
+      cudaError_t e = launch_cgrid(g, thr, CS, nclu, grid_smem_bytes(per), P.stream);
+      if (e == cudaErrorCooperativeLaunchTooLarge) return MGCD_ERR_GRID;
+      if (e != cudaSuccess) return MGCD_ERR_CUDA;
+      ++P.launches;
+      continue;
+    }
+    // cooperative grid: at most one CTA per SM and at least 256 moduli per CTA (fewer CTAs in
+    // each exchange); or the reference's shape: 256-thread CTAs, 256 moduli
+    uint32_t per = ref_shape ? 256u : std::max<uint32_t>(256, (d.nq + c->sms - 1) / c->sms);
     const int threads = (ref_shape || per <= 256) ? 256 : per <= 512 ? 512 : GRID_THREADS;
     int bps = 0;
     if (grid_max_blocks_per_sm(threads, grid_smem_bytes(per), &bps) != cudaSuccess || bps < 1) return MGCD_ERR_GRID;
@@ -963,7 +989,9 @@ int mgcd_batch_use_graph(mgcd_context* c, int enable)
 
 int mgcd_set_single_pair_policy(mgcd_context* c, int policy)
 {
-  if (!c || (policy != MGCD_SINGLE_AUTO && policy != MGCD_SINGLE_REFERENCE_SHAPE)) return MGCD_ERR_INVALID_ARG;
+  if (!c || (policy != MGCD_SINGLE_AUTO && policy != MGCD_SINGLE_REFERENCE_SHAPE &&
+             policy != MGCD_SINGLE_CLUSTER_GRID))
+    return MGCD_ERR_INVALID_ARG;
   c->single_policy = policy;
   return MGCD_OK;
 }

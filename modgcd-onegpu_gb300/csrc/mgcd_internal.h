@@ -114,6 +114,11 @@ cudaError_t cluster_batch_max_clusters(int threads, int k, int csize, size_t sme
 cudaError_t launch_cluster_batch(const BatchArgs& a, int threads, int k, int csize, int clusters, size_t smem,
                                  cudaStream_t s);
 
+// One pair on a cooperative grid of `clusters` clusters of `csize` CTAs (hierarchical
+// exchange; a.sync is the global state, a.per_cta the moduli per CTA).
+cudaError_t cgrid_max_clusters(int threads, int csize, size_t smem, int* clusters);
+cudaError_t launch_cgrid(const GridArgs& a, int threads, int csize, int clusters, size_t smem, cudaStream_t s);
+
 // Resets the grid exchange state on the device (capturable in a CUDA graph).
 cudaError_t launch_gridsync_init(GridSync* gs, unsigned long long timeout_ns, uint32_t withhold, cudaStream_t s);
 

@@ -526,6 +526,33 @@ __global__ void __launch_bounds__(T) cluster_kernel(const GridArgs a)
   cluster_sync_all();   // no CTA leaves while others may still address its shared memory
 }
 
+// One pair over a cooperative grid of thread-block clusters: CTA b owns moduli
+// [b * per_cta, ...); pivot keys meet inside each cluster through DSMEM and only one
+// leader per cluster joins the global exchange (fewer atomics on one address than one per
+// CTA).
+template <int T>
+__global__ void __launch_bounds__(T) cgrid_kernel(const GridArgs a)
+{
+  extern __shared__ __align__(16) uint32_t smem[];
+  __shared__ RedSmem rs;
+  __shared__ CGridSmem cg;
+  const uint32_t nq = a.pair.nq;
+  const uint32_t j0 = blockIdx.x * a.per_cta;
+  const uint32_t nloc = j0 >= nq ? 0u : (nq - j0 < a.per_cta ? nq - j0 : a.per_cta);
+  uint32_t* st = smem;
+  uint32_t* acc2 = smem + a.per_cta;
+  uint32_t* chunk = acc2 + a.per_cta;
+  uint32_t* u0 = a.scratch + j0;
+  uint32_t* v0 = a.scratch + nq + j0;
+  int2* hist = reinterpret_cast<int2*>(a.scratch + 2 * (size_t)nq);
+  if (threadIdx.x == 0) cg.g = a.sync;
+  __syncthreads();
+  cluster_sync_all();   // every CTA of the cluster is running before remote stores begin
+  run_pair<T, SYNC_CGRID>(a.limbs, a.pair, a.mods, a.L, j0, nloc, st, acc2, chunk, rs, u0, v0, hist,
+                          reinterpret_cast<GridSync*>(&cg), a.digits, a.count, a.iters, a.status, a.inv);
+  cluster_sync_all();   // no CTA leaves while others may still address its shared memory
+}
+
 // Persistent batched kernel for pairs too large for one CTA: each thread-block cluster of
 // C CTAs takes the next pair of the queue and computes it with the cluster path above
 // (pair moduli split into C contiguous ranges).  The queue is popped by CTA 0 of the
@@ -785,6 +812,40 @@ cudaError_t launch_cluster_batch(const BatchArgs& a, int threads, int k, int csi
   cudaLaunchAttribute attr[1];
   const cudaLaunchConfig_t cfg = cluster_config(clusters * csize, threads, csize, smem, s, attr);
   void* args[] = {const_cast<BatchArgs*>(&a)};
+  return cudaLaunchKernelExC(&cfg, fn, args);
+}
+
+static const void* cgrid_fn(int threads)
+{
+  switch (threads) {
+    case 256: return reinterpret_cast<const void*>(&cgrid_kernel<256>);
+    case 512: return reinterpret_cast<const void*>(&cgrid_kernel<512>);
+    case 1024: return reinterpret_cast<const void*>(&cgrid_kernel<1024>);
+    default: return nullptr;
+  }
+}
+
+cudaError_t cgrid_max_clusters(int threads, int csize, size_t smem, int* clusters)
+{
+  const void* fn = cgrid_fn(threads);
+  cudaError_t e = prepare_cluster_fn(fn, csize, smem);
+  if (e != cudaSuccess) return e;
+  cudaLaunchAttribute attr[1];
+  const cudaLaunchConfig_t cfg = cluster_config(csize, threads, csize, smem, nullptr, attr);
+  return cudaOccupancyMaxActiveClusters(clusters, fn, &cfg);
+}
+
+cudaError_t launch_cgrid(const GridArgs& a, int threads, int csize, int clusters, size_t smem, cudaStream_t s)
+{
+  const void* fn = cgrid_fn(threads);
+  cudaError_t e = prepare_cluster_fn(fn, csize, smem);
+  if (e != cudaSuccess) return e;
+  cudaLaunchAttribute attr[2];
+  cudaLaunchConfig_t cfg = cluster_config(clusters * csize, threads, csize, smem, s, attr);
+  attr[1].id = cudaLaunchAttributeCooperative;   // all clusters resident at once
+  attr[1].val.cooperative = 1;
+  cfg.numAttrs = 2;
+  void* args[] = {const_cast<GridArgs*>(&a)};
   return cudaLaunchKernelExC(&cfg, fn, args);
 }
 

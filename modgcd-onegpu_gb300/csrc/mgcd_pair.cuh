@@ -16,7 +16,9 @@ constexpr int CHUNK = 1024;  // operand limbs staged per residue pass
 enum SyncMode : int {
   SYNC_CTA = 0,      // the pair lives in one CTA
   SYNC_CLUSTER = 1,  // the pair spans a thread-block cluster: DSMEM exchange + barrier.cluster
-  SYNC_GRID = 2      // the pair spans a cooperative grid: global-memory exchange, bounded wait
+  SYNC_GRID = 2,     // the pair spans a cooperative grid: global-memory exchange, bounded wait
+  SYNC_CGRID = 3     // a cooperative grid of clusters: DSMEM inside each cluster, one
+                     // leader per cluster in the global exchange
 };
 
 struct RedSmem {
@@ -30,6 +32,14 @@ struct RedSmem {
 // barrier per reduction suffices.  Double-buffered by parity.
 struct ClusterSmem {
   unsigned long long key[2][MAX_CLUSTER][32];
+};
+
+// Cluster-grid mode: the global exchange state and, per CTA, the cluster's slots.
+struct CGridSmem {
+  GridSync* g;                                  // global exchange (one arrival per cluster)
+  unsigned long long key[2][MAX_CLUSTER];       // each CTA's minimum, double-buffered
+  unsigned long long res[2];                    // the grid-wide minimum, from the leader
+  uint32_t bad[2];                              // the leader's wait expired
 };
 
 __device__ __forceinline__ uint32_t cluster_rank()
@@ -125,7 +135,7 @@ __device__ __forceinline__ bool lead_cta()
 {
   if constexpr (MODE == SYNC_CTA) return true;
   else if constexpr (MODE == SYNC_CLUSTER) return cluster_rank() == 0;
-  else return blockIdx.x == 0;
+  else return blockIdx.x == 0;   // the grid's first CTA (also in the cluster grid)
 }
 
 // Lexicographic (hi, lo) minimum over the CTA; every thread gets the result.
@@ -180,6 +190,57 @@ __device__ __forceinline__ bool reduce_min(uint32_t& hi, uint32_t& lo, RedSmem& 
   block_min_key<T>(hi, lo, rs, parity);
   if constexpr (MODE == SYNC_CTA) {
     return true;
+  } else if constexpr (MODE == SYNC_CGRID) {
+    // CTA minima -> every CTA of the cluster (DSMEM), one cluster barrier; the cluster's
+    // rank-0 thread 0 takes part in the global exchange (atomic min, release arrival,
+    // bounded acquire wait) and stores the result into every CTA; one more cluster barrier.
+    CGridSmem& cg = *reinterpret_cast<CGridSmem*>(gs);
+    GridSync* g = cg.g;
+    const uint32_t cb = epoch & 1u, lane = threadIdx.x & 31u, me = cluster_rank(), nc = cluster_size();
+    if (threadIdx.x < 32u && lane < nc) st_cluster_u64(&cg.key[cb][me], lane, ((unsigned long long)hi << 32) | lo);
+    cluster_sync_all();
+    if (me == 0u && threadIdx.x < 32u) {
+      unsigned long long k = lane < nc ? cg.key[cb][lane] : ~0ull;
+      hi = (uint32_t)(k >> 32);
+      lo = (uint32_t)k;
+      warp_min_key(hi, lo);
+      k = ((unsigned long long)hi << 32) | lo;
+      unsigned long long res = ~0ull;
+      uint32_t bad = 0;
+      if (lane == 0) {
+        const uint32_t cid = blockIdx.x / nc, ncl = gridDim.x / nc;
+        const uint32_t s = epoch % 3u;
+        if (cid != g->withhold_cta) {
+          atomicMin(&g->slot[s], k);
+          if (cid == 0) g->slot[(epoch + 1u) % 3u] = ~0ull;
+          red_release_add_u32(&g->arrive, 1u);
+        }
+        const unsigned int target = (epoch + 1u) * ncl;
+        const unsigned long long t0 = globaltimer_ns();
+        while (ld_acquire_u32(&g->arrive) < target) {
+          if (ld_relaxed_u32(&g->error)) { bad = 1; break; }
+          if (globaltimer_ns() - t0 > g->timeout_ns) { atomicExch(&g->error, 1u); bad = 1; break; }
+        }
+        res = bad ? ~0ull : ld_relaxed_u64(&g->slot[s]);
+      }
+      __syncwarp();
+      res = __shfl_sync(0xFFFFFFFFu, res, 0);
+      bad = __shfl_sync(0xFFFFFFFFu, bad, 0);
+      if (lane < nc) {
+        st_cluster_u64(&cg.res[cb], lane, res);
+        const uint32_t ad = (uint32_t)__cvta_generic_to_shared(&cg.bad[cb]);
+        uint32_t ra;
+        asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(ad), "r"(lane));
+        asm volatile("st.shared::cluster.u32 [%0], %1;" :: "r"(ra), "r"(bad) : "memory");
+      }
+    }
+    cluster_sync_all();
+    const unsigned long long k = cg.res[cb];
+    const bool ok = cg.bad[cb] == 0u;
+    hi = (uint32_t)(k >> 32);
+    lo = (uint32_t)k;
+    epoch += 1u;
+    return ok;
   } else {
     if (threadIdx.x == 0) {
       const uint32_t s = epoch % 3u;

@@ -21,10 +21,14 @@ def _pair(rng, nbits, gbits):
     return g * (rng.getrandbits(nbits - gbits) | 1), g * (rng.getrandbits(nbits - gbits) | 1)
 
 
-def test_grid_wait_runs_out_and_context_survives(mgcd):
+@pytest.mark.parametrize("policy", [0, 2])
+def test_grid_wait_runs_out_and_context_survives(mgcd, policy):
+    """policy 0: CTA 1 of the cooperative grid withholds; policy 2: cluster 1 of the grid
+    of clusters does."""
     rng = random.Random(31)
     u, v = _pair(rng, 420000, 60000)          # > 16,384 moduli: cooperative grid
     with mgcd.Device(0, 32) as dev:
+        dev.set_single_pair_policy(policy)
         dev.set_wait_timeout_ms(200)
         dev.test_withhold_cta(1)
         with pytest.raises(mgcd.GcdError) as e:

@@ -156,13 +156,20 @@ def test_single_pair_launch_shapes_agree(mgcd, oracle):
             assert dev.gcd_digits(u, v) == dig
             dev.set_single_pair_policy(1)
             assert dev.gcd_digits(u, v) == dig
-        # 26,880 and 34,816 moduli: the cooperative grid
+        # 26,880 and 34,816 moduli: the cooperative grid, the reference's shape, the grid of
+        # 8-CTA clusters (digits compared with the oracle's at the smaller size)
         for nbits in (300000, 400000):
             u, v = rand_pair(rng, nbits, 80000)
             g = math.gcd(u, v)
-            for pol in (0, 1):
+            for pol in (0, 1, 2):
                 dev.set_single_pair_policy(pol)
                 assert dev.gcd(u, v) == g
+        uu, vv = max(u, v), min(u, v)
+        nq = oracle.num_moduli_needed(uu.bit_length(), 32)
+        st, dig, _, _ = oracle.modgcd(uu, vv, 32, oracle.gen_moduli(32, nq), nq)
+        assert st == 0
+        dev.set_single_pair_policy(2)
+        assert dev.gcd_digits(u, v) == dig
 
 
 def test_not_enough_moduli(mgcd):

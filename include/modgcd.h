@@ -41,7 +41,8 @@ extern "C" {
 #define MGCD_ERR_RECOVERY          7   /* "Ran out of moduli in the recovery loop." */
 #define MGCD_ERR_KERNEL            8   /* "Unknown error in the gcd kernel." */
 #define MGCD_ERR_TIMEOUT           9   /* a bounded device-side wait expired */
-#define MGCD_ERR_CAPACITY         10   /* caller's output buffer is too small */
+#define MGCD_ERR_CAPACITY         10   /* caller's output buffer is too small, or a batch needs
+                                          more than 2^32 - 1 digit slots (split it) */
 #define MGCD_ERR_BUDGET           11   /* serving: request larger than the admission budget */
 #define MGCD_ERR_BUSY             12   /* serving: queue full, retry later */
 

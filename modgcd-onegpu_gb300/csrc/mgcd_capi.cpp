@@ -377,6 +377,7 @@ int mgcd::plan_batch(mgcd_context* c, Plan& P, size_t np, const uint32_t* limbs,
       nq = std::min(ref_nq, std::max(256, ((int)std::ceil(scale * ref_nq) + 255) / 256 * 256));
     d.nq = (uint32_t)nq;
     d.out_off = out_off;
+    if ((uint64_t)out_off + (uint64_t)ref_nq + 1 > 0xFFFFFFFFull) return MGCD_ERR_CAPACITY;   // digit slots of one batch
     out_off += (uint32_t)ref_nq + 1;
     d.g_off = glimbs;                 // gcd <= the smaller operand
     d.g_cap = d.v_len;

@@ -1,15 +1,15 @@
-"""Seeded synthetic gcd workloads with the shapes of the benchmark configurations.
+"""Seeded synthetic gcd workloads with the shapes of the benchmark workloads.
 
 No public dataset is involved: the reference generates its inputs with GMP's Mersenne
 Twister (testmodgcd.cpp:219-229, u = g*a, v = g*b from mpz_urandomb); these generators draw
 uniform random limbs the same way from Python's seeded Mersenne Twister.
 
-  single_pair      config 1: g 2048-bit odd, a, b 8192-bit coprime, u = g*a, v = g*b
-  size_sweep_pair  config 2: n-bit operands with an n/4-bit planted gcd
-  mixed_batch      config 3: 4096 pairs, bits(u) log-uniform in [1k, 64k], bits(v) =
-                   bits(u)/U(1, 2); 25% coprime, 5% v | u, 70% planted gcd of U[0, 50%]
-                   of the smaller operand
-  skewed_batch     config 4: 64 pairs at 1M bits + 16384 pairs of U[512, 4096] bits
+  single_pair      one pair: g 2048-bit odd, a, b 8192-bit coprime, u = g*a, v = g*b
+  size_sweep_pair  n-bit operands with an n/4-bit planted gcd
+  mixed_batch      4096 pairs, bits(u) log-uniform in [1k, 64k], bits(v) = bits(u)/U(1, 2);
+                   25% coprime, 5% v | u, 70% planted gcd of U[0, 50%] of the smaller operand
+  skewed_batch     64 pairs at 1M bits + 16384 pairs of U[512, 4096] bits
+  serve_requests   Poisson arrivals, mixed-batch sizes plus 1% 1M-bit requests
 """
 import math
 import random

@@ -85,3 +85,33 @@ def test_context_refuses_direct_calls_while_serving(mgcd):
             mgcd.Server(dev)
         srv.close()
         assert dev.gcd(6, 4) == 2
+
+
+def test_many_threads_submit_and_take(mgcd):
+    """Submissions and takes from several host threads at once: every answer is exact and
+    belongs to its own request."""
+    import threading
+    results, errors = {}, []
+    with mgcd.Device(0, 32) as dev:
+        with mgcd.Server(dev) as srv:
+            def worker(tid):
+                try:
+                    rng = random.Random(1000 + tid)
+                    mine = []
+                    for _ in range(60):
+                        nb = rng.randint(500, 20000)
+                        g = rng.getrandbits(rng.randint(1, nb // 2)) | 1
+                        u, v = g * (rng.getrandbits(nb) | 1), g * (rng.getrandbits(nb) | 1)
+                        mine.append((srv.submit(u, v), u, v))
+                    for t, u, v in mine:
+                        results[t] = (srv.take(t, _cap(u, v))[0], math.gcd(u, v))
+                except Exception as e:   # surfaced by the assertion below
+                    errors.append(e)
+            ths = [threading.Thread(target=worker, args=(i,)) for i in range(6)]
+            for th in ths:
+                th.start()
+            for th in ths:
+                th.join()
+    assert not errors, errors
+    assert len(results) == 360
+    assert all(got == exp for got, exp in results.values())

@@ -3,6 +3,8 @@
 Outputs stay in the source tree (``lib/``); objects go to ``_build/``.  Translation units
 compile in parallel.  GMP: the runtime library libgmp.so.10 is linked directly; the
 project's declaration header stands in for <gmp.h> when the system has none.
+Extra compiler flags for experiments: MGCD_NVCC_FLAGS (CUDA units), MGCD_CXX_FLAGS (host
+units); rebuild with --force after changing them.
 """
 import os
 import shutil
@@ -73,6 +75,7 @@ def build(verbose=False, force=False):
         src = os.path.join(CSRC, f)
         obj = os.path.join(BUILD, f + ".o")
         cmd = [CXX, "-O2", "-fPIC", "-std=c++17", "-Wall", cuda_inc, "-I" + os.path.join(ROOT, "include")] + \
+            os.environ.get("MGCD_CXX_FLAGS", "").split() + \
             gmpinc + ["-c", src, "-o", obj]
         units.append((obj, [src] + hdrs, cmd))
 

@@ -461,11 +461,12 @@ static int schedule(mgcd_context* c, Plan& P, const std::vector<PairDesc>& descs
     bk.scratch_off = scratch;
     if (!plain && (b == CLUSTER_CLASS || c->cfg[b].csize > 0)) {
       // k pairs per cluster; more CTAs per cluster when a CTA's share of the moduli would
-      // not fit its shared memory (16 KB kept for the kernel's static shared memory)
+      // not fit its shared memory (24 KB kept for the kernel's static shared memory, which
+      // holds the cluster keys and the recovery panel)
       if (b == CLUSTER_CLASS && P.cluster_k) bk.k = P.cluster_k;
       if (bk.k > 4) bk.k = 4;
       int cs = (b == CLUSTER_CLASS && P.cluster_ctas) ? P.cluster_ctas : c->cfg[b].csize;
-      const size_t room = c->smem_optin - 16384;
+      const size_t room = c->smem_optin - 24576;
       while (cs < MAX_CLUSTER && cluster_batch_smem_bytes(cs, bk.nq_max, bk.k) > room) cs *= 2;
       cs = std::min(cs, MAX_CLUSTER);
       bk.csize = cs;
@@ -550,7 +551,7 @@ static int launch_set(mgcd_context* c, Plan& P, const std::vector<Bucket>& bucke
     const bool ref_shape = c->single_policy == MGCD_SINGLE_REFERENCE_SHAPE;
     if (!ref_shape && d.nq <= (uint32_t)MAX_CLUSTER * 1024) {
       // thread-block cluster: as many CTAs (<= 16) as keep one modulus per thread (two per
-      // thread measured 1.7x slower at 23,552 moduli than the grid)
+      // thread measured 1.5-1.8x slower than the grid at 18,176-31,744 moduli)
       const int ctas = (int)std::min<uint32_t>(MAX_CLUSTER, (d.nq + 255) / 256);
       const uint32_t per = (d.nq + ctas - 1) / ctas;
       const int threads = per <= 256 ? 256 : per <= 512 ? 512 : 1024;

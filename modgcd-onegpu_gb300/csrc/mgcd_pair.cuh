@@ -401,6 +401,188 @@ __device__ void run_pair(const uint32_t* __restrict__ limbs, const PairDesc& d, 
                        digits, count, status, inv);
 }
 
+// Recovery (MGCD4, GmpCudaDevice-getGcdKernel.cu:404-443) for a pair spread over several
+// CTAs, in panels of up to 32 digits instead of one cross-CTA exchange per digit.  The
+// reference takes one digit per round -- the lowest-indexed surviving modulus with a
+// nonzero value gives (p, g) and every surviving value becomes (u - g) / p -- and ends when
+// no nonzero value is left (or, with a digit just taken, when no modulus is left).
+//   1. one exchange finds the lowest remaining modulus (zero or not); its CTA holds the
+//      lowest remaining moduli of the pair;
+//   2. that CTA takes its first <= 32 remaining moduli as the panel, computes their pairwise
+//      inverses once, and one warp produces digits inside the panel by the reference's
+//      rule -- the lanes are the lowest remaining moduli overall, so the lowest nonzero lane
+//      is the lowest nonzero modulus overall -- until no lane is nonzero, 32 digits, or no
+//      modulus is left; it writes the digits and the running count before
+//   3. one exchange (its release publishes them);
+//   4. every other surviving modulus applies the panel as one composed map
+//      u <- (u - S) / P, S = sum_i g_i prod_{l<i} p_l, P = prod_l p_l (one inverse);
+//   5. a panel without digits (its lanes all zero) falls back to one reference round over
+//      all CTAs, which also detects the end (no nonzero value left).
+// Digits, their order and the end conditions are those of the per-digit loop.
+template <int T, int MODE>
+__device__ void recover_panels(const ModConst* __restrict__ mods, const PairDesc& d, uint32_t j0, uint32_t nloc,
+                               uint32_t* st, RedSmem& rs, uint32_t& parity, uint32_t& epoch, GridSync* gs,
+                               int remaining, mgcd_pair* digits, uint32_t* count, int32_t* status, InvTab inv)
+{
+  __shared__ uint32_t pidx[32];        // panel lanes: local moduli indices, ascending
+  __shared__ uint32_t pinv[32][32];    // pinv[a][b] = R / q_a mod q_b (Montgomery)
+  __shared__ mgcd_pair pdig[32];       // the panel's digits
+  __shared__ uint32_t pn;              // panel size, then the digits it produced
+  const bool writer = threadIdx.x == 0 && lead_cta<MODE>();
+  const ModConst* __restrict__ my = mods + j0;
+  const uint32_t lane = threadIdx.x & 31u;
+  mgcd_pair* const out = digits + d.out_off;
+  uint32_t ndig = 0;                   // digits emitted (the same in every CTA)
+  uint32_t scan = 0;                   // local moduli below this are retired
+  bool fail = false;                   // a bounded wait ran out
+  __syncthreads();                     // the replayed values of every thread are in st
+  for (;;) {
+    // ---- 1. the lowest remaining modulus
+    while (scan < nloc && st[scan] == U_RETIRED) ++scan;
+    uint32_t kh = scan < nloc ? j0 + scan : 0xFFFFFFFFu, kl = 0u;
+    if (!reduce_min<T, MODE>(kh, kl, rs, parity, gs, epoch)) { fail = true; break; }
+    if (kh == 0xFFFFFFFFu) break;      // no modulus left (not reached while remaining > 0)
+    const bool front = kh >= j0 && kh < j0 + nloc;
+    uint32_t np = 0;
+    // ---- 2. the front CTA's panel
+    if (front) {
+      if (threadIdx.x < 32u) {
+        uint32_t n = 0;
+        for (uint32_t base = scan; n < 32u && base < nloc; base += 32u) {
+          const uint32_t j = base + lane;
+          const bool rem = j < nloc && st[j] != U_RETIRED;
+          const uint32_t m = __ballot_sync(0xFFFFFFFFu, rem);
+          const uint32_t pos = n + __popc(m & ((1u << lane) - 1u));
+          if (rem && pos < 32u) pidx[pos] = j;
+          n += __popc(m);
+        }
+        if (lane == 0) pn = n < 32u ? n : 32u;
+      }
+      __syncthreads();
+      np = pn;
+      for (uint32_t e = threadIdx.x; e < np * np; e += T) {
+        const uint32_t a = e / np, bb = e % np;
+        uint32_t v = 0u;
+        if (a != bb) {
+          const uint32_t ja = pidx[a], jb = pidx[bb];
+          const ModConst cb = my[jb];
+          const uint32_t qa = my[ja].q;
+          v = (j0 + ja < inv.n && j0 + jb < inv.n)
+                  ? __ldg(inv.tab + (size_t)(j0 + ja) * inv.n + (j0 + jb))
+                  : inv_mod(redc((uint64_t)(qa > cb.q ? qa - cb.q : qa), cb.q, cb.qinv), cb.q, cb.qinv);
+        }
+        pinv[a][bb] = v;
+      }
+      __syncthreads();
+      if (threadIdx.x < 32u) {
+        const bool in = lane < np;
+        const uint32_t j = in ? pidx[lane] : 0u;
+        const ModConst c = my[in ? j : pidx[0]];
+        uint32_t u = in ? st[j] : 0u;
+        uint32_t live = __ballot_sync(0xFFFFFFFFu, in);
+        uint32_t nd = 0;
+        int rem = remaining;
+        while (nd < 32u && rem > 0) {
+          const uint32_t nz = __ballot_sync(0xFFFFFFFFu, ((live >> lane) & 1u) && u != 0u);
+          if (!nz) break;
+          const uint32_t src = __ffs((int)nz) - 1u;
+          const int32_t g = __shfl_sync(0xFFFFFFFFu, to_signed(u, c.q), (int)src);
+          const uint32_t p = __shfl_sync(0xFFFFFFFFu, c.q, (int)src);
+          if (lane == 0) out[ndig + nd] = mgcd_pair{p, g};
+          live &= ~(1u << src);
+          if ((live >> lane) & 1u) u = mont_mul(mod_sub(u, from_signed(g, c.q), c.q), pinv[src][lane], c.q, c.qinv);
+          ++nd;
+          --rem;
+        }
+        if (in) st[j] = ((live >> lane) & 1u) ? u : U_RETIRED;
+        if (lane == 0) {
+          pn = nd;
+          __threadfence();             // the digits before the count
+          *count = ndig + nd;          // published by the exchange below
+          __threadfence();
+        }
+      }
+      __syncthreads();
+    }
+    // ---- 3. publish the panel
+    kh = 0xFFFFFFFFu;
+    kl = 0u;
+    if (!reduce_min<T, MODE>(kh, kl, rs, parity, gs, epoch)) { fail = true; break; }
+    if (threadIdx.x == 0) pn = *reinterpret_cast<volatile uint32_t*>(count) - ndig;
+    __syncthreads();
+    const uint32_t nd = pn;
+    if (threadIdx.x < nd) {
+      const volatile uint32_t* src = reinterpret_cast<const volatile uint32_t*>(out + ndig + threadIdx.x);
+      pdig[threadIdx.x] = mgcd_pair{src[0], (int32_t)src[1]};
+    }
+    __syncthreads();
+    if (nd == 0u) {
+      // ---- 5. one reference round: the lowest nonzero modulus anywhere, or the end
+      kh = 0xFFFFFFFFu;
+      kl = 0u;
+      for (uint32_t j = threadIdx.x; j < nloc; j += T) {
+        const uint32_t u = st[j];
+        if (u != U_RETIRED && u != 0u) { kh = j0 + j; kl = (uint32_t)to_signed(u, my[j].q); break; }
+      }
+      if (!reduce_min<T, MODE>(kh, kl, rs, parity, gs, epoch)) { fail = true; break; }
+      if (kh == 0xFFFFFFFFu) {         // no nonzero value left: done
+        if (ndig == 0u) {              // u = 0: the per-digit loop emits one zero digit
+          if (writer) out[0] = mgcd_pair{mods[0].q, 0};
+          ndig = 1u;
+        }
+        break;
+      }
+      const uint32_t p = mods[kh].q;
+      const int32_t g = (int32_t)kl;
+      for (uint32_t j = threadIdx.x; j < nloc; j += T) {
+        uint32_t u = st[j];
+        if (u == U_RETIRED) continue;
+        const ModConst c = my[j];
+        if (c.q == p) { st[j] = U_RETIRED; continue; }
+        const uint32_t jj = j0 + j;
+        const uint32_t dinv = (kh < inv.n && jj < inv.n)
+                                  ? __ldg(inv.tab + (size_t)kh * inv.n + jj)
+                                  : inv_mod(redc((uint64_t)(p > c.q ? p - c.q : p), c.q, c.qinv), c.q, c.qinv);
+        st[j] = mont_mul(mod_sub(u, from_signed(g, c.q), c.q), dinv, c.q, c.qinv);
+      }
+      if (writer) out[ndig] = mgcd_pair{p, g};
+      ++ndig;
+      remaining -= 1;
+      __syncthreads();
+      if (remaining <= 0) break;
+      continue;
+    }
+    // ---- 4. the panel's digits on every other surviving modulus, as one composed map
+    const uint32_t last = front ? pidx[np - 1u] : 0u;
+    for (uint32_t j = threadIdx.x; j < nloc; j += T) {
+      const uint32_t u = st[j];
+      if (u == U_RETIRED || (front && j <= last)) continue;   // the panel lanes are done
+      const ModConst c = my[j];
+      const uint32_t q = c.q, qi = c.qinv;
+      uint32_t accP = c.r1, S = 0u;                            // Montgomery forms of P and S
+      for (uint32_t i = 0; i < nd; ++i) {
+        const mgcd_pair dg = pdig[i];
+        const uint32_t pR = mont_mul(dg.modulus > q ? dg.modulus - q : dg.modulus, c.r2, q, qi);
+        const uint32_t gR = mont_mul(from_signed(dg.value, q), c.r2, q, qi);
+        const uint32_t t = mont_mul(gR, accP, q, qi);
+        S = S + t - ((S >= q - t) ? q : 0u);
+        accP = mont_mul(accP, pR, q, qi);
+      }
+      const uint32_t uR = mont_mul(u, c.r2, q, qi);
+      st[j] = mont_mul(mod_sub(uR, S, q), inv_mod(redc((uint64_t)accP, q, qi), q, qi), q, qi);
+    }
+    ndig += nd;
+    remaining -= (int)nd;
+    __syncthreads();
+    if (remaining <= 0) break;
+  }
+  if (writer) {
+    *status = fail ? ST_TIMEOUT : (remaining <= 0 ? ST_RECOVERY : ST_OK);
+    *count = ndig;
+  }
+  __syncthreads();
+}
+
 // After the reduction loop of one pair: certification, replay and recovery (MGCD4).
 // st holds the final t states of this CTA's moduli; `remaining` the surviving count;
 // lu, lv (meaningful in thread 0) the size bounds of the final u and v.
@@ -448,6 +630,11 @@ __device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d
       V = V2;
     }
     st[j] = mont_mul(U, inv_mod(redc((uint64_t)s, q, qi), q, qi), q, qi);   // U / s
+  }
+
+  if constexpr (MODE != SYNC_CTA) {   // several CTAs: recovery in panels
+    recover_panels<T, MODE>(mods, d, j0, nloc, st, rs, parity, epoch, gs, remaining, digits, count, status, inv);
+    return;
   }
 
   // ---- MGCD4: recovery (GmpCudaDevice-getGcdKernel.cu:404-443)

@@ -2,17 +2,17 @@
 // the device it runs on (the reference certifies its quoRem<QUASI> the same way, per
 // device, certifyQuoRemQuasi.cu:25-48).
 //
-// Each Euclid step of inv_mod estimates Q = floor(r0 / r1) from a float reciprocal and
-// corrects it with one exact integer step, which is right iff the estimate is Q or Q - 1:
-//   phase A (2^22 <= r1 < r0 < 2^32): est = fma_rz(ru(r0), rcp(ru(r1)), -2^-9), Q = rz(est);
-//   phase C (2 <= r1 < r0 < 2^22):    qf = fma_rz(r0, rcp(r1), 2^23 - 1/2) - 2^23,
-//                                      rem = fma_rn(-qf, r1, r0), one correction.
+// Each Euclid step of inv_mod takes a nearest-integer quotient estimate Q from a float
+// reciprocal and the exact remainder r = r0 - Q r1; the step makes progress (|r| < r1) iff
+// Q is within 1 of r0 / r1:
+//   phase A (2^22 <= r1 < r0 < 2^32): Q = rn(rn(r0) * rcp(rn(r1)));
+//   phase C (2 <= r1 < r0 < 2^22):    Q from fma_rn(r0, rcp(r1), 1.5 * 2^23), remainder
+//                                      fma_rn(-Q, r1, r0).
+// On [k r1, (k+1) r1 - 1] the allowed quotients are k at r0 = k r1 and {k, k + 1} above.
 // For a fixed r1 both estimates are non-decreasing in r0 (every operation is monotone and
-// rcp(r1) is fixed), while the true quotient is constant (= k) on [k r1, (k+1) r1 - 1].  So
-// the estimate lies in {k - 1, k} on the whole interval iff it does at the two ends:
-// checking both ends of every interval, for every r1, covers every (r0, r1) of the phase.
-// Phase A: ~6e10 end points; phase C: ~1.3e8 (where the whole step -- quotient, exact
-// remainder, correction -- is also checked at the end points).
+// rcp(r1) is fixed), so the estimate is allowed on the whole interval iff it is at the two
+// ends: checking both ends of every interval, for every r1, covers every (r0, r1) of the
+// phase.  Phase A: ~6e10 end points; phase C: ~1.3e8 (where the remainder is also checked).
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -30,24 +30,21 @@ struct CertOut {
   uint32_t first_r0, first_r1;
 };
 
-__device__ __forceinline__ uint32_t est_a(uint32_t r0, uint32_t r1)
+// Q allowed for r0 in [k r1, (k+1) r1): k at the bottom end, k or k + 1 above it.
+__device__ __forceinline__ bool quot_ok(uint64_t r0, uint32_t r1, uint32_t k, uint32_t Q)
 {
-  const float est = __fmaf_rz(__uint2float_ru(r0), rcp_approx(__uint2float_ru(r1)), -0x1p-9f);
-  return __float2uint_rz(est);
+  return r0 == (uint64_t)k * r1 ? Q == k : (Q == k || Q == k + 1u);
 }
 
-// Phase C step as inv_mod runs it; returns false if it does not yield (Q, r0 mod r1).
+// Phase C step as inv_mod runs it: an allowed quotient and the exact signed remainder.
 __device__ __forceinline__ bool step_c_ok(uint32_t r0, uint32_t r1, uint32_t k)
 {
   const float f0 = (float)r0, f1 = (float)r1;
-  const float rc = rcp_approx(f1);
-  float qm = __fmaf_rz(f0, rc, 8388607.5f);
-  const float qf = qm - 8388608.0f;
-  if (qf < (float)(k - 1) || qf > (float)k) return false;     // estimate in {k - 1, k}
-  float rem = __fmaf_rn(-qf, f1, f0);
-  if (rem >= f1) { rem -= f1; qm += 1.0f; }
-  const uint32_t Q = __float_as_uint(qm) - 0x4B000000u;
-  return Q == k && rem == (float)(r0 - k * r1);
+  const float qm = inv_quot_c(f0, f1);
+  const uint32_t Q = __float_as_uint(qm) - INV_MAGIC_BITS;
+  if (!quot_ok(r0, r1, k, Q)) return false;
+  const float rem = __fmaf_rn(INV_MAGIC - qm, f1, f0);
+  return rem == (float)((int32_t)r0 - (int32_t)(Q * r1));
 }
 
 __device__ void fail(CertOut* o, uint32_t r0, uint32_t r1)
@@ -84,9 +81,8 @@ __global__ void __launch_bounds__(256) certify_kernel(CertOut* out)
       const uint64_t hi = min((uint64_t)(k + 1) * r1w - 1, A_TOP);
       if (lo > hi) continue;
       n += 2;
-      const uint32_t el = est_a((uint32_t)lo, r1), eh = est_a((uint32_t)hi, r1);
-      if (el + 1u < k || el > k) fail(out, (uint32_t)lo, r1);
-      if (eh + 1u < k || eh > k) fail(out, (uint32_t)hi, r1);
+      if (!quot_ok(lo, r1, k, inv_quot_a((uint32_t)lo, r1))) fail(out, (uint32_t)lo, r1);
+      if (!quot_ok(hi, r1, k, inv_quot_a((uint32_t)hi, r1))) fail(out, (uint32_t)hi, r1);
     }
   }
   atomicAdd(&out->checked, n);

@@ -82,56 +82,82 @@ static __device__ __noinline__ uint32_t inv_mod_slow(uint32_t x, uint32_t q)
   return (uint32_t)(s0 < 0 ? s0 + q : s0);
 }
 
+// Quotient estimates of inv_mod's Euclid steps (also run by the certification kernel).
+// Phase A (2^22 <= r1 < r0 < 2^32): nearest integer to r0 / r1 from a float reciprocal.
+__device__ __forceinline__ uint32_t inv_quot_a(uint32_t r0, uint32_t r1)
+{
+  return __float2uint_rn(__fmul_rn(__uint2float_rn(r0), rcp_approx(__uint2float_rn(r1))));
+}
+
+// Phase C (r1 < r0 < 2^22, both exact in float): Q = rint(f0 * rcp(f1)) read from the
+// mantissa of Q + 1.5 * 2^23; returns the float whose low mantissa bits hold Q.
+constexpr float INV_MAGIC = 12582912.0f;     // 1.5 * 2^23
+constexpr uint32_t INV_MAGIC_BITS = 0x4B400000u;
+__device__ __forceinline__ float inv_quot_c(float f0, float f1)
+{
+  return __fmaf_rn(f0, rcp_approx(f1), INV_MAGIC);
+}
+
 // x^{-1} mod q for 0 < x < q, q an odd prime < 2^32.
 //
-// Extended Euclid on (r0, r1) = (q, x) tracking the unsigned cofactor s with
-// s_k * x == (-1)^k * r1_k (mod q); at r1 = 1 the inverse is s or q - s by parity.
-// Quotients come from a float reciprocal estimate biased low so that the estimate is
-// the true quotient or one less, then one exact integer correction step:
-//   phase A (r1 >= 2^22): operands rounded up to float, quotient < 2^10, error < 2^-10;
+// Extended Euclid on (r0, r1) = (q, x) with nearest-integer quotients (remainders of
+// either sign, their magnitudes kept; about 13 steps for 32-bit operands instead of 19),
+// tracking the cofactor s_k modulo 2^32 with s_k * x == r_k (mod q):
+//   phase A (r1 >= 2^22): operands rounded to float, quotient < 2^10, estimate within
+//            2^-11 of r0/r1, so the rounded quotient is within 1 of it and |r| < r1;
 //   phase B (r0 >= 2^22 > r1): one exact integer division at the transition;
-//   phase C (r0, r1 < 2^22): operands exact in float, remainders exact by FMA, quotient
-//            read from the float's mantissa (x + 2^23 trick), no conversion instruction.
-// The bounds assume rcp.approx.ftz.f32's documented error (1 ulp).  The result is then
-// checked (x * inv == 1 mod q) and recomputed by the integer-only routine if it is wrong,
-// so no float error can reach a result.
+//   phase C (r0, r1 < 2^22): operands exact in float, quotient < 2^22 within 1/2 of
+//            r0/r1 before rounding, remainder exact by FMA (an integer below 2^22).
+// The bounds assume rcp.approx.ftz.f32's documented error (1 ulp).  At the end |s| < q,
+// so s is either the 32-bit value read as unsigned or that minus 2^32 (possible only for
+// q > 2^31); the candidate whose product with x is 1 is taken, and if neither is (never
+// observed), the integer-only routine recomputes it, so no float error can reach a result.
 __device__ __forceinline__ uint32_t inv_mod(uint32_t x, uint32_t q, uint32_t qinv)
 {
-  uint32_t r0 = q, r1 = x, s0 = 0, s1 = 1, par = 0;
+  uint32_t r0 = q, r1 = x, s0 = 0, s1 = 1;
   while (r1 >= (1u << 22)) {
-    const float f1 = __uint2float_ru(r1);
-    const float est = __fmaf_rz(__uint2float_ru(r0), rcp_approx(f1), -0x1p-9f);
-    uint32_t Q = __float2uint_rz(est);
-    uint32_t r = r0 - Q * r1;
-    if (r >= r1) { r -= r1; Q += 1; }
-    const uint32_t s = s0 + Q * s1;
-    r0 = r1; r1 = r; s0 = s1; s1 = s; par ^= 1u;
+    const uint32_t Q = inv_quot_a(r0, r1);
+    const uint64_t m = (uint64_t)Q * r1;
+    const bool neg = m > r0;
+    const uint32_t d = r0 - (uint32_t)m;        // r0 - Q r1 modulo 2^32, |r0 - Q r1| < r1
+    const uint32_t s = s0 - Q * s1;
+    r0 = r1; s0 = s1;
+    r1 = neg ? 0u - d : d;
+    s1 = neg ? 0u - s : s;
   }
   if (r1 > 1u) {
     if (r0 >= (1u << 22)) {
       const uint32_t Q = r0 / r1;
       const uint32_t r = r0 - Q * r1;
-      const uint32_t s = s0 + Q * s1;
-      r0 = r1; r1 = r; s0 = s1; s1 = s; par ^= 1u;
+      const uint32_t s = s0 - Q * s1;
+      r0 = r1; r1 = r; s0 = s1; s1 = s;
     }
     float f0 = (float)r0, f1 = (float)r1;
     int guard = 64;
     while (f1 > 1.0f && --guard) {
-      const float rc = rcp_approx(f1);
-      float qm = __fmaf_rz(f0, rc, 8388607.5f);     // 2^23 + floor(f0*rc - 1/2)
-      const float qf = qm - 8388608.0f;
-      float rem = __fmaf_rn(-qf, f1, f0);          // exact: an integer below 2^24
-      if (rem >= f1) { rem -= f1; qm += 1.0f; }
-      const uint32_t Q = __float_as_uint(qm) - 0x4B000000u;
-      const uint32_t s = s0 + Q * s1;
-      f0 = f1; f1 = rem; s0 = s1; s1 = s; par ^= 1u;
+      const float qm = inv_quot_c(f0, f1);
+      const float rem = __fmaf_rn(INV_MAGIC - qm, f1, f0);   // r0 - Q r1, exact
+      const uint32_t Q = __float_as_uint(qm) - INV_MAGIC_BITS;
+      const uint32_t s = s0 - Q * s1;
+      f0 = f1; s0 = s1;
+      f1 = fabsf(rem);
+      s1 = rem < 0.0f ? 0u - s : s;
     }
   }
-  const uint32_t inv = par ? q - s1 : s1;
   // inv * x == 1 (mod q)  <=>  redc(inv * x) == redc(1)
-  if (redc((uint64_t)inv * x, q, qinv) != redc(1ull, q, qinv))
-    return inv_mod_slow(x, q);
-  return inv;
+  const uint32_t one = redc(1ull, q, qinv);
+  if (q < 0x80000000u) {
+    const uint32_t inv = (int32_t)s1 < 0 ? s1 + q : s1;
+    if (redc((uint64_t)inv * x, q, qinv) == one) return inv;
+  } else {
+    // candidates s1 mod q and (s1 - 2^32) mod q = that - (2^32 - q); redc of the second's
+    // product with x is the first's minus x
+    const uint32_t inv = s1 >= q ? s1 - q : s1;
+    const uint32_t c = redc((uint64_t)inv * x, q, qinv);
+    if (c == one) return inv;
+    if (mod_sub(c, x, q) == one) return mod_sub(inv, 0u - q, q);
+  }
+  return inv_mod_slow(x, q);
 }
 
 // Key of the reduction loop's pivot choice (postMinPair, GmpCudaDevice-getGcdKernel.cu:152-154):

@@ -245,6 +245,48 @@ __device__ __forceinline__ void t_update_k(uint32_t (&t)[K], uint32_t q, uint32_
   if (need & 1u) t[0] = mont_mul(p[0] > q ? p[0] - q : p[0], Z, q, qinv);
 }
 
+// Size bounds of the reduction loop, for certifying its result: lu >= log2|u_i| and
+// lv >= log2|v_i| in fixed point (BOUND_ONE = 1 bit), stepped by
+// |v_{i+1}| <= (|u_i| + |b| |v_i|) / p.  Integer arithmetic except for the logarithms
+// (log2f, exp2f: within a few ulp, at most 2^-18 bits here), each rounded outward by
+// BOUND_SLACK = 2^-17 bits, so the bounds stay upper bounds.
+constexpr int BOUND_FRAC = 24;
+constexpr long long BOUND_ONE = 1ll << BOUND_FRAC;
+constexpr long long BOUND_SLACK = 1ll << (BOUND_FRAC - 17);
+
+__device__ __forceinline__ long long bound_log2(float x)
+{
+  return (long long)(log2f(x) * (float)BOUND_ONE);
+}
+
+// Bit length of the operand limbs (an upper bound of log2 |x|) in bound units.
+__device__ __forceinline__ long long bound_init(const uint32_t* limbs, uint32_t len)
+{
+  return (long long)(((int)len - 1) * 32 + (32 - __clz(limbs[len - 1]))) << BOUND_FRAC;
+}
+
+__device__ __forceinline__ void bound_step(long long& lu, long long& lv, uint32_t p, int32_t b)
+{
+  const uint32_t ab = b < 0 ? 0u - (uint32_t)b : (uint32_t)b;
+  long long s = lu;                                 // log2(|u| + |b| |v|) <= s
+  if (ab != 0u) {
+    const long long y = lv + bound_log2((float)ab) + BOUND_SLACK;
+    const long long m = y > lu ? y : lu, d = y > lu ? y - lu : lu - y;
+    s = m + BOUND_SLACK;                            // log2(1 + 2^-d) < 2^-17 for d >= 40
+    if (d < 40 * BOUND_ONE) s += bound_log2(1.0f + exp2f(-(float)d * (1.0f / (float)BOUND_ONE)));
+  }
+  lu = lv;
+  lv = s - bound_log2((float)p) + BOUND_SLACK;
+}
+
+// Certified iff the surviving moduli (each > 2^(L-1)) multiply to more than |v| (so v = 0)
+// and more than 2|u| (so the symmetric digits are exact).
+__device__ __forceinline__ bool bound_certified(int remaining, int L, long long lu, long long lv)
+{
+  const long long cap = (long long)remaining * (L - 1) * BOUND_ONE;
+  return cap > lu + 2 * BOUND_ONE && cap > lv + BOUND_ONE;
+}
+
 // Initial state t = u/v mod q from the residues.
 __device__ __forceinline__ uint32_t t_init(uint32_t u, uint32_t v, uint32_t q, uint32_t qinv)
 {

@@ -69,7 +69,7 @@ struct SlotSmem {
   unsigned long long key[2][K][32];  // per-warp minima per slot, double-buffered
   PairDesc d[K];
   uint32_t pi[K];                    // pair index of each slot (~0: empty)
-  double lu[K], lv[K];               // certification bounds (thread 0)
+  long long lu[K], lv[K];            // certification bounds (bound_step)
 };
 
 template <int T, int K>
@@ -162,8 +162,8 @@ __global__ void __launch_bounds__(T, MINB) batchk_kernel(const BatchArgs a)
       if (key_less(h, l, h0, l0)) { h0 = h; l0 = l; }
     }
     if (threadIdx.x == 32u * s) {
-      ss.lu[s] = (double)(((int)d.u_len - 1) * 32 + (32 - __clz(a.limbs[d.u_off + d.u_len - 1])));
-      ss.lv[s] = (double)(((int)d.v_len - 1) * 32 + (32 - __clz(a.limbs[d.v_off + d.v_len - 1])));
+      ss.lu[s] = bound_init(a.limbs + d.u_off, d.u_len);
+      ss.lv[s] = bound_init(a.limbs + d.v_off, d.v_len);
     }
     block_min_key<T>(h0, l0, rs, rparity);
     uint32_t p0;
@@ -214,15 +214,7 @@ __global__ void __launch_bounds__(T, MINB) batchk_kernel(const BatchArgs a)
       int2* hist = reinterpret_cast<int2*>(scr + (size_t)s * 4 * NQS + 2 * (size_t)NQS);
       if (threadIdx.x == 32u * s) {   // one warp per slot keeps the history and the size bounds
         hist[iters[s]] = make_int2((int)p[s], b[s]);
-        const uint32_t ab = b[s] < 0 ? 0u - (uint32_t)b[s] : (uint32_t)b[s];
-        double sum = ss.lu[s];
-        if (ab != 0u) {
-          const double y = ss.lv[s] + (double)log2f((float)ab);
-          const double m = y > sum ? y : sum, dd = y > sum ? y - sum : sum - y;
-          sum = m + (dd < 40.0 ? (double)log2f(1.0f + exp2f(-(float)dd)) : 0.0);
-        }
-        ss.lu[s] = ss.lv[s];
-        ss.lv[s] = sum - (double)log2f((float)p[s]) + 1e-4;
+        bound_step(ss.lu[s], ss.lv[s], p[s], b[s]);
       }
       ++iters[s];
       rem[s] -= 1;
@@ -374,11 +366,11 @@ __global__ void __launch_bounds__(T) cluster_batchk_kernel(const BatchArgs a)
       if (key_less(h, l, h0, l0)) { h0 = h; l0 = l; }
     }
     if (threadIdx.x == 32u * s) {
-      ss.lu[s] = (double)(((int)d.u_len - 1) * 32 + (32 - __clz(a.limbs[d.u_off + d.u_len - 1])));
-      ss.lv[s] = (double)(((int)d.v_len - 1) * 32 + (32 - __clz(a.limbs[d.v_off + d.v_len - 1])));
+      ss.lu[s] = bound_init(a.limbs + d.u_off, d.u_len);
+      ss.lv[s] = bound_init(a.limbs + d.v_off, d.v_len);
     }
     block_min_key<T>(h0, l0, rs, bparity);
-    cluster_min_key<T>(h0, l0, cs, rparity);
+    cluster_min_key<T>(h0, l0, cs, rparity, [] {});
     uint32_t p0;
     int32_t b0;
     key_pair(h0, l0, p0, b0);
@@ -428,15 +420,7 @@ __global__ void __launch_bounds__(T) cluster_batchk_kernel(const BatchArgs a)
           int2* hist = reinterpret_cast<int2*>(scr + (size_t)s * 4 * NQS + 2 * (size_t)NQS);
           hist[iters[s]] = make_int2((int)p[s], b[s]);
         }
-        const uint32_t ab = b[s] < 0 ? 0u - (uint32_t)b[s] : (uint32_t)b[s];
-        double sum = ss.lu[s];
-        if (ab != 0u) {
-          const double y = ss.lv[s] + (double)log2f((float)ab);
-          const double m = y > sum ? y : sum, dd = y > sum ? y - sum : sum - y;
-          sum = m + (dd < 40.0 ? (double)log2f(1.0f + exp2f(-(float)dd)) : 0.0);
-        }
-        ss.lu[s] = ss.lv[s];
-        ss.lv[s] = sum - (double)log2f((float)p[s]) + 1e-4;
+        bound_step(ss.lu[s], ss.lv[s], p[s], b[s]);
       }
       ++iters[s];
       rem[s] -= 1;

@@ -61,6 +61,17 @@ __device__ __forceinline__ void cluster_sync_all()
   asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
+// The two halves of cluster_sync_all, for work that overlaps the wait.
+__device__ __forceinline__ void cluster_arrive()
+{
+  asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void cluster_wait()
+{
+  asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
 // Stores v at the same shared-memory offset as *local in CTA `rank` of this cluster.
 __device__ __forceinline__ void st_cluster_u64(unsigned long long* local, uint32_t rank, unsigned long long v)
 {
@@ -72,8 +83,9 @@ __device__ __forceinline__ void st_cluster_u64(unsigned long long* local, uint32
 
 // Minimum over the whole cluster: each warp's minimum is written into every CTA's
 // slots, one cluster barrier, then each warp reduces all slots locally.
-template <int T>
-__device__ __forceinline__ void cluster_min_key(uint32_t& hi, uint32_t& lo, ClusterSmem& cs, uint32_t& parity)
+template <int T, class F>
+__device__ __forceinline__ void cluster_min_key(uint32_t& hi, uint32_t& lo, ClusterSmem& cs, uint32_t& parity,
+                                                F&& during)
 {
   constexpr int NW = T / 32;
   const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
@@ -81,7 +93,9 @@ __device__ __forceinline__ void cluster_min_key(uint32_t& hi, uint32_t& lo, Clus
   warp_min_key(hi, lo);
   const unsigned long long k = ((unsigned long long)hi << 32) | lo;
   if (lane < nc) st_cluster_u64(&cs.key[parity][me][w], lane, k);   // lane r writes into CTA r
-  cluster_sync_all();
+  cluster_arrive();
+  during();
+  cluster_wait();
   unsigned long long m = ~0ull;
   for (uint32_t e = lane; e < nc * NW; e += 32) {
     const unsigned long long x = cs.key[parity][e / NW][e % NW];
@@ -162,15 +176,20 @@ __device__ __forceinline__ void block_min_key(uint32_t& hi, uint32_t& lo, RedSme
 // all CTAs of this epoch arrived.  CTA 0 clears the slot of epoch + 1 before arriving:
 // every CTA has finished reading that slot (epoch - 2) once CTA 0 is past epoch - 1.
 // Returns false if the wait expired (the grid then unwinds; the host sees ST_TIMEOUT).
-template <int T, int MODE>
+// `during()` is called by every thread while the CTA waits for the others (after its own
+// contribution is out), so per-iteration bookkeeping of one thread (BOUND_THREAD, never a
+// thread that takes part in the exchange) overlaps the exchange.
+constexpr uint32_t BOUND_THREAD = 32;
+
+template <int T, int MODE, class F>
 __device__ __forceinline__ bool reduce_min(uint32_t& hi, uint32_t& lo, RedSmem& rs, uint32_t& parity,
-                                           GridSync* gs, uint32_t& epoch)
+                                           GridSync* gs, uint32_t& epoch, F&& during)
 {
   if constexpr (MODE == SYNC_CLUSTER) {
     ClusterSmem& cs = *reinterpret_cast<ClusterSmem*>(gs);
     const uint32_t nc = cluster_size();
     if (nc * (T / 32) <= 64) {
-      cluster_min_key<T>(hi, lo, cs, parity);
+      cluster_min_key<T>(hi, lo, cs, parity, during);
       return true;
     }
     // Large clusters: the CTA's minimum first (one __syncthreads), then one key per CTA
@@ -179,7 +198,9 @@ __device__ __forceinline__ bool reduce_min(uint32_t& hi, uint32_t& lo, RedSmem& 
     block_min_key<T>(hi, lo, rs, parity);
     const uint32_t cb = epoch & 1u, lane = threadIdx.x & 31u, me = cluster_rank();
     if (threadIdx.x < 32u && lane < nc) st_cluster_u64(&cs.key[cb][me][0], lane, ((unsigned long long)hi << 32) | lo);
-    cluster_sync_all();
+    cluster_arrive();
+    during();
+    cluster_wait();
     const unsigned long long k = lane < nc ? cs.key[cb][lane][0] : ~0ull;
     hi = (uint32_t)(k >> 32);
     lo = (uint32_t)k;
@@ -187,10 +208,13 @@ __device__ __forceinline__ bool reduce_min(uint32_t& hi, uint32_t& lo, RedSmem& 
     epoch += 1u;
     return true;
   }
-  block_min_key<T>(hi, lo, rs, parity);
   if constexpr (MODE == SYNC_CTA) {
+    during();
+    block_min_key<T>(hi, lo, rs, parity);
     return true;
-  } else if constexpr (MODE == SYNC_CGRID) {
+  }
+  block_min_key<T>(hi, lo, rs, parity);
+  if constexpr (MODE == SYNC_CGRID) {
     // CTA minima -> every CTA of the cluster (DSMEM), one cluster barrier; the cluster's
     // rank-0 thread 0 takes part in the global exchange (atomic min, release arrival,
     // bounded acquire wait) and stores the result into every CTA; one more cluster barrier.
@@ -234,6 +258,7 @@ __device__ __forceinline__ bool reduce_min(uint32_t& hi, uint32_t& lo, RedSmem& 
         asm volatile("st.shared::cluster.u32 [%0], %1;" :: "r"(ra), "r"(bad) : "memory");
       }
     }
+    during();
     cluster_sync_all();
     const unsigned long long k = cg.res[cb];
     const bool ok = cg.bad[cb] == 0u;
@@ -259,6 +284,7 @@ __device__ __forceinline__ bool reduce_min(uint32_t& hi, uint32_t& lo, RedSmem& 
       rs.bcast = bad ? ~0ull : ld_relaxed_u64(&gs->slot[s]);
       rs.bad = bad;
     }
+    during();
     __syncthreads();
     const unsigned long long k = rs.bcast;
     const bool ok = rs.bad == 0;
@@ -267,6 +293,13 @@ __device__ __forceinline__ bool reduce_min(uint32_t& hi, uint32_t& lo, RedSmem& 
     epoch += 1u;
     return ok;
   }
+}
+
+template <int T, int MODE>
+__device__ __forceinline__ bool reduce_min(uint32_t& hi, uint32_t& lo, RedSmem& rs, uint32_t& parity,
+                                           GridSync* gs, uint32_t& epoch)
+{
+  return reduce_min<T, MODE>(hi, lo, rs, parity, gs, epoch, [] {});
 }
 
 // x mod q_j for the nloc moduli mods[0..nloc), into acc[] (shared).  Limbs are staged
@@ -302,7 +335,7 @@ template <int T, int MODE>
 __device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d, int L, uint32_t j0, uint32_t nloc,
                             uint32_t* st, RedSmem& rs, uint32_t& parity, uint32_t& epoch, GridSync* gs,
                             const uint32_t* u0g, const uint32_t* v0g, const int2* hist, uint32_t iters, int remaining,
-                            double lu, double lv, mgcd_pair* digits, uint32_t* count, int32_t* status,
+                            long long lu, long long lv, mgcd_pair* digits, uint32_t* count, int32_t* status,
                             InvTab inv);
 
 // The whole gcd of one pair by this CTA (GRID = false) or by the cooperative grid, the
@@ -349,28 +382,16 @@ __device__ void run_pair(const uint32_t* __restrict__ limbs, const PairDesc& d, 
   int remaining = (int)d.nq;
   int ubits = ((int)d.u_len + 1) * 32, vbits = ((int)d.v_len + 1) * 32;
   uint32_t iters = 0;
-  // Certification bounds (thread 0 of each CTA; every CTA computes the same values):
-  // lu >= log2|u_i|, lv >= log2|v_i| with |v_{i+1}| <= (|u_i| + |b| |v_i|) / p.
-  double lu = 0.0, lv = 0.0;
-  if (threadIdx.x == 0) {
-    lu = (double)(((int)d.u_len - 1) * 32 + (32 - __clz(limbs[d.u_off + d.u_len - 1])));
-    lv = (double)(((int)d.v_len - 1) * 32 + (32 - __clz(limbs[d.v_off + d.v_len - 1])));
+  // Certification bounds (BOUND_THREAD of each CTA; every CTA computes the same values),
+  // stepped while the CTA waits in the exchange.
+  long long lu = 0, lv = 0;
+  if (threadIdx.x == BOUND_THREAD) {
+    lu = bound_init(limbs + d.u_off, d.u_len);
+    lv = bound_init(limbs + d.v_off, d.v_len);
   }
   while (b != MOD_INFINITY) {
     if (writer) hist[iters] = make_int2((int)p, b);
     ++iters;
-    if (threadIdx.x == 0) {
-      const uint32_t ab = b < 0 ? 0u - (uint32_t)b : (uint32_t)b;
-      double s = lu;
-      if (ab != 0u) {
-        const double y = lv + (double)log2f((float)ab);
-        const double m = y > lu ? y : lu, dd = y > lu ? y - lu : lu - y;
-        s = m + (dd < 40.0 ? (double)log2f(1.0f + exp2f(-(float)dd)) : 0.0);
-      }
-      const double lnew = s - (double)log2f((float)p) + 1e-4;
-      lu = lv;
-      lv = lnew;
-    }
     kh = 0xFFFFFFFFu;
     kl = 0xFFFFFFFFu;
     for (uint32_t j = threadIdx.x; j < nloc; j += T) {
@@ -390,7 +411,11 @@ __device__ void run_pair(const uint32_t* __restrict__ limbs, const PairDesc& d, 
       if (writer) { *status = ST_REDUX; *count = 0; }
       return;
     }
-    if (!reduce_min<T, MODE>(kh, kl, rs, parity, gs, epoch)) {
+    const uint32_t pp = p;
+    const int32_t bb = b;
+    if (!reduce_min<T, MODE>(kh, kl, rs, parity, gs, epoch, [&] {
+          if (threadIdx.x == BOUND_THREAD) bound_step(lu, lv, pp, bb);
+        })) {
       if (writer) *status = ST_TIMEOUT;
       return;
     }
@@ -585,12 +610,12 @@ __device__ void recover_panels(const ModConst* __restrict__ mods, const PairDesc
 
 // After the reduction loop of one pair: certification, replay and recovery (MGCD4).
 // st holds the final t states of this CTA's moduli; `remaining` the surviving count;
-// lu, lv (meaningful in thread 0) the size bounds of the final u and v.
+// lu, lv (meaningful in BOUND_THREAD) the size bounds of the final u and v.
 template <int T, int MODE>
 __device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d, int L, uint32_t j0, uint32_t nloc,
                             uint32_t* st, RedSmem& rs, uint32_t& parity, uint32_t& epoch, GridSync* gs,
                             const uint32_t* u0g, const uint32_t* v0g, const int2* hist, uint32_t iters, int remaining,
-                            double lu, double lv, mgcd_pair* digits, uint32_t* count, int32_t* status,
+                            long long lu, long long lv, mgcd_pair* digits, uint32_t* count, int32_t* status,
                             InvTab inv)
 {
   const bool writer = threadIdx.x == 0 && lead_cta<MODE>();
@@ -599,10 +624,7 @@ __device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d
   // Certify the result: all surviving residues of v are 0, so v = 0 if the surviving
   // moduli (each > 2^(L-1)) multiply to more than |v|; recovery is exact if they exceed
   // 2|u| (symmetric digits).  Otherwise report that more moduli are needed.
-  if (threadIdx.x == 0) {
-    const double cap = (double)remaining * (double)(L - 1);
-    rs.cert = (cap > lu + 2.0 && cap > lv + 1.0) ? 0u : 1u;
-  }
+  if (threadIdx.x == BOUND_THREAD) rs.cert = bound_certified(remaining, L, lu, lv) ? 0u : 1u;
   if constexpr (MODE == SYNC_GRID) __threadfence();
   __syncthreads();
   if (rs.cert) {

@@ -600,6 +600,7 @@ static int launch_set(mgcd_context* c, Plan& P, const std::vector<Bucket>& bucke
           grid > (uint32_t)(c->sms * bps))
         return MGCD_ERR_GRID;
     }
+    if (grid > (uint32_t)MAX_GRID_CTAS) return MGCD_ERR_GRID;   // one exchange slot per CTA
     g.per_cta = per;
     g.sync = P.d_gsync.as<GridSync>();
     CK(launch_gridsync_init(g.sync, c->wait_timeout_ns, c->withhold_cta, P.stream));

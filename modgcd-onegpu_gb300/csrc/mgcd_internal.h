@@ -68,16 +68,24 @@ struct BatchArgs {
 };
 
 // State of the cross-CTA reduction used by a single pair spread over a cooperative grid.
-// Exchange e: thread 0 of every CTA folds its minimum into slot[e % 3] (atomic min) and
-// arrives on a monotonic counter; CTAs wait (bounded) for e + 1 full rounds of arrivals,
-// then read the slot.  CTA 0 resets slot[(e + 1) % 3] before arriving: all CTAs have read
-// that slot (exchange e - 2) once CTA 0 is past exchange e - 1.
+// Cooperative grid (leader exchange), exchange e: every CTA stores its minimum, tagged with
+// bit (e / 2 + 1) & 1, into keys[e & 1][cta]; CTA 0 polls all slots until their tags
+// match, reduces them and stores the tagged result into bcast[e & 1]; the other CTAs poll
+// that word.  A slot read in exchange e holds the value of e or of e - 2 (no CTA can be two
+// exchanges ahead of another), which the tag tells apart: no atomics and no fences.
+// Cluster grid, exchange e: the leader thread of every cluster folds the cluster's minimum
+// into slot[e % 3] (atomic min) and arrives on a monotonic counter; leaders wait (bounded)
+// for e + 1 full rounds of arrivals, then read the slot.  Cluster 0 resets slot[(e + 1) % 3]
+// before arriving: all leaders have read that slot (exchange e - 2) once it is past e - 1.
+constexpr int MAX_GRID_CTAS = 1024;
 struct GridSync {
-  unsigned long long slot[3];              // ~0 before use
+  unsigned long long keys[2][MAX_GRID_CTAS];   // zero before use
+  unsigned long long bcast[2][16];             // [b][0]; one 128-byte line each
+  unsigned long long slot[3];                  // ~0 before use
   unsigned int arrive;
-  unsigned int error;                      // set by the first CTA whose wait expired
-  unsigned int withhold_cta;               // test hook: this CTA never publishes (0xFFFFFFFF: none)
-  unsigned long long timeout_ns;           // bound of every wait
+  unsigned int error;                          // set by the first CTA whose wait expired
+  unsigned int withhold_cta;                   // test hook: this CTA never publishes (0xFFFFFFFF: none)
+  unsigned long long timeout_ns;               // bound of every wait
 };
 
 struct GridArgs {

@@ -595,18 +595,23 @@ __global__ void __launch_bounds__(256) int_peak_kernel(uint32_t* out, int iters)
   if ((a0 ^ a1 ^ a2 ^ a3 ^ a4 ^ a5 ^ a6 ^ a7) == 0x2545F491u) out[0] = 1u;
 }
 
-__global__ void gridsync_init_kernel(GridSync* gs, unsigned long long timeout_ns, uint32_t withhold)
+__global__ void __launch_bounds__(256) gridsync_init_kernel(GridSync* gs, unsigned long long timeout_ns,
+                                                             uint32_t withhold)
 {
-  gs->slot[0] = gs->slot[1] = gs->slot[2] = ~0ull;
-  gs->arrive = 0u;
-  gs->error = 0u;
-  gs->withhold_cta = withhold;
-  gs->timeout_ns = timeout_ns;
+  for (uint32_t i = threadIdx.x; i < 2u * MAX_GRID_CTAS; i += blockDim.x) (&gs->keys[0][0])[i] = 0ull;
+  if (threadIdx.x < 32u) (&gs->bcast[0][0])[threadIdx.x] = 0ull;
+  if (threadIdx.x == 0) {
+    gs->slot[0] = gs->slot[1] = gs->slot[2] = ~0ull;
+    gs->arrive = 0u;
+    gs->error = 0u;
+    gs->withhold_cta = withhold;
+    gs->timeout_ns = timeout_ns;
+  }
 }
 
 cudaError_t launch_gridsync_init(GridSync* gs, unsigned long long timeout_ns, uint32_t withhold, cudaStream_t s)
 {
-  gridsync_init_kernel<<<1, 1, 0, s>>>(gs, timeout_ns, withhold);
+  gridsync_init_kernel<<<1, 256, 0, s>>>(gs, timeout_ns, withhold);
   return cudaGetLastError();
 }
 

@@ -170,18 +170,40 @@ __device__ __forceinline__ void block_min_key(uint32_t& hi, uint32_t& lo, RedSme
   parity ^= 1u;
 }
 
-// Minimum over the CTA and, in grid mode, over all CTAs of the cooperative grid.
-// Grid exchange: thread 0 of every CTA folds its minimum into slot[epoch % 3] with an
-// atomic min, then arrives on a monotonic counter and waits (bounded by timeout_ns) until
-// all CTAs of this epoch arrived.  CTA 0 clears the slot of epoch + 1 before arriving:
-// every CTA has finished reading that slot (epoch - 2) once CTA 0 is past epoch - 1.
-// Returns false if the wait expired (the grid then unwinds; the host sees ST_TIMEOUT).
+// Minimum over the CTA and, with several CTAs, over the cluster (DSMEM + cluster barrier),
+// the cooperative grid (leader exchange over tagged slots) or the cluster grid (atomic
+// minimum and arrival counter per cluster leader); the grid protocols are described at
+// GridSync.  Every wait is bounded by timeout_ns; returns false if one expired (the grid
+// then unwinds; the host sees ST_TIMEOUT).
 // `during()` is called by every thread while the CTA waits for the others (after its own
-// contribution is out), so per-iteration bookkeeping of one thread (BOUND_THREAD, never a
-// thread that takes part in the exchange) overlaps the exchange.
+// contribution is out), so per-iteration bookkeeping of one thread (BOUND_THREAD, not the
+// thread that carries the CTA's part of the exchange) overlaps the exchange.
 constexpr uint32_t BOUND_THREAD = 32;
 
-template <int T, int MODE, class F>
+// 63-bit form of a key for the tagged grid exchange, in the same order: |value| keys stay
+// below 2^31 - 1, MOD_INFINITY (0x80000000) and "no key" (0xFFFFFFFF, 0xFFFFFFFF) share the
+// high word 2^31 - 1 and differ in the low word.  Bit 63 carries the exchange tag.
+constexpr unsigned long long KEY_TAG = 1ull << 63;
+
+__device__ __forceinline__ unsigned long long pack_key(uint32_t hi, uint32_t lo)
+{
+  const uint32_t h = hi >= 0x7FFFFFFFu ? 0x7FFFFFFFu : hi;
+  return ((unsigned long long)h << 32) | lo;
+}
+
+__device__ __forceinline__ void unpack_key(unsigned long long k, uint32_t& hi, uint32_t& lo)
+{
+  lo = (uint32_t)k;
+  const uint32_t h = (uint32_t)(k >> 32) & 0x7FFFFFFFu;
+  hi = h != 0x7FFFFFFFu ? h : (lo == 0xFFFFFFFFu ? 0xFFFFFFFFu : KEY_INF_HI);
+}
+
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned long long v)
+{
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" :: "l"(p), "l"(v) : "memory");
+}
+
+template <int T, int MODE, bool PUB = false, class F>
 __device__ __forceinline__ bool reduce_min(uint32_t& hi, uint32_t& lo, RedSmem& rs, uint32_t& parity,
                                            GridSync* gs, uint32_t& epoch, F&& during)
 {
@@ -267,39 +289,69 @@ __device__ __forceinline__ bool reduce_min(uint32_t& hi, uint32_t& lo, RedSmem& 
     epoch += 1u;
     return ok;
   } else {
-    if (threadIdx.x == 0) {
-      const uint32_t s = epoch % 3u;
-      uint32_t bad = 0;
-      if (blockIdx.x != gs->withhold_cta) {
-        atomicMin(&gs->slot[s], ((unsigned long long)hi << 32) | lo);
-        if (blockIdx.x == 0) gs->slot[(epoch + 1u) % 3u] = ~0ull;
-        red_release_add_u32(&gs->arrive, 1u);
+    // Leader exchange (GridSync): tagged slots, relaxed stores and loads, bounded polls.
+    // PUB adds release fences before the stores and acquire fences after the polls, for
+    // exchanges that also publish data written before them.
+    const uint32_t b = epoch & 1u;
+    const unsigned long long tag = (unsigned long long)(((epoch >> 1) + 1u) & 1u) << 63;
+    unsigned long long* const keys = gs->keys[b];
+    unsigned long long k = pack_key(hi, lo);
+    uint32_t bad = 0;
+    if (blockIdx.x != 0) {
+      if (threadIdx.x == 0) {
+        if constexpr (PUB) __threadfence();
+        if (blockIdx.x != gs->withhold_cta) st_relaxed_u64(keys + blockIdx.x, tag | k);
+        const unsigned long long t0 = globaltimer_ns();
+        unsigned long long v;
+        for (;;) {
+          v = ld_relaxed_u64(&gs->bcast[b][0]);
+          if ((v & KEY_TAG) == tag) break;
+          if (ld_relaxed_u32(&gs->error)) { bad = 1; break; }
+          if (globaltimer_ns() - t0 > gs->timeout_ns) { atomicExch(&gs->error, 1u); bad = 1; break; }
+        }
+        if constexpr (PUB) __threadfence();
+        rs.bcast = v & ~KEY_TAG;
+        rs.bad = bad;
       }
-      const unsigned int target = (epoch + 1u) * gridDim.x;
+      during();
+      __syncthreads();
+      k = rs.bcast;
+      bad = rs.bad;
+    } else {
+      during();
+      unsigned long long m = threadIdx.x == 0 ? k : ~0ull;
       const unsigned long long t0 = globaltimer_ns();
-      while (ld_acquire_u32(&gs->arrive) < target) {
-        if (ld_relaxed_u32(&gs->error)) { bad = 1; break; }
-        if (globaltimer_ns() - t0 > gs->timeout_ns) { atomicExch(&gs->error, 1u); bad = 1; break; }
+      for (uint32_t i = threadIdx.x == 0 ? T : threadIdx.x; i < gridDim.x && !bad; i += T) {
+        unsigned long long v;
+        for (;;) {
+          v = ld_relaxed_u64(keys + i);
+          if ((v & KEY_TAG) == tag) break;
+          if (globaltimer_ns() - t0 > gs->timeout_ns) { atomicExch(&gs->error, 1u); bad = 1; break; }
+        }
+        v &= ~KEY_TAG;
+        m = v < m ? v : m;
       }
-      rs.bcast = bad ? ~0ull : ld_relaxed_u64(&gs->slot[s]);
-      rs.bad = bad;
+      if constexpr (PUB) __threadfence();
+      bad = __syncthreads_or(bad) ? 1u : 0u;
+      uint32_t mh = (uint32_t)(m >> 32), ml = (uint32_t)m;
+      block_min_key<T>(mh, ml, rs, parity);
+      k = ((unsigned long long)mh << 32) | ml;
+      if (threadIdx.x == 0 && !bad && blockIdx.x != gs->withhold_cta) {
+        if constexpr (PUB) __threadfence();
+        st_relaxed_u64(&gs->bcast[b][0], tag | k);
+      }
     }
-    during();
-    __syncthreads();
-    const unsigned long long k = rs.bcast;
-    const bool ok = rs.bad == 0;
-    hi = (uint32_t)(k >> 32);
-    lo = (uint32_t)k;
+    unpack_key(k, hi, lo);
     epoch += 1u;
-    return ok;
+    return bad == 0;
   }
 }
 
-template <int T, int MODE>
+template <int T, int MODE, bool PUB = false>
 __device__ __forceinline__ bool reduce_min(uint32_t& hi, uint32_t& lo, RedSmem& rs, uint32_t& parity,
                                            GridSync* gs, uint32_t& epoch)
 {
-  return reduce_min<T, MODE>(hi, lo, rs, parity, gs, epoch, [] {});
+  return reduce_min<T, MODE, PUB>(hi, lo, rs, parity, gs, epoch, [] {});
 }
 
 // x mod q_j for the nloc moduli mods[0..nloc), into acc[] (shared).  Limbs are staged
@@ -464,7 +516,7 @@ __device__ void recover_panels(const ModConst* __restrict__ mods, const PairDesc
   for (;;) {
     // ---- 1. the lowest remaining modulus
     while (scan < nloc && st[scan] == U_RETIRED) ++scan;
-    uint32_t kh = scan < nloc ? j0 + scan : 0xFFFFFFFFu, kl = 0u;
+    uint32_t kh = scan < nloc ? j0 + scan : 0xFFFFFFFFu, kl = scan < nloc ? 0u : 0xFFFFFFFFu;
     if (!reduce_min<T, MODE>(kh, kl, rs, parity, gs, epoch)) { fail = true; break; }
     if (kh == 0xFFFFFFFFu) break;      // no modulus left (not reached while remaining > 0)
     const bool front = kh >= j0 && kh < j0 + nloc;
@@ -529,10 +581,10 @@ __device__ void recover_panels(const ModConst* __restrict__ mods, const PairDesc
       }
       __syncthreads();
     }
-    // ---- 3. publish the panel
+    // ---- 3. publish the panel (an exchange that orders the digits and the count before it)
     kh = 0xFFFFFFFFu;
-    kl = 0u;
-    if (!reduce_min<T, MODE>(kh, kl, rs, parity, gs, epoch)) { fail = true; break; }
+    kl = 0xFFFFFFFFu;
+    if (!reduce_min<T, MODE, true>(kh, kl, rs, parity, gs, epoch)) { fail = true; break; }
     if (threadIdx.x == 0) pn = *reinterpret_cast<volatile uint32_t*>(count) - ndig;
     __syncthreads();
     const uint32_t nd = pn;
@@ -544,7 +596,7 @@ __device__ void recover_panels(const ModConst* __restrict__ mods, const PairDesc
     if (nd == 0u) {
       // ---- 5. one reference round: the lowest nonzero modulus anywhere, or the end
       kh = 0xFFFFFFFFu;
-      kl = 0u;
+      kl = 0xFFFFFFFFu;
       for (uint32_t j = threadIdx.x; j < nloc; j += T) {
         const uint32_t u = st[j];
         if (u != U_RETIRED && u != 0u) { kh = j0 + j; kl = (uint32_t)to_signed(u, my[j].q); break; }
@@ -631,6 +683,15 @@ __device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d
     if (writer) { *status = ST_INSUFFICIENT; *count = 0; }
     __syncthreads();
     return;
+  }
+  if constexpr (MODE == SYNC_GRID) {
+    // CTA 0's thread 0 wrote the (p, b) history during the loop, whose exchanges order
+    // nothing but the keys: one fenced exchange publishes it to every CTA.
+    uint32_t h = 0xFFFFFFFFu, l = 0xFFFFFFFFu;
+    if (!reduce_min<T, MODE, true>(h, l, rs, parity, gs, epoch)) {
+      if (writer) *status = ST_TIMEOUT;
+      return;
+    }
   }
 
   // ---- replay: u mod q of the surviving moduli from (u0, v0) and the (p, b) history.

@@ -198,12 +198,14 @@ def serve_leg(mg, wl, po, dev, rates, n_req, nthreads, seed=5):
 
 
 def apply_tuning(dev, path):
-    """Loads the tuning table (mgcd_load_tuning); returns its path or None."""
+    """Loads the tuning table (mgcd_load_tuning); returns its path (relative to the
+    repository when inside it) or None."""
     try:
         dev.load_tuning(path)
-        return path
     except (OSError, RuntimeError):
         return None
+    rel = os.path.relpath(os.path.abspath(path), ROOT)
+    return path if rel.startswith("..") else rel
 
 
 def run_reference(args, rank, pg):

@@ -129,18 +129,19 @@ int mgcd_set_nq_scale(mgcd_context *ctx, float scale);
 /* Launch shape of single pairs too large for one CTA:
      MGCD_SINGLE_AUTO              a thread-block cluster of up to 16 CTAs (pivot exchange
                                    through distributed shared memory) while the pair's
-                                   moduli fit 16 x 1024 threads, else a cooperative grid
-                                   with one CTA per SM (default);
+                                   moduli fit 16 x 512 threads, else a cooperative grid
+                                   with at most one CTA per SM and a leader exchange of
+                                   tagged per-CTA slots (default);
      MGCD_SINGLE_REFERENCE_SHAPE   the reference's launch shape: a cooperative grid of
                                    256-thread CTAs with 256 moduli each, one grid-wide
                                    exchange per iteration (GmpCudaDevice-gcd.cu:80-96). */
 #define MGCD_SINGLE_AUTO            0
 #define MGCD_SINGLE_REFERENCE_SHAPE 1
-/*   MGCD_SINGLE_CLUSTER_GRID      above 16 x 1024 moduli: a cooperative grid of 8-CTA
+/*   MGCD_SINGLE_CLUSTER_GRID      above 16 x 512 moduli: a cooperative grid of 8-CTA
                                    clusters; keys meet in each cluster through DSMEM and one
-                                   leader per cluster joins the global exchange (fewer global
-                                   atomics, two more barriers per iteration: measured 20 %
-                                   slower than the default on GB300). */
+                                   leader per cluster joins a global exchange of atomic
+                                   minimum and arrival counter (measured 20-40 % slower than
+                                   the default on GB300). */
 #define MGCD_SINGLE_CLUSTER_GRID    2
 int mgcd_set_single_pair_policy(mgcd_context *ctx, int policy);
 /* Bound of every wait a cooperative-grid pair makes on the other CTAs (default 2,000 ms).

@@ -402,7 +402,9 @@ int mgcd::plan_batch(mgcd_context* c, Plan& P, size_t np, const uint32_t* limbs,
 
   // Device buffers and upload.
   cudaStream_t s = P.stream;
-  CK(P.d_limbs.grow(std::max<uint64_t>(limb_end, 1) * sizeof(uint32_t), c->pool, s));
+  // + 4 limbs: the kernels stage operand tiles by bulk copies widened to 16-byte bounds
+  CK(P.d_limbs.grow((std::max<uint64_t>(limb_end, 1) + 4) * sizeof(uint32_t), c->pool, s));
+  if (reinterpret_cast<uintptr_t>(P.d_limbs.p) % 16 != 0) return MGCD_ERR_CUDA;   // pool blocks are 256-aligned
   CK(P.d_pairs.grow(std::max<size_t>(ng, 1) * sizeof(PairDesc), c->pool, s));
   CK(P.d_order.grow(std::max<size_t>(P.order.size(), 1) * sizeof(uint32_t), c->pool, s));
   CK(P.d_digits.grow(std::max<size_t>(P.ndig, 1) * sizeof(mgcd_pair), c->pool, s));
@@ -549,9 +551,11 @@ static int launch_set(mgcd_context* c, Plan& P, const std::vector<Bucket>& bucke
     g.iters = P.d_iters.as<uint32_t>() + k;
     g.status = P.d_status.as<int32_t>() + k;
     const bool ref_shape = c->single_policy == MGCD_SINGLE_REFERENCE_SHAPE;
-    if (!ref_shape && d.nq <= (uint32_t)MAX_CLUSTER * 1024) {
-      // thread-block cluster: as many CTAs (<= 16) as keep one modulus per thread (two per
-      // thread measured 1.5-1.8x slower than the grid at 18,176-31,744 moduli)
+    if (!ref_shape && d.nq <= (uint32_t)MAX_CLUSTER * 512) {
+      // thread-block cluster: as many CTAs (<= 16) as keep one modulus per thread, up to 512
+      // threads per CTA (with 1024-thread CTAs the cluster's two-level exchange measured
+      // slower than the grid's leader exchange: 16.8 vs 16.5 ms at 9,728 moduli, 20.8 vs
+      // 19.0 ms at 11,264; at 8,192 moduli the 512-thread cluster wins, 13.0 vs 14.0 ms)
       const int ctas = (int)std::min<uint32_t>(MAX_CLUSTER, (d.nq + 255) / 256);
       const uint32_t per = (d.nq + ctas - 1) / ctas;
       const int threads = per <= 256 ? 256 : per <= 512 ? 512 : 1024;

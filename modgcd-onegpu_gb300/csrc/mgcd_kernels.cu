@@ -33,9 +33,12 @@ __global__ void __launch_bounds__(T) batch_kernel(const BatchArgs a)
   extern __shared__ __align__(16) uint32_t smem[];
   __shared__ RedSmem rs;
   __shared__ uint32_t next;
-  uint32_t* st = smem;
-  uint32_t* acc2 = smem + a.nq_max;
-  uint32_t* chunk = acc2 + a.nq_max;
+  __shared__ unsigned long long stage_bar[2];
+  __shared__ uint32_t stage_state;
+  const Stage stg{smem, stage_bar, &stage_state};     // dynamic shared memory starts with it
+  stage_init(stg);
+  uint32_t* st = smem + STAGE_SMEM_WORDS;
+  uint32_t* acc2 = st + a.nq_max;
   uint32_t* scr = a.scratch + (size_t)blockIdx.x * a.scratch_words;
   uint32_t* u0 = scr;
   uint32_t* v0 = scr + a.nq_max;
@@ -48,7 +51,7 @@ __global__ void __launch_bounds__(T) batch_kernel(const BatchArgs a)
     if (k >= a.npairs) break;
     const uint32_t pi = a.order[k];
     const PairDesc d = a.pairs[pi];
-    run_pair<T, SYNC_CTA>(a.limbs, d, a.mods, a.L, 0u, d.nq, st, acc2, chunk, rs, u0, v0, hist, nullptr,
+    run_pair<T, SYNC_CTA>(a.limbs, d, a.mods, a.L, 0u, d.nq, st, acc2, stg, rs, u0, v0, hist, nullptr,
                        a.digits, a.count + pi, a.iters + pi, a.status + pi, a.inv);
     __syncthreads();
   }
@@ -120,10 +123,13 @@ __global__ void __launch_bounds__(T, MINB) batchk_kernel(const BatchArgs a)
   __shared__ SlotSmem<K> ss;
   __shared__ RedSmem rs;
   __shared__ uint32_t next;
+  __shared__ unsigned long long stage_bar[2];
+  __shared__ uint32_t stage_state;
+  const Stage stg{smem, stage_bar, &stage_state};     // dynamic shared memory starts with it
+  stage_init(stg);
   const uint32_t NQS = a.nq_max;
-  uint32_t* const tS = smem;                          // K x NQS states
-  uint32_t* const acc2 = smem + (size_t)K * NQS;      // residues of v during set-up
-  uint32_t* const chunk = acc2 + NQS;
+  uint32_t* const tS = smem + STAGE_SMEM_WORDS;       // K x NQS states
+  uint32_t* const acc2 = tS + (size_t)K * NQS;        // residues of v during set-up
   uint32_t* const scr = a.scratch + (size_t)blockIdx.x * a.scratch_words;   // per slot u0, v0, hist
   const int L = a.L;
   uint32_t kparity = 0, rparity = 0, repoch = 0;
@@ -133,22 +139,28 @@ __global__ void __launch_bounds__(T, MINB) batchk_kernel(const BatchArgs a)
   int32_t b[K];
 
   // Takes the next pair of the queue into slot s: residues, initial ratios, first pivot.
+  // A pair whose operands could not be staged is answered with ST_TIMEOUT.
   auto load = [&](int s) -> bool {
-    if (threadIdx.x == 0) next = atomicAdd(a.queue, 1u);
-    __syncthreads();
-    const uint32_t k = next;
-    __syncthreads();
-    if (k >= a.npairs) return false;
-    if (threadIdx.x == 0) {
-      ss.pi[s] = a.order[k];
-      ss.d[s] = a.pairs[ss.pi[s]];
-    }
-    __syncthreads();
-    const PairDesc& d = ss.d[s];
     uint32_t* ts = tS + (size_t)s * NQS;
+    for (;;) {
+      if (threadIdx.x == 0) next = atomicAdd(a.queue, 1u);
+      __syncthreads();
+      const uint32_t k = next;
+      __syncthreads();
+      if (k >= a.npairs) return false;
+      if (threadIdx.x == 0) {
+        ss.pi[s] = a.order[k];
+        ss.d[s] = a.pairs[ss.pi[s]];
+      }
+      __syncthreads();
+      const PairDesc& d = ss.d[s];
+      const bool staged = residues<T>(a.limbs + d.u_off, d.u_len, a.mods, d.nq, ts, stg);
+      if (residues<T>(a.limbs + d.v_off, d.v_len, a.mods, d.nq, acc2, stg) && staged) break;
+      if (threadIdx.x == 0) { a.status[ss.pi[s]] = ST_TIMEOUT; a.count[ss.pi[s]] = 0; a.iters[ss.pi[s]] = 0; }
+      __syncthreads();
+    }
+    const PairDesc& d = ss.d[s];
     uint32_t* u0 = scr + (size_t)s * 4 * NQS;
-    residues<T>(a.limbs + d.u_off, d.u_len, a.mods, d.nq, ts, chunk);
-    residues<T>(a.limbs + d.v_off, d.v_len, a.mods, d.nq, acc2, chunk);
     uint32_t h0 = 0xFFFFFFFFu, l0 = 0xFFFFFFFFu;
     for (uint32_t j = threadIdx.x; j < d.nq; j += T) {
       const ModConst c = a.mods[j];
@@ -308,12 +320,15 @@ __global__ void __launch_bounds__(T) cluster_batchk_kernel(const BatchArgs a)
   __shared__ ClusterSlotKeys<K> ck;
   __shared__ ClusterSmem cs;                          // single-slot exchanges (set-up, finish)
   __shared__ RedSmem rs;
+  __shared__ unsigned long long stage_bar[2];
+  __shared__ uint32_t stage_state;
+  const Stage stg{smem, stage_bar, &stage_state};     // dynamic shared memory starts with it
+  stage_init(stg);
   const uint32_t C = cluster_size(), r = cluster_rank();
   const uint32_t per = (a.nq_max + C - 1) / C;        // slice of every slot's moduli
   const uint32_t j0 = r * per;
-  uint32_t* const tS = smem;                          // K x per states
-  uint32_t* const acc2 = smem + (size_t)K * per;      // residues of v during set-up
-  uint32_t* const chunk = acc2 + per;
+  uint32_t* const tS = smem + STAGE_SMEM_WORDS;       // K x per states
+  uint32_t* const acc2 = tS + (size_t)K * per;        // residues of v during set-up
   uint32_t* const scr = a.scratch + (size_t)(blockIdx.x / C) * a.scratch_words;   // per slot u0, v0, hist
   const uint32_t NQS = a.nq_max;
   const int L = a.L;
@@ -327,50 +342,66 @@ __global__ void __launch_bounds__(T) cluster_batchk_kernel(const BatchArgs a)
   int32_t b[K];
 
   cluster_sync_all();
+  // Takes the next pair of the queue into slot s.  A CTA whose operands could not be staged
+  // contributes the key (0, 0) (no modulus produces it), so the whole cluster answers that
+  // pair with ST_TIMEOUT and takes the next one together.
   auto load = [&](int s) -> bool {
-    if (r == 0 && threadIdx.x < C) {
-      const uint32_t k = __shfl_sync(0xFFFFFFFFu >> (32 - C), threadIdx.x == 0 ? atomicAdd(a.queue, 1u) : 0u, 0);
-      const uint32_t ad = (uint32_t)__cvta_generic_to_shared(&ck.next);
-      uint32_t ra;
-      asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(ad), "r"(threadIdx.x));
-      asm volatile("st.shared::cluster.u32 [%0], %1;" :: "r"(ra), "r"(k) : "memory");
+    uint32_t h0, l0;
+    for (;;) {
+      if (r == 0 && threadIdx.x < C) {
+        const uint32_t k = __shfl_sync(0xFFFFFFFFu >> (32 - C), threadIdx.x == 0 ? atomicAdd(a.queue, 1u) : 0u, 0);
+        const uint32_t ad = (uint32_t)__cvta_generic_to_shared(&ck.next);
+        uint32_t ra;
+        asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(ad), "r"(threadIdx.x));
+        asm volatile("st.shared::cluster.u32 [%0], %1;" :: "r"(ra), "r"(k) : "memory");
+      }
+      cluster_sync_all();
+      const uint32_t k = ck.next;
+      cluster_sync_all();                             // everyone has read next before it changes
+      if (k >= a.npairs) return false;
+      if (threadIdx.x == 0) {
+        ss.pi[s] = a.order[k];
+        ss.d[s] = a.pairs[ss.pi[s]];
+        const uint32_t nq = ss.d[s].nq;
+        ck.nloc[s] = j0 >= nq ? 0u : (nq - j0 < per ? nq - j0 : per);
+      }
+      __syncthreads();
+      const PairDesc& d = ss.d[s];
+      const uint32_t nloc = ck.nloc[s];
+      uint32_t* ts = tS + (size_t)s * per;
+      uint32_t* u0 = scr + (size_t)s * 4 * NQS;
+      const ModConst* my = a.mods + j0;
+      const bool staged = residues<T>(a.limbs + d.u_off, d.u_len, my, nloc, ts, stg);
+      const bool ok = residues<T>(a.limbs + d.v_off, d.v_len, my, nloc, acc2, stg) && staged;
+      h0 = 0xFFFFFFFFu;
+      l0 = 0xFFFFFFFFu;
+      for (uint32_t j = threadIdx.x; j < nloc; j += T) {
+        const ModConst c = my[j];
+        const uint32_t u = ts[j], v = acc2[j];
+        u0[j0 + j] = u;
+        u0[NQS + j0 + j] = v;
+        const uint32_t t = t_init(u, v, c.q, c.qinv);
+        ts[j] = t;
+        uint32_t h, l;
+        t_key(t, c.q, h, l);
+        if (key_less(h, l, h0, l0)) { h0 = h; l0 = l; }
+      }
+      if (threadIdx.x == 32u * s) {
+        ss.lu[s] = bound_init(a.limbs + d.u_off, d.u_len);
+        ss.lv[s] = bound_init(a.limbs + d.v_off, d.v_len);
+      }
+      if (!ok) h0 = l0 = 0u;
+      block_min_key<T>(h0, l0, rs, bparity);
+      cluster_min_key<T>(h0, l0, cs, rparity, [] {});
+      if (h0 != 0u || l0 != 0u) break;
+      if (r == 0 && threadIdx.x == 0) {
+        a.status[ss.pi[s]] = ST_TIMEOUT;
+        a.count[ss.pi[s]] = 0;
+        a.iters[ss.pi[s]] = 0;
+      }
+      __syncthreads();
     }
-    cluster_sync_all();
-    const uint32_t k = ck.next;
-    cluster_sync_all();                               // everyone has read next before it changes
-    if (k >= a.npairs) return false;
-    if (threadIdx.x == 0) {
-      ss.pi[s] = a.order[k];
-      ss.d[s] = a.pairs[ss.pi[s]];
-      const uint32_t nq = ss.d[s].nq;
-      ck.nloc[s] = j0 >= nq ? 0u : (nq - j0 < per ? nq - j0 : per);
-    }
-    __syncthreads();
     const PairDesc& d = ss.d[s];
-    const uint32_t nloc = ck.nloc[s];
-    uint32_t* ts = tS + (size_t)s * per;
-    uint32_t* u0 = scr + (size_t)s * 4 * NQS;
-    const ModConst* my = a.mods + j0;
-    residues<T>(a.limbs + d.u_off, d.u_len, my, nloc, ts, chunk);
-    residues<T>(a.limbs + d.v_off, d.v_len, my, nloc, acc2, chunk);
-    uint32_t h0 = 0xFFFFFFFFu, l0 = 0xFFFFFFFFu;
-    for (uint32_t j = threadIdx.x; j < nloc; j += T) {
-      const ModConst c = my[j];
-      const uint32_t u = ts[j], v = acc2[j];
-      u0[j0 + j] = u;
-      u0[NQS + j0 + j] = v;
-      const uint32_t t = t_init(u, v, c.q, c.qinv);
-      ts[j] = t;
-      uint32_t h, l;
-      t_key(t, c.q, h, l);
-      if (key_less(h, l, h0, l0)) { h0 = h; l0 = l; }
-    }
-    if (threadIdx.x == 32u * s) {
-      ss.lu[s] = bound_init(a.limbs + d.u_off, d.u_len);
-      ss.lv[s] = bound_init(a.limbs + d.v_off, d.v_len);
-    }
-    block_min_key<T>(h0, l0, rs, bparity);
-    cluster_min_key<T>(h0, l0, cs, rparity, [] {});
     uint32_t p0;
     int32_t b0;
     key_pair(h0, l0, p0, b0);
@@ -473,16 +504,19 @@ __global__ void __launch_bounds__(T) grid_kernel(const GridArgs a)
 {
   extern __shared__ __align__(16) uint32_t smem[];
   __shared__ RedSmem rs;
+  __shared__ unsigned long long stage_bar[2];
+  __shared__ uint32_t stage_state;
+  const Stage stg{smem, stage_bar, &stage_state};     // dynamic shared memory starts with it
+  stage_init(stg);
   const uint32_t nq = a.pair.nq;
   const uint32_t j0 = blockIdx.x * a.per_cta;
   const uint32_t nloc = j0 >= nq ? 0u : (nq - j0 < a.per_cta ? nq - j0 : a.per_cta);
-  uint32_t* st = smem;
-  uint32_t* acc2 = smem + a.per_cta;
-  uint32_t* chunk = acc2 + a.per_cta;
+  uint32_t* st = smem + STAGE_SMEM_WORDS;
+  uint32_t* acc2 = st + a.per_cta;
   uint32_t* u0 = a.scratch + j0;
   uint32_t* v0 = a.scratch + nq + j0;
   int2* hist = reinterpret_cast<int2*>(a.scratch + 2 * (size_t)nq);
-  run_pair<T, SYNC_GRID>(a.limbs, a.pair, a.mods, a.L, j0, nloc, st, acc2, chunk, rs, u0, v0, hist,
+  run_pair<T, SYNC_GRID>(a.limbs, a.pair, a.mods, a.L, j0, nloc, st, acc2, stg, rs, u0, v0, hist,
                                a.sync, a.digits, a.count, a.iters, a.status, a.inv);
 }
 
@@ -495,17 +529,20 @@ __global__ void __launch_bounds__(T) cluster_kernel(const GridArgs a)
   extern __shared__ __align__(16) uint32_t smem[];
   __shared__ RedSmem rs;
   __shared__ ClusterSmem cs;
+  __shared__ unsigned long long stage_bar[2];
+  __shared__ uint32_t stage_state;
+  const Stage stg{smem, stage_bar, &stage_state};     // dynamic shared memory starts with it
+  stage_init(stg);
   const uint32_t nq = a.pair.nq;
   const uint32_t j0 = cluster_rank() * a.per_cta;
   const uint32_t nloc = j0 >= nq ? 0u : (nq - j0 < a.per_cta ? nq - j0 : a.per_cta);
-  uint32_t* st = smem;
-  uint32_t* acc2 = smem + a.per_cta;
-  uint32_t* chunk = acc2 + a.per_cta;
+  uint32_t* st = smem + STAGE_SMEM_WORDS;
+  uint32_t* acc2 = st + a.per_cta;
   uint32_t* u0 = a.scratch + j0;
   uint32_t* v0 = a.scratch + nq + j0;
   int2* hist = reinterpret_cast<int2*>(a.scratch + 2 * (size_t)nq);
   cluster_sync_all();   // every CTA of the cluster is running before remote stores begin
-  run_pair<T, SYNC_CLUSTER>(a.limbs, a.pair, a.mods, a.L, j0, nloc, st, acc2, chunk, rs, u0, v0, hist,
+  run_pair<T, SYNC_CLUSTER>(a.limbs, a.pair, a.mods, a.L, j0, nloc, st, acc2, stg, rs, u0, v0, hist,
                             reinterpret_cast<GridSync*>(&cs), a.digits, a.count, a.iters, a.status, a.inv);
   cluster_sync_all();   // no CTA leaves while others may still address its shared memory
 }
@@ -520,19 +557,22 @@ __global__ void __launch_bounds__(T) cgrid_kernel(const GridArgs a)
   extern __shared__ __align__(16) uint32_t smem[];
   __shared__ RedSmem rs;
   __shared__ CGridSmem cg;
+  __shared__ unsigned long long stage_bar[2];
+  __shared__ uint32_t stage_state;
+  const Stage stg{smem, stage_bar, &stage_state};     // dynamic shared memory starts with it
+  stage_init(stg);
   const uint32_t nq = a.pair.nq;
   const uint32_t j0 = blockIdx.x * a.per_cta;
   const uint32_t nloc = j0 >= nq ? 0u : (nq - j0 < a.per_cta ? nq - j0 : a.per_cta);
-  uint32_t* st = smem;
-  uint32_t* acc2 = smem + a.per_cta;
-  uint32_t* chunk = acc2 + a.per_cta;
+  uint32_t* st = smem + STAGE_SMEM_WORDS;
+  uint32_t* acc2 = st + a.per_cta;
   uint32_t* u0 = a.scratch + j0;
   uint32_t* v0 = a.scratch + nq + j0;
   int2* hist = reinterpret_cast<int2*>(a.scratch + 2 * (size_t)nq);
   if (threadIdx.x == 0) cg.g = a.sync;
   __syncthreads();
   cluster_sync_all();   // every CTA of the cluster is running before remote stores begin
-  run_pair<T, SYNC_CGRID>(a.limbs, a.pair, a.mods, a.L, j0, nloc, st, acc2, chunk, rs, u0, v0, hist,
+  run_pair<T, SYNC_CGRID>(a.limbs, a.pair, a.mods, a.L, j0, nloc, st, acc2, stg, rs, u0, v0, hist,
                           reinterpret_cast<GridSync*>(&cg), a.digits, a.count, a.iters, a.status, a.inv);
   cluster_sync_all();   // no CTA leaves while others may still address its shared memory
 }
@@ -549,11 +589,14 @@ __global__ void __launch_bounds__(T) cluster_batch_kernel(const BatchArgs a)
   __shared__ RedSmem rs;
   __shared__ ClusterSmem cs;
   __shared__ uint32_t next;
+  __shared__ unsigned long long stage_bar[2];
+  __shared__ uint32_t stage_state;
+  const Stage stg{smem, stage_bar, &stage_state};     // dynamic shared memory starts with it
+  stage_init(stg);
   const uint32_t C = cluster_size(), r = cluster_rank();
   const uint32_t per_max = (a.nq_max + C - 1) / C;
-  uint32_t* st = smem;
-  uint32_t* acc2 = smem + per_max;
-  uint32_t* chunk = acc2 + per_max;
+  uint32_t* st = smem + STAGE_SMEM_WORDS;
+  uint32_t* acc2 = st + per_max;
   uint32_t* scr = a.scratch + (size_t)(blockIdx.x / C) * a.scratch_words;
   cluster_sync_all();
   for (;;) {
@@ -572,7 +615,7 @@ __global__ void __launch_bounds__(T) cluster_batch_kernel(const BatchArgs a)
     const uint32_t per = (d.nq + C - 1) / C;
     const uint32_t j0 = r * per;
     const uint32_t nloc = j0 >= d.nq ? 0u : (d.nq - j0 < per ? d.nq - j0 : per);
-    run_pair<T, SYNC_CLUSTER>(a.limbs, d, a.mods, a.L, j0, nloc, st, acc2, chunk, rs, scr + j0, scr + d.nq + j0,
+    run_pair<T, SYNC_CLUSTER>(a.limbs, d, a.mods, a.L, j0, nloc, st, acc2, stg, rs, scr + j0, scr + d.nq + j0,
                               reinterpret_cast<int2*>(scr + 2 * (size_t)d.nq), reinterpret_cast<GridSync*>(&cs),
                               a.digits, a.count + pi, a.iters + pi, a.status + pi, a.inv);
     cluster_sync_all();   // every CTA is done with `next` and with the pair's scratch
@@ -646,7 +689,7 @@ cudaError_t launch_build_invtab(const ModConst* mods, uint32_t n, uint32_t* tab,
 
 size_t batch_smem_bytes(int /*threads*/, int k, uint32_t nq_max)
 {
-  return sizeof(uint32_t) * ((size_t)(k > 1 ? k + 1 : 2) * nq_max + CHUNK);
+  return sizeof(uint32_t) * ((size_t)(k > 1 ? k + 1 : 2) * nq_max + STAGE_SMEM_WORDS);
 }
 
 static const void* batch_fn_for(int threads, int k)
@@ -768,7 +811,7 @@ static const void* cluster_batch_fn_k(int threads, int k)
 size_t cluster_batch_smem_bytes(int csize, uint32_t nq_max, int k)
 {
   const size_t per = (nq_max + csize - 1) / csize;
-  return sizeof(uint32_t) * ((size_t)(k > 1 ? k + 1 : 2) * per + CHUNK);
+  return sizeof(uint32_t) * ((size_t)(k > 1 ? k + 1 : 2) * per + STAGE_SMEM_WORDS);
 }
 
 cudaError_t cluster_batch_max_clusters(int threads, int k, int csize, size_t smem, int* clusters)
@@ -840,7 +883,7 @@ cudaError_t launch_cgrid(const GridArgs& a, int threads, int csize, int clusters
 
 size_t grid_smem_bytes(uint32_t per_cta)
 {
-  return sizeof(uint32_t) * (2 * (size_t)per_cta + CHUNK);
+  return sizeof(uint32_t) * (2 * (size_t)per_cta + STAGE_SMEM_WORDS);
 }
 
 static const void* grid_fn(int threads)

@@ -354,26 +354,151 @@ __device__ __forceinline__ bool reduce_min(uint32_t& hi, uint32_t& lo, RedSmem& 
   return reduce_min<T, MODE, PUB>(hi, lo, rs, parity, gs, epoch, [] {});
 }
 
+// ---- operand staging: bulk copies (the TMA engine, cp.async.bulk) into shared memory
+//
+// Two staging buffers of STAGE_WORDS words each at a 16-byte-aligned shared address (the
+// start of the dynamic shared memory), each with an mbarrier that the copy completes.  A
+// bulk copy needs 16-byte-aligned addresses and a size that is a multiple of 16 bytes, so
+// a tile [lo, hi) of an operand is widened to the 16-byte bounds around it (at most 3
+// limbs each side) and read from its offset inside the buffer.  The widened copy stays
+// inside the limb buffer: its base is 16-byte aligned (pool allocation) and the plan pads
+// it by 16 bytes.  Every wait is bounded.
+constexpr int STAGE_WORDS = CHUNK + 8;               // one tile widened to 16-byte bounds
+constexpr int STAGE_SMEM_WORDS = 2 * STAGE_WORDS;    // two buffers (the next tile in flight)
+constexpr unsigned long long STAGE_TIMEOUT_NS = 1000000000ull;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+struct Stage {
+  uint32_t* buf;                 // 2 x STAGE_WORDS words, 16-byte aligned, shared
+  unsigned long long* mbar;      // 2 mbarriers in shared memory; nullptr: plain loads
+  uint32_t* state;               // shared: bit b = parity of buffer b's next phase;
+                                 // STAGE_BROKEN once a wait ran out
+};
+constexpr uint32_t STAGE_BROKEN = 0x80000000u;
+
+// Once per kernel, by every thread, before the first residues().
+__device__ __forceinline__ void stage_init(Stage s)
+{
+  if (s.mbar != nullptr && threadIdx.x == 0) {
+    for (int b = 0; b < 2; ++b)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(s.mbar + b)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    *s.state = 0u;
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* m, uint32_t parity)
+{
+  uint32_t ok;
+  asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+               "selp.u32 %0, 1, 0, p;\n\t}"
+               : "=r"(ok) : "r"(smem_u32(m)), "r"(parity) : "memory");
+  return ok != 0u;
+}
+
+// Waits (bounded) until phase `parity` of the mbarrier has completed.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* m, uint32_t parity)
+{
+  if (mbar_try_wait(m, parity)) return true;
+  const unsigned long long t0 = globaltimer_ns();
+  while (!mbar_try_wait(m, parity))
+    if (globaltimer_ns() - t0 > STAGE_TIMEOUT_NS) return false;
+  return true;
+}
+
+// Tile t (most significant first) of an n-limb operand: [lo, hi).
+__device__ __forceinline__ void stage_tile(int t, int n, int& lo, int& hi)
+{
+  hi = n - t * CHUNK;
+  lo = hi > CHUNK ? hi - CHUNK : 0;
+}
+
+// Thread 0: bulk copy of tile [lo, hi) of x, widened to 16-byte bounds, into buffer b.
+__device__ __forceinline__ void stage_issue(const uint32_t* x, int lo, int hi, Stage s, int b)
+{
+  const uintptr_t ga = (uintptr_t)(x + lo) & ~(uintptr_t)15;
+  const uintptr_t gb = ((uintptr_t)(x + hi) + 15) & ~(uintptr_t)15;
+  const uint32_t bytes = (uint32_t)(gb - ga);                  // <= 4 (CHUNK + 6), multiple of 16
+  const uint32_t m = smem_u32(s.mbar + b);
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(m), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               :: "r"(smem_u32(s.buf + b * STAGE_WORDS)), "l"(ga), "r"(bytes), "r"(m) : "memory");
+}
+
 // x mod q_j for the nloc moduli mods[0..nloc), into acc[] (shared).  Limbs are staged
 // most-significant tile first; Horner in Montgomery form keeps z = y * 2^-32 where y is the
-// residue of the limbs consumed so far: z' = REDC(z * (2^64 mod q) + limb).
+// residue of the limbs consumed so far: z' = REDC(z * (2^64 mod q) + limb).  Returns false
+// if a staging wait ran out (after waiting, bounded, for the copy still in flight).
 template <int T>
-__device__ void residues(const uint32_t* __restrict__ x, uint32_t n, const ModConst* __restrict__ mods,
-                         uint32_t nloc, uint32_t* __restrict__ acc, uint32_t* __restrict__ chunk)
+__device__ bool residues(const uint32_t* __restrict__ x, uint32_t n, const ModConst* __restrict__ mods,
+                         uint32_t nloc, uint32_t* __restrict__ acc, Stage stg)
 {
   for (uint32_t j = threadIdx.x; j < nloc; j += T) acc[j] = 0u;
-  for (int hi = (int)n; hi > 0; hi -= CHUNK) {
-    const int lo = hi > CHUNK ? hi - CHUNK : 0;
-    __syncthreads();
-    for (int i = lo + (int)threadIdx.x; i < hi; i += T) chunk[i - lo] = __ldg(x + i);
-    __syncthreads();
-    const int len = hi - lo;
-    for (uint32_t j = threadIdx.x; j < nloc; j += T) {
-      const ModConst c = mods[j];
-      uint32_t z = acc[j];
-      for (int i = len - 1; i >= 0; --i) z = redc((uint64_t)z * c.r2 + chunk[i], c.q, c.qinv);
-      acc[j] = z;
+  int nt = ((int)n + CHUNK - 1) / CHUNK;
+  bool ok = true;
+  if (stg.mbar == nullptr) {
+    uint32_t* const chunk = stg.buf;
+    for (int t = 0; t < nt; ++t) {
+      int lo, hi;
+      stage_tile(t, (int)n, lo, hi);
+      __syncthreads();
+      for (int i = lo + (int)threadIdx.x; i < hi; i += T) chunk[i - lo] = __ldg(x + i);
+      __syncthreads();
+      const int len = hi - lo;
+      for (uint32_t j = threadIdx.x; j < nloc; j += T) {
+        const ModConst c = mods[j];
+        uint32_t z = acc[j];
+        for (int i = len - 1; i >= 0; --i) z = redc((uint64_t)z * c.r2 + chunk[i], c.q, c.qinv);
+        acc[j] = z;
+      }
     }
+  } else {
+    __syncthreads();                   // the state word of the previous call is written
+    uint32_t phase = *stg.state;       // bit b: the parity of buffer b's next phase
+    if (phase & STAGE_BROKEN) nt = 0, ok = false;
+    __syncthreads();                   // every thread read it before thread 0 issues
+    if (threadIdx.x == 0 && nt > 0) {
+      int lo, hi;
+      stage_tile(0, (int)n, lo, hi);
+      stage_issue(x, lo, hi, stg, 0);
+    }
+    for (int t = 0; t < nt; ++t) {
+      const int b = t & 1;
+      int lo, hi;
+      stage_tile(t, (int)n, lo, hi);
+      if (threadIdx.x == 0 && t + 1 < nt) {          // the other buffer was released by the
+        int lo1, hi1;                                // barrier that ended tile t - 1
+        stage_tile(t + 1, (int)n, lo1, hi1);
+        stage_issue(x, lo1, hi1, stg, b ^ 1);
+      }
+      const bool got = mbar_wait(stg.mbar + b, (phase >> b) & 1u);
+      phase ^= 1u << b;
+      if (!__syncthreads_and(got)) {
+        // a copy did not complete: wait (bounded) for the one issued into the other buffer;
+        // the mbarrier phases are no longer known, so later calls fail at once
+        if (t + 1 < nt) mbar_wait(stg.mbar + (b ^ 1), (phase >> (b ^ 1)) & 1u);
+        ok = false;
+        phase = STAGE_BROKEN;
+        break;
+      }
+      const uint32_t* const chunk =
+          stg.buf + b * STAGE_WORDS + (uint32_t)(((uintptr_t)(x + lo) & 15) >> 2);
+      const int len = hi - lo;
+      for (uint32_t j = threadIdx.x; j < nloc; j += T) {
+        const ModConst c = mods[j];
+        uint32_t z = acc[j];
+        for (int i = len - 1; i >= 0; --i) z = redc((uint64_t)z * c.r2 + chunk[i], c.q, c.qinv);
+        acc[j] = z;
+      }
+      __syncthreads();                 // buffer b is free for tile t + 2
+    }
+    if (threadIdx.x == 0) *stg.state = phase;
   }
   __syncthreads();
   for (uint32_t j = threadIdx.x; j < nloc; j += T) {
@@ -381,6 +506,7 @@ __device__ void residues(const uint32_t* __restrict__ x, uint32_t n, const ModCo
     acc[j] = redc((uint64_t)acc[j] * c.r2, c.q, c.qinv);
   }
   __syncthreads();
+  return ok;
 }
 
 template <int T, int MODE>
@@ -392,12 +518,15 @@ __device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d
 
 // The whole gcd of one pair by this CTA (GRID = false) or by the cooperative grid, the
 // calling CTA owning global moduli [j0, j0 + nloc).
-//   st, acc2   shared arrays of nloc words; chunk: CHUNK words
+//   st, acc2   shared arrays of nloc words; stg: the operand staging buffers (stage_init done)
 //   u0g, v0g   this CTA's initial residues (global scratch, nloc words each)
 //   hist       (p, b) history, one entry per reduction iteration (global scratch, nq entries)
+// A CTA whose operands could not be staged contributes the key (0, 0), which no modulus
+// produces (it would need q = 1): the first exchange then stops every CTA of the pair
+// together and the pair is answered with ST_TIMEOUT.
 template <int T, int MODE>
 __device__ void run_pair(const uint32_t* __restrict__ limbs, const PairDesc& d, const ModConst* __restrict__ mods,
-                         int L, uint32_t j0, uint32_t nloc, uint32_t* st, uint32_t* acc2, uint32_t* chunk,
+                         int L, uint32_t j0, uint32_t nloc, uint32_t* st, uint32_t* acc2, Stage stg,
                          RedSmem& rs, uint32_t* u0g, uint32_t* v0g, int2* hist, GridSync* gs,
                          mgcd_pair* digits, uint32_t* count, uint32_t* iters_out, int32_t* status,
                          InvTab inv)
@@ -407,8 +536,8 @@ __device__ void run_pair(const uint32_t* __restrict__ limbs, const PairDesc& d, 
   uint32_t parity = 0, epoch = 0;
 
   // ---- MGCD2: residues
-  residues<T>(limbs + d.u_off, d.u_len, my, nloc, st, chunk);
-  residues<T>(limbs + d.v_off, d.v_len, my, nloc, acc2, chunk);
+  const bool staged = residues<T>(limbs + d.u_off, d.u_len, my, nloc, st, stg);
+  const bool ok = residues<T>(limbs + d.v_off, d.v_len, my, nloc, acc2, stg) && staged;
 
   uint32_t kh = 0xFFFFFFFFu, kl = 0xFFFFFFFFu;
   for (uint32_t j = threadIdx.x; j < nloc; j += T) {
@@ -422,8 +551,13 @@ __device__ void run_pair(const uint32_t* __restrict__ limbs, const PairDesc& d, 
     t_key(t, c.q, h, l);
     if (key_less(h, l, kh, kl)) { kh = h; kl = l; }
   }
+  if (!ok) kh = kl = 0u;
   if (!reduce_min<T, MODE>(kh, kl, rs, parity, gs, epoch)) {
     if (writer) *status = ST_TIMEOUT;
+    return;
+  }
+  if (kh == 0u && kl == 0u) {
+    if (writer) { *status = ST_TIMEOUT; *count = 0; }
     return;
   }
   uint32_t p;

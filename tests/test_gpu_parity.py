@@ -129,7 +129,7 @@ def test_other_modulus_widths(mgcd, oracle, L):
 
 
 def test_large_pairs_clusters_and_grid(device):
-    """Pairs too large for one CTA: single pairs on a cluster (up to 16,384 moduli) or the
+    """Pairs too large for one CTA: single pairs on a cluster (up to 8,192 moduli) or the
     cooperative grid; in a batch, on clusters from the size-class-3 queue."""
     rng = random.Random(16)
     u, v = rand_pair(rng, 65536, 16384)

@@ -13,6 +13,9 @@
 // rcp(r1) is fixed), so the estimate is allowed on the whole interval iff it is at the two
 // ends: checking both ends of every interval, for every r1, covers every (r0, r1) of the
 // phase.  Phase A: ~6e10 end points; phase C: ~1.3e8 (where the remainder is also checked).
+// inv_mod runs phase C on signed remainders; its estimate is odd in each operand (a
+// reciprocal and round-to-nearest-even products), so the positive operands checked here
+// cover the negative ones too.
 #include <cstdint>
 #include <cuda_runtime.h>
 

@@ -106,8 +106,9 @@ __device__ __forceinline__ float inv_quot_c(float f0, float f1)
 //   phase A (r1 >= 2^22): operands rounded to float, quotient < 2^10, estimate within
 //            2^-11 of r0/r1, so the rounded quotient is within 1 of it and |r| < r1;
 //   phase B (r0 >= 2^22 > r1): one exact integer division at the transition;
-//   phase C (r0, r1 < 2^22): operands exact in float, quotient < 2^22 within 1/2 of
-//            r0/r1 before rounding, remainder exact by FMA (an integer below 2^22).
+//   phase C (|r0|, |r1| < 2^22): operands exact in float, quotient below 2^22 in magnitude
+//            and within 1/2 of r0/r1 before rounding, remainder exact by FMA (an integer
+//            below 2^22 in magnitude); remainders and quotients keep their signs.
 // The bounds assume rcp.approx.ftz.f32's documented error (1 ulp).  At the end |s| < q,
 // so s is either the 32-bit value read as unsigned or that minus 2^32 (possible only for
 // q > 2^31); the candidate whose product with x is 1 is taken, and if neither is (never
@@ -132,17 +133,19 @@ __device__ __forceinline__ uint32_t inv_mod(uint32_t x, uint32_t q, uint32_t qin
       const uint32_t s = s0 - Q * s1;
       r0 = r1; r1 = r; s0 = s1; s1 = s;
     }
+    // remainders keep their sign here (quotients of either sign, read from the mantissa
+    // as two's complement), so s_k x == r_k holds without a sign fix per step
     float f0 = (float)r0, f1 = (float)r1;
     int guard = 64;
-    while (f1 > 1.0f && --guard) {
+    while (fabsf(f1) > 1.0f && --guard) {
       const float qm = inv_quot_c(f0, f1);
       const float rem = __fmaf_rn(INV_MAGIC - qm, f1, f0);   // r0 - Q r1, exact
       const uint32_t Q = __float_as_uint(qm) - INV_MAGIC_BITS;
       const uint32_t s = s0 - Q * s1;
       f0 = f1; s0 = s1;
-      f1 = fabsf(rem);
-      s1 = rem < 0.0f ? 0u - s : s;
+      f1 = rem; s1 = s;
     }
+    if (f1 < 0.0f) s1 = 0u - s1;                   // s1 x == -1
   }
   // inv * x == 1 (mod q)  <=>  redc(inv * x) == redc(1)
   const uint32_t one = redc(1ull, q, qinv);
@@ -208,14 +211,15 @@ __device__ __forceinline__ uint32_t t_update(uint32_t t, uint32_t q, uint32_t qi
 
 // The same update for K pairs that share the modulus q (slot s uses pivot (p[s], b[s]);
 // slots outside `mask` are left alone).  The K inverses are all mod q, so Montgomery's
-// trick replaces them by one: with x_s = d_s / R and prefix products P_s = x_0..x_s R^-s,
-// Z = P_{K-1}^{-1} = (x_0..x_{K-1})^{-1} R^{K-1}; walking back, mont_mul(Z, P_{s-1}) = x_s^{-1}
+// trick replaces them by one: with x_s = d_s and prefix products P_s = x_0..x_s R^-s,
+// Z = R P_{K-1}^{-1} = R^K (x_0..x_{K-1})^{-1}; walking back, mont_mul(Z, P_{s-1}) = R / x_s
 // and Z <- mont_mul(Z, x_s).  Slots that need no inverse contribute R mod q (the
-// Montgomery one).  Then t'_s = mont_mul(pm_s, x_s^{-1}) = pm_s / d_s.
+// Montgomery one).  Then t'_s = mont_mul(pm_s, R / x_s) = pm_s / d_s.
 template <int K>
-__device__ __forceinline__ void t_update_k(uint32_t (&t)[K], uint32_t q, uint32_t qinv, uint32_t r1,
-                                           const uint32_t (&p)[K], const int32_t (&b)[K], uint32_t mask)
+__device__ __forceinline__ void t_update_k(uint32_t (&t)[K], const ModConst& c, const uint32_t (&p)[K],
+                                           const int32_t (&b)[K], uint32_t mask)
 {
+  const uint32_t q = c.q, qinv = c.qinv, r1 = c.r1;
   uint32_t x[K];
   uint32_t need = 0;
 #pragma unroll
@@ -227,7 +231,7 @@ __device__ __forceinline__ void t_update_k(uint32_t (&t)[K], uint32_t q, uint32_
     if (q == p[s]) { t[s] = T_RETIRED; continue; }
     const uint32_t d = mod_sub(ts, from_signed(b[s], q), q);
     if (d == 0u) { t[s] = T_INF; continue; }
-    x[s] = redc((uint64_t)d, q, qinv);
+    x[s] = d;
     need |= 1u << s;
   }
   if (!need) return;
@@ -235,7 +239,7 @@ __device__ __forceinline__ void t_update_k(uint32_t (&t)[K], uint32_t q, uint32_
   P[0] = x[0];
 #pragma unroll
   for (int s = 1; s < K; ++s) P[s] = mont_mul(P[s - 1], x[s], q, qinv);
-  uint32_t Z = inv_mod(P[K - 1], q, qinv);
+  uint32_t Z = mont_mul(inv_mod(P[K - 1], q, qinv), c.r2, q, qinv);   // times R
 #pragma unroll
   for (int s = K - 1; s >= 1; --s) {
     const uint32_t y = mont_mul(Z, P[s - 1], q, qinv);

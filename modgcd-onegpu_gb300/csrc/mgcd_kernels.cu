@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(T, MINB) batchk_kernel(const BatchArgs a)
       }
       if (!m) continue;
       const ModConst c = a.mods[j];
-      t_update_k<K>(tv, c.q, c.qinv, c.r1, p, b, m);
+      t_update_k<K>(tv, c, p, b, m);
 #pragma unroll
       for (int s = 0; s < K; ++s) {
         if (!((m >> s) & 1u)) continue;
@@ -479,7 +479,7 @@ __global__ void __launch_bounds__(T) cluster_batchk_kernel(const BatchArgs a)
       }
       if (!m) continue;
       const ModConst c = a.mods[j0 + j];
-      t_update_k<K>(tv, c.q, c.qinv, c.r1, p, b, m);
+      t_update_k<K>(tv, c, p, b, m);
 #pragma unroll
       for (int s = 0; s < K; ++s) {
         if (!((m >> s) & 1u)) continue;

@@ -461,13 +461,14 @@ static int schedule(mgcd_context* c, Plan& P, const std::vector<PairDesc>& descs
     bk.n = (uint32_t)v.size();
     bk.nq_max = descs[v[0]].nq;
     bk.scratch_off = scratch;
-    if (!plain && (b == CLUSTER_CLASS || c->cfg[b].csize > 0)) {
+    const int small_cs = (b > 0 && b < CLUSTER_CLASS) ? P.small_cluster_ctas : 0;
+    if (!plain && (b == CLUSTER_CLASS || c->cfg[b].csize > 0 || small_cs > 0)) {
       // k pairs per cluster; more CTAs per cluster when a CTA's share of the moduli would
       // not fit its shared memory (24 KB kept for the kernel's static shared memory, which
       // holds the cluster keys and the recovery panel)
       if (b == CLUSTER_CLASS && P.cluster_k) bk.k = P.cluster_k;
       if (bk.k > 4) bk.k = 4;
-      int cs = (b == CLUSTER_CLASS && P.cluster_ctas) ? P.cluster_ctas : c->cfg[b].csize;
+      int cs = (b == CLUSTER_CLASS && P.cluster_ctas) ? P.cluster_ctas : small_cs > 0 ? small_cs : c->cfg[b].csize;
       const size_t room = c->smem_optin - 24576;
       while (cs < MAX_CLUSTER && cluster_batch_smem_bytes(cs, bk.nq_max, bk.k) > room) cs *= 2;
       cs = std::min(cs, MAX_CLUSTER);

@@ -75,6 +75,8 @@ struct Plan {
   bool plain = false;                  // single-pair latency policy
   bool graphable = true;               // may be recorded into a CUDA graph (context setting)
   int cluster_ctas = 0;                // CTAs per cluster of size class 3 (0: the context's setting)
+  int small_cluster_ctas = 0;          // CTAs per cluster for pairs of size classes 1-2 (0: the
+                                       // context's setting); serving waves favour latency
   int cluster_k = 0;                   // pairs per cluster of size class 3 (0: the context's setting)
 
   DevBuf d_limbs, d_pairs, d_order, d_digits, d_count, d_iters, d_status, d_queue, d_scratch, d_gsync, d_retry;

@@ -74,6 +74,12 @@ struct Wave {
 
 constexpr size_t MAX_TRACE = size_t(1) << 20;   // wave records kept
 constexpr int SERVE_CLUSTER_CTAS = 8;            // CTAs per cluster for class-3 requests
+// CTAs per cluster for the waves of lanes 1-2 (0: the batch table's one CTA per K pairs).
+// Measured on 1,000 mixed requests with 1 % at 1M bits, 10k / 100k req/s: table p50 6.1 /
+// 6.6 ms, p99 242 / 204 ms; lane 2 on 4-CTA clusters p50 6.3 / 6.6, p99 149 / 165; lanes 1
+// and 2 on 2- and 4-CTA clusters p99 104 / 135 but p50 up to 50 ms at 50k-100k req/s (lane 1
+// carries a third of the requests and loses throughput on clusters).
+constexpr int SERVE_LANE_CLUSTER[NLANES] = {0, 0, 4, 0};
 
 size_t strip(const uint32_t* x, size_t n)
 {
@@ -347,6 +353,7 @@ int mgcd_serve_start(mgcd_context* c, size_t budget_bytes, mgcd_server** out)
       w.plan.cluster_ctas = SERVE_CLUSTER_CTAS;
       w.plan.cluster_k = 1;
     }
+    w.plan.small_cluster_ctas = SERVE_LANE_CLUSTER[w.lane];
     if (w.plan.create(w.lane == CLUSTER_CLASS ? least : greatest) != cudaSuccess ||
         cudaEventCreateWithFlags(&w.done, cudaEventDisableTiming) != cudaSuccess)
       rc = MGCD_ERR_CUDA;

@@ -189,3 +189,38 @@ def test_cpp_dropin_driver(mgcd):
             assert '"mismatches": 0, "errors": 0' in r.stdout
     r = subprocess.run([exe, "rand", "5000", "1200", "6", "42"], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_operand_staging_alignment_and_tile_edges(mgcd, device):
+    """Operand tiles reach shared memory by bulk copies widened to 16-byte bounds: every
+    operand start modulo 4 limbs and lengths around the 1,024-limb tile edge, in the batched
+    kernels, on a cluster and on the cooperative grid, against Python's gcd."""
+    rng = random.Random(23)
+    us, vs = [], []
+    for ulimbs in (1, 3, 4, 5, 1023, 1024, 1025, 2049):
+        for gl in (0, 1):
+            u, v = rand_pair(rng, 32 * ulimbs, 16 * ulimbs * gl, max(2, 32 * ulimbs - 5))
+            us.append(u)
+            vs.append(v)
+    for shift in range(4):
+        # a gap of `shift` limbs before every operand moves its start through all four
+        # positions inside a 16-byte line
+        parts, uo, ul, vo, vl = [np.zeros(shift, dtype=np.uint32)], [], [], [], []
+        off = shift
+        for u, v in zip(us, vs):
+            a, b = mgcd.to_limbs(u), mgcd.to_limbs(v)
+            uo.append(off); ul.append(len(a)); parts.append(a); off += len(a)
+            parts.append(np.zeros(shift, dtype=np.uint32)); off += shift
+            vo.append(off); vl.append(len(b)); parts.append(b); off += len(b)
+            parts.append(np.zeros(shift, dtype=np.uint32)); off += shift
+        packed = (np.ascontiguousarray(np.concatenate(parts), dtype=np.uint32), np.array(uo, dtype=np.uint64),
+                  np.array(ul, dtype=np.uint32), np.array(vo, dtype=np.uint64), np.array(vl, dtype=np.uint32))
+        g, g_off, g_len, st = device.gcd_batch_packed(*packed)
+        assert (st == 0).all()
+        for i, (u, v) in enumerate(zip(us, vs)):
+            o = int(g_off[i])
+            assert mgcd.from_limbs(g[o:o + int(g_len[i])]) == math.gcd(u, v), (shift, i)
+    # single pairs: 1025 limbs on a cluster, 9000 limbs (~33,000 moduli) on the grid
+    for nl in (1025, 9000):
+        u, v = rand_pair(rng, 32 * nl, 8 * nl)
+        assert device.gcd(u, v) == math.gcd(u, v)

@@ -152,6 +152,13 @@ int mgcd_set_wait_timeout_ms(mgcd_context *ctx, unsigned ms);
 /* Test hook for the bounded waits: CTA `cta` of the next cooperative-grid pairs never
    publishes its minimum, so the other CTAs' waits run out (-1 turns the hook off). */
 int mgcd_test_withhold_cta(mgcd_context *ctx, int cta);
+/* Test hook for the operand-staging failure path: the CTA with block index `cta` of every
+   later kernel (batched, cluster or grid) reports that its bulk copies of the operand limbs
+   did not complete (after they did, so nothing is left in flight); every CTA of the pairs it
+   works on stops at the first exchange and those pairs fail with MGCD_ERR_TIMEOUT, while the
+   other pairs of a batch are unaffected (-1 turns the hook off).  No reference interface:
+   the reference stages limbs with plain loads. */
+int mgcd_test_fail_staging(mgcd_context *ctx, int cta);
 /* Test hook for the "ran out of moduli" paths: every following pair uses exactly nq
    moduli (a multiple of 256; 0 restores the reference's count) and is not rerun. */
 int mgcd_test_force_moduli(mgcd_context *ctx, unsigned nq);

@@ -66,6 +66,7 @@ SIGNATURES = {
     "mgcd_set_single_pair_policy": (_c.c_int, [_P, _c.c_int]),
     "mgcd_set_wait_timeout_ms": (_c.c_int, [_P, _c.c_uint]),
     "mgcd_test_withhold_cta": (_c.c_int, [_P, _c.c_int]),
+    "mgcd_test_fail_staging": (_c.c_int, [_P, _c.c_int]),
     "mgcd_test_force_moduli": (_c.c_int, [_P, _c.c_uint]),
     "mgcd_get_size_class": (_c.c_int, [_P, _c.c_int, _c.POINTER(_c.c_int), _c.POINTER(_c.c_int),
                                        _c.POINTER(_c.c_float)]),
@@ -367,6 +368,10 @@ class Device:
     def test_withhold_cta(self, cta):
         """Test hook: CTA `cta` of grid-mode pairs never publishes (-1: off)."""
         _check(self._lib.mgcd_test_withhold_cta(self._h, int(cta)))
+
+    def test_fail_staging(self, cta):
+        """Test hook: CTA `cta` of later kernels reports an operand-staging failure (-1: off)."""
+        _check(self._lib.mgcd_test_fail_staging(self._h, int(cta)))
 
     def test_force_moduli(self, nq):
         """Test hook: every pair uses exactly nq moduli, no rerun (0: reference count)."""

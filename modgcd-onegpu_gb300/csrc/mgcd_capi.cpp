@@ -511,6 +511,7 @@ static int launch_set(mgcd_context* c, Plan& P, const std::vector<Bucket>& bucke
   for (size_t b = 0; b < buckets.size(); ++b) {
     const Bucket& bk = buckets[b];
     BatchArgs a;
+    a.stage_fail = c->stage_fail_cta;
     a.inv = InvTab{c->d_invtab.as<uint32_t>(), c->invtab_n};
     a.limbs = P.d_limbs.as<uint32_t>();
     a.pairs = pairs;
@@ -541,6 +542,7 @@ static int launch_set(mgcd_context* c, Plan& P, const std::vector<Bucket>& bucke
   for (uint32_t k : grid_pairs) {
     const PairDesc& d = descs[k];
     GridArgs g;
+    g.stage_fail = c->stage_fail_cta;
     g.inv = InvTab{c->d_invtab.as<uint32_t>(), c->invtab_n};
     g.limbs = P.d_limbs.as<uint32_t>();
     g.pair = d;
@@ -1024,6 +1026,15 @@ int mgcd_test_withhold_cta(mgcd_context* c, int cta)
 {
   if (!c) return MGCD_ERR_INVALID_ARG;
   c->withhold_cta = cta < 0 ? 0xFFFFFFFFu : (uint32_t)cta;
+  cudaStreamSynchronize(c->main.stream);
+  c->main.drop_graph();
+  return MGCD_OK;
+}
+
+int mgcd_test_fail_staging(mgcd_context* c, int cta)
+{
+  if (!c) return MGCD_ERR_INVALID_ARG;
+  c->stage_fail_cta = cta < 0 ? 0xFFFFFFFFu : (uint32_t)cta;
   cudaStreamSynchronize(c->main.stream);
   c->main.drop_graph();
   return MGCD_OK;

@@ -65,6 +65,7 @@ struct BatchArgs {
   uint32_t* count;           // digits per pair
   uint32_t* iters;           // reduction iterations per pair (work accounting)
   int32_t* status;
+  uint32_t stage_fail;       // test hook: this CTA reports an operand-staging failure (~0: none)
 };
 
 // State of the cross-CTA reduction used by a single pair spread over a cooperative grid.
@@ -101,6 +102,7 @@ struct GridArgs {
   uint32_t* count;
   uint32_t* iters;
   int32_t* status;
+  uint32_t stage_fail;       // test hook: this CTA reports an operand-staging failure (~0: none)
 };
 
 // Launch helpers (mgcd_kernels.cu).

@@ -35,7 +35,7 @@ __global__ void __launch_bounds__(T) batch_kernel(const BatchArgs a)
   __shared__ uint32_t next;
   __shared__ unsigned long long stage_bar[2];
   __shared__ uint32_t stage_state;
-  const Stage stg{smem, stage_bar, &stage_state};     // dynamic shared memory starts with it
+  const Stage stg{smem, stage_bar, &stage_state, blockIdx.x == a.stage_fail};   // at dynamic smem start
   stage_init(stg);
   uint32_t* st = smem + STAGE_SMEM_WORDS;
   uint32_t* acc2 = st + a.nq_max;
@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(T, MINB) batchk_kernel(const BatchArgs a)
   __shared__ uint32_t next;
   __shared__ unsigned long long stage_bar[2];
   __shared__ uint32_t stage_state;
-  const Stage stg{smem, stage_bar, &stage_state};     // dynamic shared memory starts with it
+  const Stage stg{smem, stage_bar, &stage_state, blockIdx.x == a.stage_fail};   // at dynamic smem start
   stage_init(stg);
   const uint32_t NQS = a.nq_max;
   uint32_t* const tS = smem + STAGE_SMEM_WORDS;       // K x NQS states
@@ -322,7 +322,7 @@ __global__ void __launch_bounds__(T) cluster_batchk_kernel(const BatchArgs a)
   __shared__ RedSmem rs;
   __shared__ unsigned long long stage_bar[2];
   __shared__ uint32_t stage_state;
-  const Stage stg{smem, stage_bar, &stage_state};     // dynamic shared memory starts with it
+  const Stage stg{smem, stage_bar, &stage_state, blockIdx.x == a.stage_fail};   // at dynamic smem start
   stage_init(stg);
   const uint32_t C = cluster_size(), r = cluster_rank();
   const uint32_t per = (a.nq_max + C - 1) / C;        // slice of every slot's moduli
@@ -506,7 +506,7 @@ __global__ void __launch_bounds__(T) grid_kernel(const GridArgs a)
   __shared__ RedSmem rs;
   __shared__ unsigned long long stage_bar[2];
   __shared__ uint32_t stage_state;
-  const Stage stg{smem, stage_bar, &stage_state};     // dynamic shared memory starts with it
+  const Stage stg{smem, stage_bar, &stage_state, blockIdx.x == a.stage_fail};   // at dynamic smem start
   stage_init(stg);
   const uint32_t nq = a.pair.nq;
   const uint32_t j0 = blockIdx.x * a.per_cta;
@@ -531,7 +531,7 @@ __global__ void __launch_bounds__(T) cluster_kernel(const GridArgs a)
   __shared__ ClusterSmem cs;
   __shared__ unsigned long long stage_bar[2];
   __shared__ uint32_t stage_state;
-  const Stage stg{smem, stage_bar, &stage_state};     // dynamic shared memory starts with it
+  const Stage stg{smem, stage_bar, &stage_state, blockIdx.x == a.stage_fail};   // at dynamic smem start
   stage_init(stg);
   const uint32_t nq = a.pair.nq;
   const uint32_t j0 = cluster_rank() * a.per_cta;
@@ -559,7 +559,7 @@ __global__ void __launch_bounds__(T) cgrid_kernel(const GridArgs a)
   __shared__ CGridSmem cg;
   __shared__ unsigned long long stage_bar[2];
   __shared__ uint32_t stage_state;
-  const Stage stg{smem, stage_bar, &stage_state};     // dynamic shared memory starts with it
+  const Stage stg{smem, stage_bar, &stage_state, blockIdx.x == a.stage_fail};   // at dynamic smem start
   stage_init(stg);
   const uint32_t nq = a.pair.nq;
   const uint32_t j0 = blockIdx.x * a.per_cta;
@@ -591,7 +591,7 @@ __global__ void __launch_bounds__(T) cluster_batch_kernel(const BatchArgs a)
   __shared__ uint32_t next;
   __shared__ unsigned long long stage_bar[2];
   __shared__ uint32_t stage_state;
-  const Stage stg{smem, stage_bar, &stage_state};     // dynamic shared memory starts with it
+  const Stage stg{smem, stage_bar, &stage_state, blockIdx.x == a.stage_fail};   // at dynamic smem start
   stage_init(stg);
   const uint32_t C = cluster_size(), r = cluster_rank();
   const uint32_t per_max = (a.nq_max + C - 1) / C;

@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(NA_THREADS) noalloc_kernel(const NaArgs a)
   uint32_t* v0 = a.scratch + NA_MAX_NQ;
   int2* hist = reinterpret_cast<int2*>(a.scratch + 2 * (size_t)NA_MAX_NQ);
   // caller-owned operand buffers carry no padding for widened bulk copies: plain loads
-  const Stage stg{smem + 2 * NA_MAX_NQ, nullptr, nullptr};
+  const Stage stg{smem + 2 * NA_MAX_NQ, nullptr, nullptr, 0u};
   run_pair<NA_THREADS, SYNC_CTA>(a.limbs, d, a.mods, NA_L, 0u, d.nq, smem, smem + NA_MAX_NQ, stg,
                               rs, u0, v0, hist, nullptr, a.digits, a.count, &iters, a.status, InvTab{nullptr, 0u});
   if (threadIdx.x == 0) {

@@ -377,6 +377,7 @@ struct Stage {
   unsigned long long* mbar;      // 2 mbarriers in shared memory; nullptr: plain loads
   uint32_t* state;               // shared: bit b = parity of buffer b's next phase;
                                  // STAGE_BROKEN once a wait ran out
+  uint32_t inject;               // test hook: report a failure after staging normally
 };
 constexpr uint32_t STAGE_BROKEN = 0x80000000u;
 
@@ -500,6 +501,7 @@ __device__ bool residues(const uint32_t* __restrict__ x, uint32_t n, const ModCo
     }
     if (threadIdx.x == 0) *stg.state = phase;
   }
+  if (stg.inject) ok = false;
   __syncthreads();
   for (uint32_t j = threadIdx.x; j < nloc; j += T) {
     const ModConst c = mods[j];

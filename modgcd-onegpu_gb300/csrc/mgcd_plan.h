@@ -119,6 +119,7 @@ struct mgcd_context {
   int single_policy = MGCD_SINGLE_AUTO;  // launch shape of pairs that span several CTAs
   unsigned long long wait_timeout_ns = 2000000000ull;   // bound of every cross-CTA wait
   uint32_t withhold_cta = 0xFFFFFFFFu;                  // test hook (mgcd_test_withhold_cta)
+  uint32_t stage_fail_cta = 0xFFFFFFFFu;                // test hook (mgcd_test_fail_staging)
   uint32_t force_nq = 0;                                // test hook (mgcd_test_force_moduli)
 };
 

@@ -3,6 +3,10 @@
 - A bounded wait that runs out: one CTA of a cooperative-grid pair withholds its
   publication (a flag nothing sets); the other CTAs give up after the bound, the pair fails
   with MGCD_ERR_TIMEOUT, and the same context then computes correctly.
+- Operand staging that fails (host-set hook, reported after the bulk copies completed):
+  every CTA of an affected pair stops at the first exchange -- on one CTA, a cluster and the
+  cooperative grid -- the pair fails with MGCD_ERR_TIMEOUT, the other pairs of a batch are
+  exact, and the context then computes correctly.
 - Too few moduli (host-side injection): every pair is forced onto a moduli count that cannot
   hold it.  The reference's own check (sizes tracked with __ffs) misses such cases and its
   kernel can return a wrong gcd; here the result is certified on the device, so the call
@@ -60,3 +64,31 @@ def test_too_few_moduli_never_returns_a_wrong_gcd(mgcd, nbits, forced):
                 assert r == math.gcd(a, b)
         dev.test_force_moduli(0)
         assert dev.gcd(u, v) == math.gcd(u, v)
+
+
+def test_staging_failure_stops_pair_and_context_survives(mgcd):
+    rng = random.Random(32)
+    small = [_pair(rng, nb, nb // 4) for nb in (2000, 3000, 9000, 30000) for _ in range(40)]
+    big = [_pair(rng, 300000, 40000) for _ in range(2)]            # size class 3: clusters
+    cluster_pair = _pair(rng, 60000, 9000)                          # single pair, cluster
+    grid_pair = _pair(rng, 420000, 60000)                           # single pair, grid
+    with mgcd.Device(0, 32) as dev:
+        dev.set_wait_timeout_ms(200)
+        dev.test_fail_staging(1)
+        for u, v in (cluster_pair, grid_pair):
+            with pytest.raises(mgcd.GcdError) as e:
+                dev.gcd(u, v)
+            assert mgcd.STATUS_NAMES[e.value.status] == "MGCD_ERR_TIMEOUT"
+        us = [u for u, _ in small + big]
+        vs = [v for _, v in small + big]
+        res, st = dev.gcd_batch(us, vs, return_status=True)
+        names = {mgcd.STATUS_NAMES[int(x)] for x in st}
+        assert names <= {"MGCD_OK", "MGCD_ERR_TIMEOUT"}
+        assert "MGCD_ERR_TIMEOUT" in names                       # CTA 1 took some pairs
+        for (u, v), r, x in zip(small + big, res, st):
+            if mgcd.STATUS_NAMES[int(x)] == "MGCD_OK":
+                assert r == math.gcd(u, v)
+        dev.test_fail_staging(-1)
+        for u, v in (cluster_pair, grid_pair):
+            assert dev.gcd(u, v) == math.gcd(u, v)
+        assert dev.gcd_batch(us, vs) == [math.gcd(u, v) for u, v in zip(us, vs)]

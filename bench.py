@@ -3,7 +3,8 @@
 
 Workload (default): the mixed batch -- 4096 pairs, operand bit lengths log-uniform in
 [1k, 64k], bits(v) = bits(u)/U(1, 2), 25% coprime, 5% v | u, 70% planted gcds of U[0, 50%] of
-the smaller operand, 32-bit moduli -- seeded synthetic data (workloads.mixed_batch).
+the smaller operand -- seeded synthetic data (workloads.mixed_batch), at the modulus width
+whose tuned table runs the whole batch fastest (tuning/gb300_width.txt, --modulus-bits).
 
 A step is the gcd of every pair of the batch.
   value     GCDs/s with the batch resident on the device: CUDA events on the library's
@@ -41,6 +42,9 @@ TRAFFIC_FILE = os.path.join(ROOT, "profiles", "ncu_traffic.json")
 # reduction-loop update 257 (two inverses of ~19 quotient steps x 6 ops + 3 modmul + 2 modsub
 # in the reference's formulation), recovery update 124.
 OPS_RESIDUE, OPS_EUCLID, OPS_RECOVERY = 9.0, 257.0, 124.0
+# Modulus width of the serving workloads: its 1M-bit requests run faster at 32 bits
+# (84,736 moduli) than at 27 (90,624), and they bound the served throughput.
+SERVE_BITS = 32
 
 
 def parse():
@@ -60,6 +64,11 @@ def parse():
                     help="arrival rates (req/s) of the serving leg; --workload serve defaults to the full sweep")
     ap.add_argument("--serve-requests", type=int, default=1000)
     ap.add_argument("--tuning", default=None, help="tuning table (default: the package's table for this GPU)")
+    ap.add_argument("--modulus-bits", type=int, default=None,
+                    help="modulus width of the batched workload (default: the width with the fastest whole "
+                         "batch, tuning/gb300_width.txt, written by tune.py --compare-widths) and of "
+                         "--workload serve (default 32); the skewed workload uses 32-bit moduli as its "
+                         "configuration states")
     return ap.parse_args()
 
 
@@ -232,7 +241,8 @@ def run_reference(args, rank, pg):
         "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": {"workload": "mixed batch: %d pairs, bits log-uniform [1k,64k], 25%% coprime, 5%% v|u, "
-                               "70%% planted gcd U[0,50%%]" % args.pairs, "modulus_bits": 32},
+                               "70%% planted gcd U[0,50%%]" % args.pairs,
+                   "modulus_bits": args.modulus_bits or importlib.import_module("modgcd-onegpu_gb300").tuned_width()},
         "cpu_baseline": {"value": v, "unit": "GCDs/s", "cores": nthreads, "kind": "reference",
                          "sample": "GMP %s mpz_gcd (the reference's -DNO_GPU path, testmodgcd.cpp:441) over all "
                                    "%d pairs per step, %d threads" % (po.gmp_version(), args.pairs, nthreads)},
@@ -256,7 +266,8 @@ def run_ours(args, rank, local, world, pg):
     # expected results: GMP mpz_gcd (also the CPU baseline on rank 0)
     cpu_times, gx, gxo, gxn = gmp_baseline(po, packed, nthreads, args.cpu_reps if rank == 0 else 1)
 
-    dev = mg.Device(local, 32)
+    L = args.modulus_bits or mg.tuned_width()
+    dev = mg.Device(local, L)
     tuning = apply_tuning(dev, args.tuning or mg.default_tuning_path(dev))
     int_peak = dev.int_peak()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")   # > L2 (129 MB)
@@ -321,7 +332,14 @@ def run_ours(args, rank, local, world, pg):
 
     # ---- serving: Poisson arrivals through the request server
     rates = [float(r) for r in args.serve_rates.split(",") if r]
-    serve_rows, serve_stats = serve_leg(mg, wl, po, dev, rates, args.serve_requests, nthreads) if rates else ([], {})
+    serve_rows, serve_stats = [], {}
+    if rates:
+        # serving runs 32-bit moduli: its 1M-bit requests take 1.4 s there and 2.5 s at 27 bits
+        sdev = dev if L == SERVE_BITS else mg.Device(local, SERVE_BITS)
+        apply_tuning(sdev, mg.default_tuning_path(sdev))
+        serve_rows, serve_stats = serve_leg(mg, wl, po, sdev, rates, args.serve_requests, nthreads)
+        if sdev is not dev:
+            sdev.close()
 
     if rank != 0:
         return
@@ -343,7 +361,7 @@ def run_ours(args, rank, local, world, pg):
     traffic = None   # DRAM bytes of one step, scaled from an ncu capture of the same kernels
     try:
         with open(TRAFFIC_FILE) as f:
-            traffic = json.load(f)["bytes_per_pair"] * n
+            traffic = json.load(f)["by_modulus_bits"][str(L)]["bytes_per_pair"] * n
     except (OSError, ValueError, KeyError):
         pass
     line = {
@@ -353,7 +371,7 @@ def run_ours(args, rank, local, world, pg):
         "dtype": "u32", "data": "synthetic",
         "config": {"workload": "mixed batch: %d pairs, bits log-uniform [1k,64k], bits(v)=bits(u)/U(1,2), "
                                "25%% coprime, 5%% v|u, 70%% planted gcd U[0,50%%] of the smaller" % n,
-                   "modulus_bits": 32, "parallelism": "replicas" if world > 1 else "single",
+                   "modulus_bits": L, "parallelism": "replicas" if world > 1 else "single",
                    "l2": "flushed before every step (256 MB write)"},
         "bit_exact": ok_dev and ok_e2e and ok_plain and all(r["bit_exact"] for r in serve_rows),
         "e2e": {"value": n * world * args.steps / e2e_s, "unit": "GCDs/s",
@@ -364,7 +382,7 @@ def run_ours(args, rank, local, world, pg):
         "batch_latency_ms": {"p50": statistics.median(run_ms), "max": max(run_ms)},
         "serving": {"rows": serve_rows, "server": serve_stats,
                     "workload": "mixed 1k-64k-bit sizes + 1% 1M-bit, Poisson arrivals, 8 GB admission budget",
-                    "bit_exact": all(r["bit_exact"] for r in serve_rows)},
+                    "modulus_bits": SERVE_BITS, "bit_exact": all(r["bit_exact"] for r in serve_rows)},
         "tuning": tuning,
         "roofline": {"bound": "int", "achieved": achieved / 1e9, "peak": int_peak / 1e9, "unit": "Gop/s",
                      "frac": achieved / int_peak, "traffic": traffic,
@@ -454,7 +472,7 @@ def run_serve(args, rank, local):
     import pyoracle as po
     mg = importlib.import_module("modgcd-onegpu_gb300")
     wl = importlib.import_module("modgcd-onegpu_gb300.workloads")
-    dev = mg.Device(local, 32)
+    dev = mg.Device(local, args.modulus_bits or SERVE_BITS)
     tuning = apply_tuning(dev, args.tuning or mg.default_tuning_path(dev))
     rates = [float(r) for r in (args.serve_rates if args.serve_rates != "10000" else
                                 "1000,10000,50000,100000,200000").split(",")]

@@ -191,6 +191,17 @@ def default_tuning_path(dev):
     return os.path.join(TUNING_DIR, "gb300_L%d.txt" % dev.L)
 
 
+def tuned_width(default=32):
+    """Modulus width with the fastest whole mixed batch on GB300 (tune.py --compare-widths
+    writes tuning/gb300_width.txt); `default` when no comparison was recorded."""
+    try:
+        with open(os.path.join(TUNING_DIR, "gb300_width.txt")) as f:
+            L = int(f.readline().split()[0])
+        return L if L in (22, 27, 32) else default
+    except (OSError, ValueError, IndexError):
+        return default
+
+
 def device_count():
     n = ctypes.c_int()
     _check(load().mgcd_device_count(ctypes.byref(n)))

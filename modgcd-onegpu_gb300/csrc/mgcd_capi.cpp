@@ -485,7 +485,8 @@ static int schedule(mgcd_context* c, Plan& P, const std::vector<PairDesc>& descs
       while (bk.k > 1 && batch_smem_bytes(bk.threads, bk.k, bk.nq_max) > c->smem_optin - 16384) bk.k /= 2;
       bk.smem = batch_smem_bytes(bk.threads, bk.k, bk.nq_max);
       int bps = 0;
-      if (batch_max_blocks_per_sm(bk.threads, bk.k, bk.smem, &bps) != cudaSuccess || bps < 1) return MGCD_ERR_GRID;
+      if (batch_max_blocks_per_sm(bk.threads, bk.k, c->L <= 30, bk.smem, &bps) != cudaSuccess || bps < 1)
+        return MGCD_ERR_GRID;
       bk.grid = (int)std::min<size_t>((v.size() + bk.k - 1) / bk.k, (size_t)c->sms * bps);
       scratch += (size_t)bk.grid * 4 * bk.k * bk.nq_max;
     }

@@ -249,6 +249,59 @@ __device__ __forceinline__ void t_update_k(uint32_t (&t)[K], const ModConst& c, 
   if (need & 1u) t[0] = mont_mul(p[0] > q ? p[0] - q : p[0], Z, q, qinv);
 }
 
+// Moduli below 2^30 (widths up to 30 bits): 4q < R, so the REDC of a product of two
+// operands below 2q is below 2q again without the final subtraction ((T + m q)/R < T/R + q
+// and T < 4q^2 < qR), and every sum fits 32 bits.  Values kept "lazy" in [0, 2q) only
+// where no comparison, key or inverse reads them.
+__device__ __forceinline__ uint32_t mont_mul_lazy(uint32_t a, uint32_t b, uint32_t q, uint32_t qinv)
+{
+  const uint64_t T = (uint64_t)a * b;
+  const uint32_t lo = (uint32_t)T, hi = (uint32_t)(T >> 32);
+  return hi + __umulhi(lo * qinv, q) + (lo != 0u);      // < 2q < 2^31
+}
+
+// [0, 2q) -> [0, q): x - q wraps to a large value when x < q.
+__device__ __forceinline__ uint32_t mod_canon(uint32_t x, uint32_t q)
+{
+  return min(x, x - q);
+}
+
+// t_update_k for moduli below 2^30: the prefix products, the scaled inverse and the walk
+// back stay lazy; the inverse's input and the new states are canonical.
+template <int K>
+__device__ __forceinline__ void t_update_k_narrow(uint32_t (&t)[K], const ModConst& c, const uint32_t (&p)[K],
+                                                  const int32_t (&b)[K], uint32_t mask)
+{
+  const uint32_t q = c.q, qinv = c.qinv, r1 = c.r1;
+  uint32_t x[K];
+  uint32_t need = 0;
+#pragma unroll
+  for (int s = 0; s < K; ++s) {
+    x[s] = r1;
+    if (!((mask >> s) & 1u)) continue;
+    const uint32_t ts = t[s];
+    if (ts >= T_MARK) { t[s] = (ts == T_INF) ? 0u : ts; continue; }
+    if (q == p[s]) { t[s] = T_RETIRED; continue; }
+    const uint32_t d = mod_sub(ts, from_signed(b[s], q), q);
+    if (d == 0u) { t[s] = T_INF; continue; }
+    x[s] = d;
+    need |= 1u << s;
+  }
+  if (!need) return;
+  uint32_t P[K];
+  P[0] = x[0];
+#pragma unroll
+  for (int s = 1; s < K; ++s) P[s] = mont_mul_lazy(P[s - 1], x[s], q, qinv);
+  uint32_t Z = mont_mul_lazy(inv_mod(mod_canon(P[K - 1], q), q, qinv), c.r2, q, qinv);   // times R
+#pragma unroll
+  for (int s = K - 1; s >= 1; --s) {
+    const uint32_t y = mont_mul_lazy(Z, P[s - 1], q, qinv);
+    Z = mont_mul_lazy(Z, x[s], q, qinv);
+    if ((need >> s) & 1u) t[s] = mod_canon(mont_mul_lazy(p[s] > q ? p[s] - q : p[s], y, q, qinv), q);
+  }
+  if (need & 1u) t[0] = mod_canon(mont_mul_lazy(p[0] > q ? p[0] - q : p[0], Z, q, qinv), q);
+}
+
 // Size bounds of the reduction loop, for certifying its result: lu >= log2|u_i| and
 // lv >= log2|v_i| in fixed point (BOUND_ONE = 1 bit), stepped by
 // |v_{i+1}| <= (|u_i| + |b| |v_i|) / p.  Integer arithmetic except for the logarithms

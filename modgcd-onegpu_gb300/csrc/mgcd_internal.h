@@ -107,9 +107,10 @@ struct GridArgs {
 
 // Launch helpers (mgcd_kernels.cu).
 // k = pairs per CTA run in lockstep (1: batch_kernel; 2, 4: batchk_kernel).  Scratch per
-// CTA: 4 * k * nq_max words.
+// CTA: 4 * k * nq_max words.  Moduli below 2^30 (a.L <= 30; `narrow` for the occupancy
+// query) select the kernels with lazily reduced Montgomery products.
 size_t batch_smem_bytes(int threads, int k, uint32_t nq_max);
-cudaError_t batch_max_blocks_per_sm(int threads, int k, size_t smem, int* blocks);
+cudaError_t batch_max_blocks_per_sm(int threads, int k, bool narrow, size_t smem, int* blocks);
 cudaError_t launch_batch(const BatchArgs& a, int threads, int k, int grid, size_t smem, cudaStream_t s);
 
 // One pair on a cluster of `ctas` CTAs (<= 16) of `threads` threads; same arguments and

@@ -116,8 +116,9 @@ __device__ __forceinline__ void put(V (&a)[K], int s, V v)
     if (t == s) a[t] = v;
 }
 
-template <int T, int K, int MINB = 1>
-__global__ void __launch_bounds__(T, MINB) batchk_kernel(const BatchArgs a)
+// NARROW: moduli below 2^30 (widths up to 30 bits), lazily reduced Montgomery products.
+template <int T, int K, bool NARROW = false>
+__global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
 {
   extern __shared__ __align__(16) uint32_t smem[];
   __shared__ SlotSmem<K> ss;
@@ -255,7 +256,8 @@ __global__ void __launch_bounds__(T, MINB) batchk_kernel(const BatchArgs a)
       }
       if (!m) continue;
       const ModConst c = a.mods[j];
-      t_update_k<K>(tv, c, p, b, m);
+      if constexpr (NARROW) t_update_k_narrow<K>(tv, c, p, b, m);
+      else t_update_k<K>(tv, c, p, b, m);
 #pragma unroll
       for (int s = 0; s < K; ++s) {
         if (!((m >> s) & 1u)) continue;
@@ -692,7 +694,31 @@ size_t batch_smem_bytes(int /*threads*/, int k, uint32_t nq_max)
   return sizeof(uint32_t) * ((size_t)(k > 1 ? k + 1 : 2) * nq_max + STAGE_SMEM_WORDS);
 }
 
-static const void* batch_fn_for(int threads, int k)
+template <bool NARROW>
+static const void* batchk_fn_for(int threads, int k)
+{
+  if (k == 2) {
+    switch (threads) {
+      case 256: return reinterpret_cast<const void*>(&batchk_kernel<256, 2, NARROW>);
+      case 512: return reinterpret_cast<const void*>(&batchk_kernel<512, 2, NARROW>);
+      case 1024: return reinterpret_cast<const void*>(&batchk_kernel<1024, 2, NARROW>);
+      default: return nullptr;
+    }
+  }
+  if (k == 4) {
+    switch (threads) {
+      case 256: return reinterpret_cast<const void*>(&batchk_kernel<256, 4, NARROW>);
+      case 512: return reinterpret_cast<const void*>(&batchk_kernel<512, 4, NARROW>);
+      case 1024: return reinterpret_cast<const void*>(&batchk_kernel<1024, 4, NARROW>);   // 64 registers, 32 warps/SM
+      default: return nullptr;
+    }
+  }
+  if (k == 8 && threads == 512) return reinterpret_cast<const void*>(&batchk_kernel<512, 8, NARROW>);
+  return nullptr;
+}
+
+// narrow: the context's moduli are below 2^30 (width <= 30)
+static const void* batch_fn_for(int threads, int k, bool narrow)
 {
   if (k == 1) {
     switch (threads) {
@@ -702,29 +728,12 @@ static const void* batch_fn_for(int threads, int k)
       default: return nullptr;
     }
   }
-  if (k == 2) {
-    switch (threads) {
-      case 256: return reinterpret_cast<const void*>(&batchk_kernel<256, 2>);
-      case 512: return reinterpret_cast<const void*>(&batchk_kernel<512, 2>);
-      case 1024: return reinterpret_cast<const void*>(&batchk_kernel<1024, 2>);
-      default: return nullptr;
-    }
-  }
-  if (k == 4) {
-    switch (threads) {
-      case 256: return reinterpret_cast<const void*>(&batchk_kernel<256, 4>);
-      case 512: return reinterpret_cast<const void*>(&batchk_kernel<512, 4>);
-      case 1024: return reinterpret_cast<const void*>(&batchk_kernel<1024, 4>);   // 64 registers, 32 warps/SM
-      default: return nullptr;
-    }
-  }
-  if (k == 8 && threads == 512) return reinterpret_cast<const void*>(&batchk_kernel<512, 8>);
-  return nullptr;
+  return narrow ? batchk_fn_for<true>(threads, k) : batchk_fn_for<false>(threads, k);
 }
 
-cudaError_t batch_max_blocks_per_sm(int threads, int k, size_t smem, int* blocks)
+cudaError_t batch_max_blocks_per_sm(int threads, int k, bool narrow, size_t smem, int* blocks)
 {
-  const void* fn = batch_fn_for(threads, k);
+  const void* fn = batch_fn_for(threads, k, narrow);
   if (!fn) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -733,7 +742,7 @@ cudaError_t batch_max_blocks_per_sm(int threads, int k, size_t smem, int* blocks
 
 cudaError_t launch_batch(const BatchArgs& a, int threads, int k, int grid, size_t smem, cudaStream_t s)
 {
-  const void* fn = batch_fn_for(threads, k);
+  const void* fn = batch_fn_for(threads, k, a.L <= 30);
   if (!fn) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;

@@ -55,9 +55,31 @@ def time_config(dev, packed, exp, reps):
     return statistics.median(ms[1:])
 
 
+def compare_widths(args):
+    """Times the whole mixed batch at each modulus width with that width's tuning table and
+    writes the fastest width to tuning/gb300_width.txt (read by mg.tuned_width())."""
+    us, vs, _ = wl.mixed_batch(args.pairs, seed=args.seed)
+    packed = mg.pack_pairs(us, vs)
+    exp = [math.gcd(u, v) for u, v in zip(us, vs)]
+    res = {}
+    for L in (32, 27, 22):
+        with mg.Device(0, L) as dev:
+            dev.load_tuning(os.path.join(HERE, "tuning", "gb300_L%d.txt" % L))
+            res[L] = time_config(dev, packed, exp, args.reps)
+            print(json.dumps({"L": L, "ms": res[L]}), flush=True)
+    best = min(res, key=res.get)
+    out = args.out or os.path.join(HERE, "tuning", "gb300_width.txt")
+    with open(out, "w") as f:
+        f.write("%d\n# modulus width with the fastest whole mixed batch (%d pairs, seed %d): %s\n" %
+                (best, args.pairs, args.seed, ", ".join("L=%d %.1f ms" % (L, res[L]) for L in sorted(res))))
+    print(open(out).read())
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--L", type=int, default=32)
+    ap.add_argument("--compare-widths", action="store_true",
+                    help="time the mixed batch at every width with its table; write tuning/gb300_width.txt")
     ap.add_argument("--pairs", type=int, default=4096)
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--big-pairs", type=int, default=24)
@@ -66,6 +88,9 @@ def main():
     ap.add_argument("--out", default=None)
     ap.add_argument("--log", default=None)
     args = ap.parse_args()
+    if args.compare_widths:
+        compare_widths(args)
+        return
 
     us, vs, _ = wl.mixed_batch(args.pairs, seed=args.seed)
     by = {c: ([], []) for c in range(4)}

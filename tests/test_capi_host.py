@@ -105,3 +105,25 @@ def test_reference_testmodgcd_compiles_against_dropin(mgcd, tmp_path):
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     assert os.path.exists(exe)
+
+
+def test_tuning_tables_width_choice_and_traffic_record(mgcd):
+    """The committed tuning artifacts the benchmark reads: one table per modulus width in the
+    loader's format (class threads k nq_scale cluster_ctas, '#' comments), the width choice,
+    and an ncu traffic figure for every width the batched benchmark can run."""
+    import json
+    tdir = os.path.join(os.path.dirname(mgcd.__file__), "tuning")
+    for L in (22, 27, 32):
+        rows = [ln.split() for ln in open(os.path.join(tdir, "gb300_L%d.txt" % L))
+                if ln.strip() and not ln.lstrip().startswith("#")]
+        assert sorted(int(r[0]) for r in rows) == [0, 1, 2, 3]
+        for cls, threads, k, scale, cs in rows:
+            assert int(threads) in (256, 512, 1024) and int(k) in (1, 2, 4, 8)
+            assert 0.5 <= float(scale) <= 1.0 and int(cs) in (0, 2, 4, 8, 16)
+    assert mgcd.tuned_width() in (22, 27, 32)
+    root = os.path.dirname(os.path.dirname(os.path.abspath(mgcd.__file__)))
+    traffic = json.load(open(os.path.join(root, "profiles", "ncu_traffic.json")))["by_modulus_bits"]
+    assert str(mgcd.tuned_width()) in traffic and "32" in traffic
+    for rec in traffic.values():
+        assert abs(rec["bytes_per_pair"] - rec["dram_bytes"] / rec["pairs"]) < 1
+        assert os.path.exists(os.path.join(root, "profiles", rec["source"]))

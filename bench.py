@@ -374,6 +374,9 @@ def run_ours(args, rank, local, world, pg):
                    "modulus_bits": L, "parallelism": "replicas" if world > 1 else "single",
                    "l2": "flushed before every step (256 MB write)"},
         "bit_exact": ok_dev and ok_e2e and ok_plain and all(r["bit_exact"] for r in serve_rows),
+        # operand bits (both operands of every pair) per second, device-resident and end to end
+        "operand_bits_per_s": {"value": 8.0 * alg_bytes * world * args.steps / tot_s,
+                               "e2e": 8.0 * alg_bytes * world * args.steps / e2e_s},
         "e2e": {"value": n * world * args.steps / e2e_s, "unit": "GCDs/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "plain": {"value": plain_rate, "unit": "GCDs/s", "sample_pairs": len(idx),

@@ -155,8 +155,8 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
       }
       __syncthreads();
       const PairDesc& d = ss.d[s];
-      const bool staged = residues<T>(a.limbs + d.u_off, d.u_len, a.mods, d.nq, ts, stg);
-      if (residues<T>(a.limbs + d.v_off, d.v_len, a.mods, d.nq, acc2, stg) && staged) break;
+      const bool staged = residues<T>(a.limbs + d.u_off, d.u_len, a.mods, d.nq, ts, stg, NARROW);
+      if (residues<T>(a.limbs + d.v_off, d.v_len, a.mods, d.nq, acc2, stg, NARROW) && staged) break;
       if (threadIdx.x == 0) { a.status[ss.pi[s]] = ST_TIMEOUT; a.count[ss.pi[s]] = 0; a.iters[ss.pi[s]] = 0; }
       __syncthreads();
     }
@@ -373,8 +373,8 @@ __global__ void __launch_bounds__(T) cluster_batchk_kernel(const BatchArgs a)
       uint32_t* ts = tS + (size_t)s * per;
       uint32_t* u0 = scr + (size_t)s * 4 * NQS;
       const ModConst* my = a.mods + j0;
-      const bool staged = residues<T>(a.limbs + d.u_off, d.u_len, my, nloc, ts, stg);
-      const bool ok = residues<T>(a.limbs + d.v_off, d.v_len, my, nloc, acc2, stg) && staged;
+      const bool staged = residues<T>(a.limbs + d.u_off, d.u_len, my, nloc, ts, stg, L <= 30);
+      const bool ok = residues<T>(a.limbs + d.v_off, d.v_len, my, nloc, acc2, stg, L <= 30) && staged;
       h0 = 0xFFFFFFFFu;
       l0 = 0xFFFFFFFFu;
       for (uint32_t j = threadIdx.x; j < nloc; j += T) {

@@ -432,13 +432,32 @@ __device__ __forceinline__ void stage_issue(const uint32_t* x, int lo, int hi, S
                :: "r"(smem_u32(s.buf + b * STAGE_WORDS)), "l"(ga), "r"(bytes), "r"(m) : "memory");
 }
 
+// One tile of Horner steps z' = REDC(z * (2^64 mod q) + limb), most significant limb last
+// in `chunk`.  narrow (moduli below 2^30): z stays lazily in [0, 2q) in 32-bit arithmetic
+// (z * r2 + limb < 2q^2 + 2^32 < q 2^32, so REDC without the final subtraction is below 2q).
+__device__ __forceinline__ uint32_t horner_tile(uint32_t z, const uint32_t* chunk, int len, const ModConst& c,
+                                                bool narrow)
+{
+  if (narrow) {
+    for (int i = len - 1; i >= 0; --i) {
+      const uint64_t t = (uint64_t)z * c.r2 + chunk[i];
+      const uint32_t lo = (uint32_t)t, hi = (uint32_t)(t >> 32);
+      z = hi + __umulhi(lo * c.qinv, c.q) + (lo != 0u);
+    }
+  } else {
+    for (int i = len - 1; i >= 0; --i) z = redc((uint64_t)z * c.r2 + chunk[i], c.q, c.qinv);
+  }
+  return z;
+}
+
 // x mod q_j for the nloc moduli mods[0..nloc), into acc[] (shared).  Limbs are staged
 // most-significant tile first; Horner in Montgomery form keeps z = y * 2^-32 where y is the
-// residue of the limbs consumed so far: z' = REDC(z * (2^64 mod q) + limb).  Returns false
-// if a staging wait ran out (after waiting, bounded, for the copy still in flight).
+// residue of the limbs consumed so far: z' = REDC(z * (2^64 mod q) + limb).  narrow: the
+// moduli are below 2^30 (z lazy until the final conversion, which is canonical).  Returns
+// false if a staging wait ran out (after waiting, bounded, for the copy still in flight).
 template <int T>
 __device__ bool residues(const uint32_t* __restrict__ x, uint32_t n, const ModConst* __restrict__ mods,
-                         uint32_t nloc, uint32_t* __restrict__ acc, Stage stg)
+                         uint32_t nloc, uint32_t* __restrict__ acc, Stage stg, bool narrow)
 {
   for (uint32_t j = threadIdx.x; j < nloc; j += T) acc[j] = 0u;
   int nt = ((int)n + CHUNK - 1) / CHUNK;
@@ -452,12 +471,7 @@ __device__ bool residues(const uint32_t* __restrict__ x, uint32_t n, const ModCo
       for (int i = lo + (int)threadIdx.x; i < hi; i += T) chunk[i - lo] = __ldg(x + i);
       __syncthreads();
       const int len = hi - lo;
-      for (uint32_t j = threadIdx.x; j < nloc; j += T) {
-        const ModConst c = mods[j];
-        uint32_t z = acc[j];
-        for (int i = len - 1; i >= 0; --i) z = redc((uint64_t)z * c.r2 + chunk[i], c.q, c.qinv);
-        acc[j] = z;
-      }
+      for (uint32_t j = threadIdx.x; j < nloc; j += T) acc[j] = horner_tile(acc[j], chunk, len, mods[j], narrow);
     }
   } else {
     __syncthreads();                   // the state word of the previous call is written
@@ -491,12 +505,7 @@ __device__ bool residues(const uint32_t* __restrict__ x, uint32_t n, const ModCo
       const uint32_t* const chunk =
           stg.buf + b * STAGE_WORDS + (uint32_t)(((uintptr_t)(x + lo) & 15) >> 2);
       const int len = hi - lo;
-      for (uint32_t j = threadIdx.x; j < nloc; j += T) {
-        const ModConst c = mods[j];
-        uint32_t z = acc[j];
-        for (int i = len - 1; i >= 0; --i) z = redc((uint64_t)z * c.r2 + chunk[i], c.q, c.qinv);
-        acc[j] = z;
-      }
+      for (uint32_t j = threadIdx.x; j < nloc; j += T) acc[j] = horner_tile(acc[j], chunk, len, mods[j], narrow);
       __syncthreads();                 // buffer b is free for tile t + 2
     }
     if (threadIdx.x == 0) *stg.state = phase;
@@ -538,8 +547,8 @@ __device__ void run_pair(const uint32_t* __restrict__ limbs, const PairDesc& d, 
   uint32_t parity = 0, epoch = 0;
 
   // ---- MGCD2: residues
-  const bool staged = residues<T>(limbs + d.u_off, d.u_len, my, nloc, st, stg);
-  const bool ok = residues<T>(limbs + d.v_off, d.v_len, my, nloc, acc2, stg) && staged;
+  const bool staged = residues<T>(limbs + d.u_off, d.u_len, my, nloc, st, stg, L <= 30);
+  const bool ok = residues<T>(limbs + d.v_off, d.v_len, my, nloc, acc2, stg, L <= 30) && staged;
 
   uint32_t kh = 0xFFFFFFFFu, kl = 0xFFFFFFFFu;
   for (uint32_t j = threadIdx.x; j < nloc; j += T) {

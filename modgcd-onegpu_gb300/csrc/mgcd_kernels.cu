@@ -1,19 +1,23 @@
 // mgcd_kernels.cu -- the modular GCD kernels for sm_103a.
 //
-// One gcd pair is processed by one CTA (batched, persistent kernel pulling pairs from a
-// size-ordered queue) or, when its moduli do not fit one CTA, by a cooperative grid.
+// One gcd pair is processed by one CTA (batched, persistent kernels pulling pairs from a
+// size-ordered queue, K pairs per CTA in lockstep), or, when its moduli do not fit one CTA,
+// by a thread-block cluster or a cooperative grid.
 // Stages, with the reference's labels (GmpCudaDevice-getGcdKernel.cu:342-444):
-//   MGCD2  residues of u and v for every modulus: limb tiles staged in shared memory,
-//          Montgomery Horner per modulus (z <- REDC(z * 2^64 mod q + limb));
+//   MGCD2  residues of u and v for every modulus: limb tiles brought into shared memory by
+//          bulk copies (cp.async.bulk, double-buffered), Montgomery Horner per modulus
+//          (z <- REDC(z * 2^64 mod q + limb));
 //   MGCD3  reduction loop: per modulus only t = u/v mod q is kept; each iteration picks
 //          the pivot (p, b) = argmin of the reference's key (|t|, q - sign) with warp
-//          redux.sync minima and one barrier, then updates t' = p / (t - b) (one modular
-//          inverse per update; the reference needs two) and records (p, b);
+//          redux.sync minima and one barrier (plus a DSMEM or grid exchange across CTAs),
+//          then updates t' = p / (t - b) (one modular inverse per update, shared by the K
+//          pairs of a CTA; the reference needs two per pair) and records (p, b);
 //   replay the surviving moduli rebuild u mod q by applying the recorded (p, b) sequence
 //          to their initial residues projectively (three Montgomery products per step, no
 //          inverse) and dividing out the accumulated scale once;
 //   MGCD4  recovery: signed mixed-radix digits, next digit from the lowest-indexed
-//          modulus with a nonzero value, exactly as the reference selects it.
+//          modulus with a nonzero value, exactly as the reference selects it (in panels of
+//          up to 32 digits when the pair spans several CTAs).
 // The (p, b) sequence and the digits are identical to the reference algorithm's.
 #include <cstdint>
 #include <cstdlib>

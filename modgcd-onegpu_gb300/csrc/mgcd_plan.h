@@ -46,7 +46,8 @@ struct Bucket {
 };
 
 // Size classes of the batched path, one persistent kernel (and stream) each: pairs with at
-// most 1,024 / 4,096 / 16,384 moduli run one per CTA; larger pairs one per cluster.
+// most 1,024 / 4,096 / 16,384 moduli run K per CTA (or K per small cluster, when the class
+// or a serving lane asks for one); larger pairs K per thread-block cluster.
 constexpr int NSTREAMS = MGCD_NUM_SIZE_CLASSES;
 constexpr int CLUSTER_CLASS = 3;
 constexpr uint32_t CTA_MAX_NQ = 16384;

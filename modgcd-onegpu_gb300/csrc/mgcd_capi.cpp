@@ -370,11 +370,13 @@ int mgcd::plan_batch(mgcd_context* c, Plan& P, size_t np, const uint32_t* limbs,
       continue;
     }
     // Batches may use fewer moduli than the reference formula (less work per iteration);
-    // a pair whose result cannot then be certified is rerun with the reference count.
+    // a pair whose result cannot then be certified is rerun with the reference count.  The
+    // scaled count is rounded up to a warp (32): rounding to the reference's 256 undid the
+    // scale for pairs below ~16k bits (reference counts of 512-2,048).
     int nq = ref_nq;
     const float scale = c->cfg[size_class(ref_nq)].nq_scale;
     if (!plain && scale < 1.0f)
-      nq = std::min(ref_nq, std::max(256, ((int)std::ceil(scale * ref_nq) + 255) / 256 * 256));
+      nq = std::min(ref_nq, std::max(256, ((int)std::ceil(scale * ref_nq) + 31) / 32 * 32));
     d.nq = (uint32_t)nq;
     d.out_off = out_off;
     if ((uint64_t)out_off + (uint64_t)ref_nq + 1 > 0xFFFFFFFFull) return MGCD_ERR_CAPACITY;   // digit slots of one batch

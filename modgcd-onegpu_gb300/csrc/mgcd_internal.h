@@ -15,7 +15,8 @@ struct ModConst;
 struct PairDesc {
   uint64_t u_off, v_off;
   uint32_t u_len, v_len;
-  uint32_t nq;       // moduli used (multiple of 256)
+  uint32_t nq;       // moduli used (the reference's count, a multiple of 256, or a scaled
+                     // count rounded up to a multiple of 32)
   uint32_t out_off;  // first digit slot in the digit array; nq + 1 slots are reserved
   uint64_t g_off;    // first limb of the binary gcd in the result-limb array
   uint32_t g_cap;    // limbs reserved there (the smaller operand's length)

@@ -1,6 +1,6 @@
 /*  modgcd_oracle.c -- CPU restatement of the reference modular-GCD path.
 
-    TEST INFRASTRUCTURE ONLY.  This file is the checker: tests, the smoke check and the
+    TEST INFRASTRUCTURE ONLY.  This file is the oracle: tests, the smoke check and the
     CPU-baseline leg of the benchmark load it to verify the CUDA path.  The product never
     links or calls it.
 

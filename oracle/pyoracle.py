@@ -1,4 +1,4 @@
-"""Python binding of the checker (test infrastructure only).
+"""Python binding of the oracle (test infrastructure only).
 
 Loads ``liboracle.so`` (the C restatement of the reference algorithm) and
 ``libcpugmp.so`` (GMP ``mpz_gcd`` over a batch on the host cores).  Only the tests,
@@ -29,7 +29,7 @@ _gmp = None
 
 
 def build():
-    """Compile the checker libraries (``make -C oracle``)."""
+    """Compile the oracle libraries (``make -C oracle``)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
 
 

@@ -18,7 +18,7 @@ def pytest_configure(config):
 
 
 def _built():
-    """Builds the library and the checker once per session (cheap when up to date)."""
+    """Builds the library and the oracle once per session (cheap when up to date)."""
     pkg = importlib.import_module(PKG_NAME)
     pkg.build()
     import pyoracle

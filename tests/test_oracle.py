@@ -1,4 +1,4 @@
-"""The checker pinned before it is trusted: moduli against the reference's createModuli
+"""The oracle pinned before it is trusted: moduli against the reference's createModuli
 output, the restated algorithm against GMP mpz_gcd on the reference driver's own inputs."""
 import hashlib
 import math

@@ -281,6 +281,7 @@ def run_ours(args, rank, local, world, pg):
     ok_dev = bool((st == 0).all()) and results_equal(mg, g, go, gn, gx, gxo, gxn)
     work = dev.batch_work()
     launches = dev.batch_launches()
+    retried = dev.batch_retried()     # pairs rerun with the reference moduli count in a step
 
     clocks = Clocks(local)
     barrier(pg)
@@ -400,6 +401,7 @@ def run_ours(args, rank, local, world, pg):
                              "frac": alg_bytes / run_s / 1e9 / peaks.get("hbm_gbs", 6800.0),
                              "peak_source": peaks_kind}},
         "work": work,
+        "rerun_pairs_per_step": retried,
         "longest_kernel_ms": statistics.mean(dom_ms), "longest_kernel_threads": dom_t,
         "cpu_baseline": {"value": n / min(cpu_times), "unit": "GCDs/s", "cores": nthreads, "kind": "reference",
                          "sample": "GMP %s mpz_gcd over the same %d pairs, best of %d, %d threads" %

@@ -18,6 +18,7 @@ timed alone on 300k-bit pairs.  Every time is the median of `reps` runs and ever
 is checked against Python's gcd.
 
   python modgcd-onegpu_gb300/tune.py [--out PATH] [--log PATH] [--L 32]
+  python modgcd-onegpu_gb300/tune.py --refine --L 27 --seed 11   (finer moduli fraction)
 """
 import argparse
 import importlib
@@ -75,11 +76,50 @@ def compare_widths(args):
     print(open(out).read())
 
 
+REFINE_STEPS = (-0.08, -0.06, -0.04, -0.02, 0.0, 0.02, 0.04, 0.06, 0.08)
+
+
+def refine(args):
+    """Second pass over a width's table: the moduli fraction of classes 2, 1, 0 on a finer
+    grid (steps of 0.02 around the table's value), every other setting held, on the whole
+    mixed batch.  The fraction trades work per iteration against reruns, and the time has a
+    sharp edge below the best value, which the first pass's 0.1 grid brackets only loosely."""
+    us, vs, _ = wl.mixed_batch(args.pairs, seed=args.seed)
+    packed = mg.pack_pairs(us, vs)
+    exp = [math.gcd(u, v) for u, v in zip(us, vs)]
+    path = os.path.join(HERE, "tuning", "gb300_L%d.txt" % args.L)
+    log, best = [], {}
+    with mg.Device(0, args.L) as dev:
+        dev.load_tuning(path)
+        for c in (2, 1, 0):
+            t, k, s0 = dev.get_size_class(c)
+            for d in REFINE_STEPS:
+                s = round(s0 + d, 3)
+                if not 0.5 <= s <= 1.0:
+                    continue
+                dev.set_size_class(c, t, k, s)
+                ms = time_config(dev, packed, exp, args.reps)
+                log.append({"class": c, "threads": t, "k": k, "nq_scale": s, "cluster": dev.get_class_cluster(c),
+                            "ms": ms, "retried": dev.batch_retried()})
+                print(json.dumps(log[-1]), flush=True)
+                if c not in best or ms < best[c][0]:
+                    best[c] = (ms, s)
+            dev.set_size_class(c, t, k, best[c][1])
+        out = args.out or path
+        dev.save_tuning(out)
+    if args.log:
+        with open(args.log, "w") as f:
+            json.dump({"best": {str(c): b for c, b in best.items()}, "runs": log, "seed": args.seed}, f, indent=1)
+    print(open(out).read())
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--L", type=int, default=32)
     ap.add_argument("--compare-widths", action="store_true",
                     help="time the mixed batch at every width with its table; write tuning/gb300_width.txt")
+    ap.add_argument("--refine", action="store_true",
+                    help="finer moduli-fraction pass over the width's table (classes 0-2)")
     ap.add_argument("--pairs", type=int, default=4096)
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--big-pairs", type=int, default=24)
@@ -90,6 +130,9 @@ def main():
     args = ap.parse_args()
     if args.compare_widths:
         compare_widths(args)
+        return
+    if args.refine:
+        refine(args)
         return
 
     us, vs, _ = wl.mixed_batch(args.pairs, seed=args.seed)

@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--serve-rates", default="10000",
                     help="arrival rates (req/s) of the serving leg; --workload serve defaults to the full sweep")
     ap.add_argument("--serve-requests", type=int, default=1000)
+    ap.add_argument("--serve-sat-requests", type=int, default=8192,
+                    help="requests of the serving saturation replay (1k-64k bits at 1M req/s; 0: none)")
     ap.add_argument("--tuning", default=None, help="tuning table (default: the package's table for this GPU)")
     ap.add_argument("--modulus-bits", type=int, default=None,
                     help="modulus width of the batched workload (default: the width with the fastest whole "
@@ -167,16 +169,17 @@ def results_equal(mg, g1, o1, n1, g2, o2, n2):
     return True
 
 
-def serve_leg(mg, wl, po, dev, rates, n_req, nthreads, seed=5):
+def serve_leg(mg, wl, po, dev, rates, n_req, nthreads, seed=5, sat_requests=0):
     """Open-loop serving: n_req requests (mixed 1k-64k-bit sizes plus 1% 1M-bit), Poisson
     arrivals at each rate, through the request server (mgcd_serve_replay, C ABI); latency
-    = scheduled arrival -> answer.  Results checked against GMP."""
+    = scheduled arrival -> answer.  With sat_requests, one more replay of that many 1k-64k-bit
+    requests arriving at 1M req/s (the server's throughput).  Results checked against GMP."""
     import numpy as np
     us, vs, arr1 = wl.serve_requests(n_req, 1.0, seed=seed)
     packed = mg.pack_pairs(us, vs)
     _, gx, gxo, gxn = po.cpu_gmp_gcd_batch(*packed, nthreads)
     big = np.array([max(u.bit_length(), v.bit_length()) > (1 << 19) for u, v in zip(us, vs)])
-    rows = []
+    rows, sat = [], None
     with mg.Server(dev, budget_bytes=8 << 30) as srv:
         # untimed warm-up at 10x the highest rate: every lane's plans, pool blocks and pinned
         # buffers reach their working size before the first measured replay
@@ -205,8 +208,22 @@ def serve_leg(mg, wl, po, dev, rates, n_req, nthreads, seed=5):
                             "max_ms_1M": float(ms[big].max())})
             rows.append(row)
             print(json.dumps(row), file=sys.stderr, flush=True)
+        if sat_requests:
+            # saturation: mixed 1k-64k-bit requests only, all arriving within a few ms, so
+            # the served rate is the server's throughput (comparable with the plain method's)
+            su, sv, sarr = wl.serve_requests(sat_requests, 1e6, seed=seed + 1, big_frac=0.0)
+            spk = mg.pack_pairs(su, sv)
+            _, sx, sxo, sxn = po.cpu_gmp_gcd_batch(*spk, nthreads)
+            srv.replay_packed(*spk, np.asarray(sarr))            # untimed: plans reach their size
+            g, go, gn, st, lat, mk = srv.replay_packed(*spk, np.asarray(sarr))
+            ms = lat * 1e3
+            sat = {"rate_req_s": 1e6, "requests": sat_requests, "sizes": "mixed 1k-64k bits, no 1M-bit requests",
+                   "gcds_per_s": sat_requests / mk, "makespan_s": mk,
+                   "p50_ms": float(np.percentile(ms, 50)), "p99_ms": float(np.percentile(ms, 99)),
+                   "bit_exact": bool((st == 0).all()) and results_equal(mg, g, go, gn, sx, sxo, sxn)}
+            print(json.dumps(sat), file=sys.stderr, flush=True)
         stats = srv.stats()
-    return rows, stats
+    return rows, stats, sat
 
 
 def apply_tuning(dev, path):
@@ -333,12 +350,13 @@ def run_ours(args, rank, local, world, pg):
 
     # ---- serving: Poisson arrivals through the request server
     rates = [float(r) for r in args.serve_rates.split(",") if r]
-    serve_rows, serve_stats = [], {}
+    serve_rows, serve_stats, serve_sat = [], {}, None
     if rates:
         # serving runs 32-bit moduli: its 1M-bit requests take 1.4 s there and 2.5 s at 27 bits
         sdev = dev if L == SERVE_BITS else mg.Device(local, SERVE_BITS)
         apply_tuning(sdev, mg.default_tuning_path(sdev))
-        serve_rows, serve_stats = serve_leg(mg, wl, po, sdev, rates, args.serve_requests, nthreads)
+        serve_rows, serve_stats, serve_sat = serve_leg(mg, wl, po, sdev, rates, args.serve_requests, nthreads,
+                                                       sat_requests=args.serve_sat_requests)
         if sdev is not dev:
             sdev.close()
 
@@ -374,7 +392,8 @@ def run_ours(args, rank, local, world, pg):
                                "25%% coprime, 5%% v|u, 70%% planted gcd U[0,50%%] of the smaller" % n,
                    "modulus_bits": L, "parallelism": "replicas" if world > 1 else "single",
                    "l2": "flushed before every step (256 MB write)"},
-        "bit_exact": ok_dev and ok_e2e and ok_plain and all(r["bit_exact"] for r in serve_rows),
+        "bit_exact": ok_dev and ok_e2e and ok_plain and all(r["bit_exact"] for r in serve_rows) and
+                     (serve_sat is None or serve_sat["bit_exact"]),
         # operand bits (both operands of every pair) per second, device-resident and end to end
         "operand_bits_per_s": {"value": 8.0 * alg_bytes * world * args.steps / tot_s,
                                "e2e": 8.0 * alg_bytes * world * args.steps / e2e_s},
@@ -386,7 +405,10 @@ def run_ours(args, rank, local, world, pg):
         "batch_latency_ms": {"p50": statistics.median(run_ms), "max": max(run_ms)},
         "serving": {"rows": serve_rows, "server": serve_stats,
                     "workload": "mixed 1k-64k-bit sizes + 1% 1M-bit, Poisson arrivals, 8 GB admission budget",
-                    "modulus_bits": SERVE_BITS, "bit_exact": all(r["bit_exact"] for r in serve_rows)},
+                    "modulus_bits": SERVE_BITS,
+                    "saturation": serve_sat,
+                    "saturation_over_plain": (serve_sat["gcds_per_s"] / plain_rate) if serve_sat else None,
+                    "bit_exact": all(r["bit_exact"] for r in serve_rows) and (serve_sat is None or serve_sat["bit_exact"])},
         "tuning": tuning,
         "roofline": {"bound": "int", "achieved": achieved / 1e9, "peak": int_peak / 1e9, "unit": "Gop/s",
                      "frac": achieved / int_peak, "traffic": traffic,
@@ -481,11 +503,13 @@ def run_serve(args, rank, local):
     tuning = apply_tuning(dev, args.tuning or mg.default_tuning_path(dev))
     rates = [float(r) for r in (args.serve_rates if args.serve_rates != "10000" else
                                 "1000,10000,50000,100000,200000").split(",")]
-    rows, stats = serve_leg(mg, wl, po, dev, rates, args.serve_requests, os.cpu_count() or 1)
+    rows, stats, sat = serve_leg(mg, wl, po, dev, rates, args.serve_requests, os.cpu_count() or 1,
+                                 sat_requests=args.serve_sat_requests)
     print(json.dumps({"metric": "served GCDs/s and p50/p99 latency (enqueue -> result)", "unit": "GCDs/s, ms",
                       "data": "synthetic", "workload": "mixed 1k-64k-bit + 1% 1M-bit requests, Poisson arrivals, "
-                      "8 GB admission budget", "tuning": tuning, "rows": rows, "server": stats,
-                      "bit_exact": all(r["bit_exact"] for r in rows)}), flush=True)
+                      "8 GB admission budget", "tuning": tuning, "rows": rows, "saturation": sat, "server": stats,
+                      "bit_exact": all(r["bit_exact"] for r in rows) and (sat is None or sat["bit_exact"])}),
+          flush=True)
 
 
 def run_skewed(args, rank, local):

@@ -78,7 +78,8 @@ constexpr int SERVE_CLUSTER_CTAS = 8;            // CTAs per cluster for class-3
 // Measured on 1,000 mixed requests with 1 % at 1M bits, 10k / 100k req/s: table p50 6.1 /
 // 6.6 ms, p99 242 / 204 ms; lane 2 on 4-CTA clusters p50 6.3 / 6.6, p99 149 / 165; lanes 1
 // and 2 on 2- and 4-CTA clusters p99 104 / 135 but p50 up to 50 ms at 50k-100k req/s (lane 1
-// carries a third of the requests and loses throughput on clusters).
+// carries a third of the requests and loses throughput on clusters).  Applied to waves
+// whose clusters fit the GPU at once (start_wave); larger waves use the batch table.
 constexpr int SERVE_LANE_CLUSTER[NLANES] = {0, 0, 4, 0};
 
 size_t strip(const uint32_t* x, size_t n)
@@ -128,6 +129,10 @@ int start_wave(mgcd_server* S, Wave& w)
     w.vl[i] = r->vl;
     off += r->ul + r->vl;
   }
+  // Small clusters (latency) for a wave whose clusters fit the GPU in one round; a larger
+  // wave is throughput bound and takes the batch table's one CTA per K pairs.
+  const int lc = SERVE_LANE_CLUSTER[w.lane];
+  w.plan.small_cluster_ctas = (lc > 0 && n * (size_t)lc <= (size_t)c->sms * (size_t)c->cfg[w.lane].k) ? lc : 0;
   int rc = plan_batch(c, w.plan, n, h, w.uo.data(), w.ul.data(), w.vo.data(), w.vl.data(), false);
   if (rc == MGCD_OK) rc = run_plan(c, w.plan);
   if (rc == MGCD_OK && cudaEventRecord(w.done, w.plan.stream) != cudaSuccess) rc = MGCD_ERR_CUDA;
@@ -353,7 +358,6 @@ int mgcd_serve_start(mgcd_context* c, size_t budget_bytes, mgcd_server** out)
       w.plan.cluster_ctas = SERVE_CLUSTER_CTAS;
       w.plan.cluster_k = 1;
     }
-    w.plan.small_cluster_ctas = SERVE_LANE_CLUSTER[w.lane];
     if (w.plan.create(w.lane == CLUSTER_CLASS ? least : greatest) != cudaSuccess ||
         cudaEventCreateWithFlags(&w.done, cudaEventDisableTiming) != cudaSuccess)
       rc = MGCD_ERR_CUDA;

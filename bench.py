@@ -17,6 +17,10 @@ Every result is compared bit for bit with GMP mpz_gcd.
 
 --impl reference times the reference's CPU computation of the same batch: GMP mpz_gcd
 (testmodgcd.cpp:441, the -DNO_GPU build) on all host cores.
+
+Other workloads (--workload): sweep (single-pair latency by size and modulus width), skewed
+(64 x 1M-bit + 16,384 small pairs in one graph launch), serve (Poisson arrival sweep and a
+saturation replay), table1 (single pairs in the setting of the reference paper's Table 1).
 """
 import argparse
 import importlib
@@ -57,7 +61,7 @@ def parse():
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--plain-sample", type=int, default=64)
     ap.add_argument("--cpu-reps", type=int, default=10)
-    ap.add_argument("--workload", choices=["mixed", "sweep", "serve", "skewed"], default="mixed")
+    ap.add_argument("--workload", choices=["mixed", "sweep", "serve", "skewed", "table1"], default="mixed")
     ap.add_argument("--sizes", default="4096,16384,65536,262144,1048576")
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--serve-rates", default="10000",
@@ -547,6 +551,48 @@ def run_skewed(args, rank, local):
                                        "sample": "GMP mpz_gcd over the whole batch"}}), flush=True)
 
 
+# The reference paper's Table 1 (Weber & Brew, p.6): Tesla V100 mean wall time per call (ms),
+# random pairs with a ~1-bit gcd, 32-bit moduli, by input size in Kibit.
+PAPER_V100_MS = {16: 7, 32: 13, 64: 25, 128: 46, 192: 73, 256: 118, 352: 184}
+
+
+def run_table1(args, rank, local):
+    """Single-pair latency in the setting of the reference paper's Table 1: 10 random pairs
+    per size (planted gcd of 1 bit, i.e. random operands), 32-bit moduli, one pair per call,
+    mean wall time per call with the context set up beforehand; beside it the paper's V100
+    figure and GMP mpz_gcd on one host core (the paper's CPU column)."""
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    mg = importlib.import_module("modgcd-onegpu_gb300")
+    wl = importlib.import_module("modgcd-onegpu_gb300.workloads")
+    dev = mg.Device(local, 32)
+    rows = []
+    for kib, v100 in sorted(PAPER_V100_MS.items()):
+        pairs = [wl.size_sweep_pair(kib * 1024 + 1, seed=s, gcd_frac=0.0) for s in range(1, 11)]
+        packed = mg.pack_pairs([u for u, _ in pairs], [v for _, v in pairs])
+        gmp_s = po.cpu_gmp_gcd_batch(*packed, 1, want_results=False)[0]
+        dev.gcd(*pairs[0])                      # warm-up: plan buffers at this size
+        wall, dev_ms, ok = [], [], True
+        for u, v in pairs:
+            t0 = time.perf_counter()
+            g = dev.gcd(u, v)
+            wall.append(1e3 * (time.perf_counter() - t0))
+            dev_ms.append(dev.batch_elapsed_ms()[0])
+            ok = ok and g == math.gcd(u, v)
+        rows.append({"kibit": kib, "pairs": len(pairs), "mean_wall_ms": statistics.mean(wall),
+                     "mean_device_ms": statistics.mean(dev_ms), "paper_v100_ms": v100,
+                     "v100_over_gb300": v100 / statistics.mean(wall), "gmp_1core_ms": 1e3 * gmp_s / len(pairs),
+                     "bit_exact": bool(ok)})
+        print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
+    dev.close()
+    print(json.dumps({"metric": "single-pair gcd latency, the reference paper's Table 1 setting", "unit": "ms",
+                      "higher_is_better": False, "data": "synthetic (random pairs, seeds 1-10)",
+                      "config": {"modulus_bits": 32, "method": "plain (one pair per call)"},
+                      "rows": rows, "bit_exact": all(r["bit_exact"] for r in rows)}), flush=True)
+
+
 def main():
     args = parse()
     rank, local, world, pg = dist()
@@ -556,6 +602,8 @@ def main():
         run_serve(args, rank, local)
     elif args.workload == "skewed":
         run_skewed(args, rank, local)
+    elif args.workload == "table1":
+        run_table1(args, rank, local)
     elif args.impl == "reference":
         run_reference(args, rank, pg)
     else:

@@ -241,6 +241,14 @@ def apply_tuning(dev, path):
     return path if rel.startswith("..") else rel
 
 
+def mixed_config(n, L, world):
+    """The `config` object of the mixed-batch line, the same in both arms."""
+    return {"workload": "mixed batch: %d pairs, bits log-uniform [1k,64k], bits(v)=bits(u)/U(1,2), "
+                        "25%% coprime, 5%% v|u, 70%% planted gcd U[0,50%%] of the smaller" % n,
+            "modulus_bits": L, "parallelism": "replicas" if world > 1 else "single",
+            "l2": "flushed before every step (256 MB write)"}
+
+
 def run_reference(args, rank, pg):
     if rank != 0:
         return
@@ -261,9 +269,7 @@ def run_reference(args, rank, pg):
         "value": v, "unit": "GCDs/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": "mixed batch: %d pairs, bits log-uniform [1k,64k], 25%% coprime, 5%% v|u, "
-                               "70%% planted gcd U[0,50%%]" % args.pairs,
-                   "modulus_bits": args.modulus_bits or importlib.import_module("modgcd-onegpu_gb300").tuned_width()},
+        "config": mixed_config(args.pairs, args.modulus_bits or mg.tuned_width(), int(os.environ.get("WORLD_SIZE", "1"))),
         "cpu_baseline": {"value": v, "unit": "GCDs/s", "cores": nthreads, "kind": "reference",
                          "sample": "GMP %s mpz_gcd (the reference's -DNO_GPU path, testmodgcd.cpp:441) over all "
                                    "%d pairs per step, %d threads" % (po.gmp_version(), args.pairs, nthreads)},
@@ -392,10 +398,7 @@ def run_ours(args, rank, local, world, pg):
         "value": value, "unit": "GCDs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u32", "data": "synthetic",
-        "config": {"workload": "mixed batch: %d pairs, bits log-uniform [1k,64k], bits(v)=bits(u)/U(1,2), "
-                               "25%% coprime, 5%% v|u, 70%% planted gcd U[0,50%%] of the smaller" % n,
-                   "modulus_bits": L, "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "flushed before every step (256 MB write)"},
+        "config": mixed_config(n, L, world),
         "bit_exact": ok_dev and ok_e2e and ok_plain and all(r["bit_exact"] for r in serve_rows) and
                      (serve_sat is None or serve_sat["bit_exact"]),
         # operand bits (both operands of every pair) per second, device-resident and end to end

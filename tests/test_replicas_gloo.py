@@ -52,3 +52,28 @@ def test_reference_arm_under_torchrun_two_ranks(oracle):
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_reference_arm_line_contract(oracle):
+    """The reference arm's line at N = 1 carries every key of the benchmark contract, its
+    config is the object the GPU arm prints for the same batch, and its cpu_baseline and e2e
+    restate its own value."""
+    sys.path.insert(0, ROOT)
+    import bench
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "2",
+           "--warmup", "1", "--pairs", "64"]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+              "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert k in d, k
+    assert d["impl"] == "reference" and d["n_gpus"] == 1 and d["steps"] == 2 and d["warmup"] == 1
+    assert d["higher_is_better"] is True and d["unit"] == "GCDs/s" and d["value"] > 0
+    assert d["config"] == bench.mixed_config(64, d["config"]["modulus_bits"], 1)
+    assert d["cpu_baseline"]["kind"] == "reference" and d["cpu_baseline"]["value"] == d["value"]
+    assert d["cpu_baseline"]["cores"] >= 1
+    assert d["e2e"] == {"value": d["value"], "unit": "GCDs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert abs(d["ms_per_step"] - 1e3 * 64 / d["value"]) < 1e-6 * d["ms_per_step"] + 1e-9

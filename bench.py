@@ -63,7 +63,7 @@ def parse():
     ap.add_argument("--cpu-reps", type=int, default=10)
     ap.add_argument("--workload", choices=["mixed", "sweep", "serve", "skewed", "table1"], default="mixed")
     ap.add_argument("--sizes", default="4096,16384,65536,262144,1048576")
-    ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--reps", type=int, default=10, help="timed calls per size of --workload sweep")
     ap.add_argument("--serve-rates", default="10000",
                     help="arrival rates (req/s) of the serving leg; --workload serve defaults to the full sweep")
     ap.add_argument("--serve-requests", type=int, default=1000)

@@ -15,7 +15,13 @@ change of the restatement shows up as a fixture mismatch.
 The moduli fixture ``ref_moduli_L32.txt`` is the head and tail of the reference's
 createModuli output, plus a checksum of all 65,536 entries.
 
-Usage:  python tests/golden/make_golden.py
+``config1_seed1.txt`` is the single-pair benchmark configuration's pair (g 2048-bit odd,
+a and b 8192-bit coprime, GMP Mersenne Twister seeded with 1; workloads.single_pair) in the
+same two-line base-62 format, followed by its gcd from mpz_gcd.  The generator it comes
+from reproduces the reference driver's files above draw for draw (workloads.reference_pairs,
+checked by tests/test_workloads.py), so the fixture pins the configuration's inputs.
+
+Usage:  python tests/golden/make_golden.py [--config1-only]
 """
 import hashlib
 import json
@@ -49,7 +55,31 @@ def parse_b62(s: str) -> int:
     return x
 
 
+def to_b62(x: int) -> str:
+    s = []
+    while x:
+        x, r = divmod(x, 62)
+        s.append(B62[r])
+    return "".join(reversed(s)) or "0"
+
+
+def write_config1():
+    import importlib
+    sys.path.insert(0, ROOT)
+    wl = importlib.import_module("modgcd-onegpu_gb300.workloads")
+    u, v = wl.single_pair(seed=1)
+    a, b = po.to_limbs(u), po.to_limbs(v)
+    _, g, goff, glen = po.cpu_gmp_gcd_batch(np.concatenate([a, b]), [0], [len(a)], [len(a)], [len(b)], 1)
+    gm = po.from_limbs(g[int(goff[0]): int(goff[0]) + int(glen[0])])
+    assert gm == math.gcd(u, v)
+    with open(os.path.join(HERE, "config1_seed1.txt"), "w") as f:
+        f.write(to_b62(u) + "\n" + to_b62(v) + "\n" + to_b62(gm) + "\n")
+
+
 def main():
+    write_config1()
+    if "--config1-only" in sys.argv:
+        return
     oracle = os.path.join(ROOT, "oracle")
     subprocess.run(["make", "-s", "-C", oracle, "all", "ref"], check=True)
     driver = os.path.join(oracle, "_ref", "testmodgcd-nogpu")

@@ -14,7 +14,8 @@ import pytest
 from conftest import ROOT
 
 HEADER = os.path.join(ROOT, "include", "modgcd.h")
-REFERENCE = "/root/reference"
+# the reference's sources as installed by `make -C baseline install`
+REFERENCE = os.path.join(ROOT, "baseline", "_ref", "src")
 
 
 def declared_functions():
@@ -91,7 +92,8 @@ def test_batch_layout_helpers(mgcd):
     assert tot == int(cap.sum()) and all(cap >= 1)
 
 
-@pytest.mark.skipif(not os.path.isdir(REFERENCE), reason="reference sources not present")
+@pytest.mark.skipif(not os.path.isfile(os.path.join(REFERENCE, "testmodgcd.cpp")),
+                    reason="reference sources not installed")
 def test_reference_testmodgcd_compiles_against_dropin(mgcd, tmp_path):
     """The reference's own test driver compiles and links unchanged against GmpCuda.h."""
     import importlib.util

@@ -1,21 +1,22 @@
 // mgcd_noalloc.cu -- mgcd_gcd_digits_noalloc: the gcd of one pair without any allocation.
 //
 // Who needs it: code that may not call cudaMalloc at the point where it wants a gcd -- a
-// caller recording work into a CUDA graph (allocation is not capturable), a real-time or
-// callback context that must not block on the allocator, or an application whose device
-// memory is owned by its own pool.  Such a caller brings its own device buffers for the
-// operands and the results; the working memory this kernel needs besides them (each
-// modulus's initial residues and the pivot history of the reduction loop) lives in the
-// file-scope device array below, sized for the largest pair this entry point accepts.
+// real-time or callback context that must not block on the allocator or risk its failure,
+// or an application whose device memory is budgeted and owned by its own pool, so that a
+// library allocating behind its back would break that budget.  Such a caller brings its own
+// device buffers for the operands and the results; the working memory this kernel needs
+// besides them (each modulus's initial residues and the pivot history of the reduction
+// loop) lives in the file-scope device array below, sized for the largest pair this entry
+// point accepts.
 //
 // Limits and rules:
 //   - 32-bit moduli only, at most NA_MAX_NQ = 4,096 moduli: operands up to about 38,000
 //     bits.  Larger operands are rejected before anything is launched.
 //   - The scratch array (64 KiB) and the moduli table (64 KiB) are static device memory:
 //     every GPU that loads this library holds them until the process exits.
-//   - The first call on a device sets that device up (looks up the arrays' device addresses
-//     and copies the moduli table in, a synchronous copy): make that first call before any
-//     stream capture begins.
+//   - The first call in a CUDA context (per device, and again after a device reset) sets it
+//     up: looks up the arrays' device addresses and copies the moduli table in, a
+//     synchronous copy.  Make that first call before any stream capture begins.
 //   - Every call shares the one scratch array, which keeps the last call's contents.  The
 //     kernel writes every scratch word it later reads within the same call, so nothing has
 //     to start at zero.  Calls whose kernels overlap on the GPU (other streams, other host
@@ -24,6 +25,7 @@
 #include <cstring>
 #include <mutex>
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "../../include/modgcd.h"
@@ -104,19 +106,52 @@ __global__ void __launch_bounds__(NA_THREADS) noalloc_kernel(const NaArgs a)
 }
 
 std::mutex g_setup_mu;
-bool g_ready[NA_MAX_DEVICES];
+unsigned long long g_ctx[NA_MAX_DEVICES];    // id of the CUDA context set up on each device (0: none)
 uint32_t* g_scratch_addr[NA_MAX_DEVICES];
 const ModConst* g_mods_addr[NA_MAX_DEVICES];
 bool g_host_ready = false;
 ModConstHost g_host_mods[NA_MAX_NQ];
 uint32_t g_thr[NA_MAX_NQ / 256];
 
-// Per-device set-up, with that device current: device addresses of the two arrays
-// (host code may not use the arrays' names as addresses) and the moduli table copy.
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+
+// Unique id of the CUDA context that work on device dev runs in from this thread (0 on
+// failure).  A device reset or a new context brings fresh, zeroed copies of the static
+// arrays, so the set-up is cached per context id, not per device.  The driver functions
+// come from the runtime's entry-point table (no link against the driver library).  A thread
+// without a current context gets the device's primary context bound by cudaSetDevice, as
+// the runtime would bind it for the launch.  Called with g_setup_mu held.
+unsigned long long current_context_id(int dev)
+{
+  if (!g_ctx_get_current || !g_ctx_get_id) {
+    cudaDriverEntryPointQueryResult q1, q2;
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+        q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+      return 0;
+    g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+    g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f2);
+  }
+  CUcontext c = nullptr;
+  if (g_ctx_get_current(&c) != CUDA_SUCCESS) return 0;
+  if (!c && (cudaSetDevice(dev) != cudaSuccess || g_ctx_get_current(&c) != CUDA_SUCCESS || !c)) return 0;
+  unsigned long long id = 0;
+  return g_ctx_get_id(c, &id) == CUDA_SUCCESS ? id : 0;
+}
+
+// Set-up of the current context on device dev: device addresses of the two arrays (host
+// code may not use the arrays' names as addresses) and the moduli table copy.
 int setup_device(int dev)
 {
   std::lock_guard<std::mutex> lock(g_setup_mu);
-  if (g_ready[dev]) return MGCD_OK;
+  const unsigned long long ctx = current_context_id(dev);
+  if (ctx == 0) return MGCD_ERR_NO_DEVICE;
+  if (g_ctx[dev] == ctx) return MGCD_OK;
   if (!g_host_ready) {
     uint32_t q[NA_MAX_NQ];
     if (gen_moduli(NA_L, q, NA_MAX_NQ) != NA_MAX_NQ) return MGCD_ERR_KERNEL;
@@ -135,7 +170,7 @@ int setup_device(int dev)
   if (cudaMemcpyToSymbol(g_na_mods, g_host_mods, sizeof(g_host_mods)) != cudaSuccess) return MGCD_ERR_CUDA;
   g_scratch_addr[dev] = static_cast<uint32_t*>(s);
   g_mods_addr[dev] = static_cast<const ModConst*>(m);
-  g_ready[dev] = true;
+  g_ctx[dev] = ctx;
   return MGCD_OK;
 }
 
@@ -170,6 +205,10 @@ extern "C" int mgcd_gcd_digits_noalloc(const uint32_t* d_limbs, size_t uSz, size
   a.count = d_count;
   a.status = d_status;
   const size_t smem = sizeof(uint32_t) * (2 * (size_t)NA_MAX_NQ + CHUNK);
-  noalloc_kernel<<<1, NA_THREADS, smem, static_cast<cudaStream_t>(stream)>>>(a);
-  return cudaGetLastError() == cudaSuccess ? MGCD_OK : MGCD_ERR_CUDA;
+  // the launch's own return code: an error left pending by earlier, unrelated calls is
+  // neither blamed on this call nor cleared
+  void* args[] = {&a};
+  const cudaError_t e = cudaLaunchKernel(reinterpret_cast<const void*>(&noalloc_kernel), dim3(1), dim3(NA_THREADS),
+                                         args, smem, static_cast<cudaStream_t>(stream));
+  return e == cudaSuccess ? MGCD_OK : MGCD_ERR_CUDA;
 }

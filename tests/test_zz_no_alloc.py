@@ -1,13 +1,15 @@
 """The allocation-free entry point (mgcd_gcd_digits_noalloc) against the regular one.
 
 mgcd_gcd_digits_noalloc serves callers that cannot allocate device memory when they need
-a gcd (graph capture, real-time paths, applications with their own memory pools): they
-pass device buffers for the operands and results, and the library works in one static
-device array instead of allocating.  This test owns its buffers (allocated here, through
-torch), calls the entry point through the C ABI twice in a row on different pairs -- the
-second call reuses the scratch array the first call left behind -- and requires the
-digits, count and status to equal what the regular entry point (mgcd_gcd_digits) returns.
-It also checks that a pair over the 4,096-moduli limit is refused before any launch.
+a gcd (real-time or callback contexts that must not wait on the allocator, applications
+whose device memory is budgeted by their own pools): they pass device buffers for the
+operands and results, and the library works in one static device array instead of
+allocating.  This test owns its buffers (allocated here, through torch), calls the entry
+point through the C ABI twice in a row on different pairs -- the second call reuses the
+scratch array the first call left behind -- and requires the digits, count and status to
+equal what the regular entry point (mgcd_gcd_digits) returns.  It also runs a pair at the
+4,096-moduli limit, where the history and the initial residues fill the static array,
+and checks that a pair over the limit is refused before any launch.
 """
 import math
 import random
@@ -61,6 +63,24 @@ def test_noalloc_matches_regular_entry_point(mgcd):
         assert status == 0 and digits == dev.gcd_digits(u, v)
         import pyoracle
         assert pyoracle.mixed_radix_to_int(digits) == math.gcd(u, v)
+
+
+def test_noalloc_at_the_moduli_limit(mgcd):
+    """Operands that need exactly 4,096 moduli (37,000-38,600 bits): the scratch array is
+    used to its end; two such calls in a row, each equal to the regular entry point."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    rng = random.Random(2025)
+    with mgcd.Device(0, 32) as dev:
+        for ubits, vbits, gbits in [(38600, 38000, 9000), (37000, 36990, 1)]:
+            assert mgcd.moduli_needed(32 * ((ubits + 31) // 32), 32) == 4096
+            g = rng.getrandbits(gbits) | (1 << (gbits - 1)) | 1
+            u = g * (rng.getrandbits(ubits - gbits) | (1 << (ubits - gbits - 1)))
+            v = g * (rng.getrandbits(vbits - gbits) | 1)
+            status, digits = _call_noalloc(mgcd, torch, u, v)
+            assert status == 0
+            assert digits == dev.gcd_digits(u, v)
 
 
 def test_noalloc_rejects_sizes_over_limit(mgcd):

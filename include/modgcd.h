@@ -276,11 +276,11 @@ int mgcd_serve_trace(mgcd_server *server, mgcd_wave_trace *out, size_t cap, size
 
 /* ------------------------------------------------------------ allocation-free call ----
    No counterpart in the reference.  For callers that cannot allocate device memory when
-   they need a gcd: code recording into a CUDA graph, a real-time or callback context that
-   must not wait on the allocator, an application whose device memory belongs to its own
-   pool.  The digits of gcd(u, v) (as mgcd_gcd_digits returns them, 32-bit moduli), with
-   every buffer supplied by the caller and no allocation at all: no context, no cudaMalloc,
-   no cudaFree.  All pointers are device pointers: u at d_limbs[0 .. uSz), v at
+   they need a gcd: a real-time or callback context that must not wait on the allocator
+   or risk its failure, an application whose device memory is budgeted and owned by its
+   own pool.  The digits of gcd(u, v) (as mgcd_gcd_digits returns them, 32-bit moduli),
+   with every buffer supplied by the caller and no allocation at all: no context, no
+   cudaMalloc, no cudaFree.  All pointers are device pointers: u at d_limbs[0 .. uSz), v at
    d_limbs[uSz .. uSz + vSz), either order, both nonzero; d_digits holds cap >= the moduli
    count of the larger operand (mgcd_moduli_needed(32, 32 * max(uSz, vSz)) suffices);
    *d_count receives the digit count and *d_status an MGCD_* code.  The kernel is launched
@@ -289,9 +289,10 @@ int mgcd_serve_trace(mgcd_server *server, mgcd_wave_trace *out, size_t cap, size
    Limit: 4,096 moduli (operands of up to about 38,000 bits); larger sizes return
    MGCD_ERR_NOT_ENOUGH_MODULI and launch nothing.  The working memory is one static device
    array of 64 KiB (plus a 64 KiB moduli table) that every GPU loading the library keeps
-   until exit.  The first call on a device sets that device up (a synchronous copy of the
-   table): make it before any stream capture.  All calls share the array: calls that
-   overlap on the GPU race and must be serialised by the caller. */
+   until exit.  The first call in a CUDA context (on each device, and again after a device
+   reset) sets it up (a synchronous copy of the table): make it before any stream capture.
+   All calls share the array: calls that overlap on the GPU race and must be serialised by
+   the caller. */
 int mgcd_gcd_digits_noalloc(const uint32_t *d_limbs, size_t uSz, size_t vSz, mgcd_pair *d_digits, size_t cap,
                             uint32_t *d_count, int32_t *d_status, void *stream);
 /* Total work of the uploaded batch by the algorithmic cost model, after a run completed:

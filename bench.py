@@ -18,9 +18,15 @@ Every result is compared bit for bit with GMP mpz_gcd.
 --impl reference times the reference's CPU computation of the same batch: GMP mpz_gcd
 (testmodgcd.cpp:441, the -DNO_GPU build) on all host cores.
 
-Other workloads (--workload): sweep (single-pair latency by size and modulus width), skewed
-(64 x 1M-bit + 16,384 small pairs in one graph launch), serve (Poisson arrival sweep and a
-saturation replay), table1 (single pairs in the setting of the reference paper's Table 1).
+The default run then measures the other benchmark configurations, each with its own clock
+record and bit-exact check, as extra keys of the same line (--legs):
+  single_pair_sweep  n-bit operands with an n/4-bit gcd, n = 4k .. 1M, at 22/27/32-bit moduli
+  skewed             64 x 1M-bit + 16,384 pairs of 512-4096 bits in one CUDA graph launch
+  serving            Poisson arrivals at 1k-200k req/s (1% 1M-bit requests) + a saturation replay
+
+Each of these also runs alone (--workload sweep|skewed|serve); --workload table1 runs single
+pairs in the setting of the reference paper's Table 1, --workload seeds the mixed batch of
+several seeds with one tuning table.
 """
 import argparse
 import importlib
@@ -41,6 +47,7 @@ os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 TRAFFIC_FILE = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+COUNTERS_FILE = os.path.join(ROOT, "profiles", "ncu_counters.json")
 
 # Algorithmic cost model (int ops per unit of work): Barrett/Montgomery limb step 9,
 # reduction-loop update 257 (two inverses of ~19 quotient steps x 6 ops + 3 modmul + 2 modsub
@@ -61,11 +68,16 @@ def parse():
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--plain-sample", type=int, default=64)
     ap.add_argument("--cpu-reps", type=int, default=10)
-    ap.add_argument("--workload", choices=["mixed", "sweep", "serve", "skewed", "table1"], default="mixed")
+    ap.add_argument("--workload", choices=["mixed", "sweep", "serve", "skewed", "table1", "seeds"], default="mixed")
+    ap.add_argument("--seeds", default="1,2,3,4,5,6,7,8,9,10",
+                    help="batch seeds of --workload seeds (the mixed batch drawn from each)")
     ap.add_argument("--sizes", default="4096,16384,65536,262144,1048576")
-    ap.add_argument("--reps", type=int, default=10, help="timed calls per size of --workload sweep")
-    ap.add_argument("--serve-rates", default="10000",
-                    help="arrival rates (req/s) of the serving leg; --workload serve defaults to the full sweep")
+    ap.add_argument("--reps", type=int, default=5, help="timed calls per size of the single-pair sweep")
+    ap.add_argument("--serve-rates", default="1000,10000,50000,100000,200000",
+                    help="arrival rates (req/s) of the serving leg")
+    ap.add_argument("--legs", default="sweep,skewed,serve",
+                    help="configurations measured after the mixed batch in the default run, each with its own "
+                         "clock record (comma list of sweep, skewed, serve; empty: none)")
     ap.add_argument("--serve-requests", type=int, default=1000)
     ap.add_argument("--serve-sat-requests", type=int, default=8192,
                     help="requests of the serving saturation replay (1k-64k bits at 1M req/s; 0: none)")
@@ -153,6 +165,17 @@ def measured_peaks():
             return json.load(f), "measured"
     except (OSError, ValueError):
         return {"hbm_gbs": 6800.0}, "fallback"
+
+
+def executed_counters(L):
+    """The dominant kernel's executed-instruction figures from its ncu capture (committed
+    under profiles/): issue-slot and lane utilisation, i.e. the pipe-level fraction beside
+    the cost model's `frac`.  None when no capture exists for this modulus width."""
+    try:
+        with open(COUNTERS_FILE) as f:
+            return json.load(f)["by_modulus_bits"][str(L)]
+    except (OSError, ValueError, KeyError):
+        return None
 
 
 def gmp_baseline(po, packed, nthreads, reps):
@@ -358,17 +381,22 @@ def run_ours(args, rank, local, world, pg):
     plain_rate = len(idx) / sum(lat)
     lat_ms = sorted(1e3 * x for x in lat)
 
-    # ---- serving: Poisson arrivals through the request server
-    rates = [float(r) for r in args.serve_rates.split(",") if r]
-    serve_rows, serve_stats, serve_sat = [], {}, None
-    if rates:
-        # serving runs 32-bit moduli: its 1M-bit requests take 1.4 s there and 2.5 s at 27 bits
-        sdev = dev if L == SERVE_BITS else mg.Device(local, SERVE_BITS)
-        apply_tuning(sdev, mg.default_tuning_path(sdev))
-        serve_rows, serve_stats, serve_sat = serve_leg(mg, wl, po, sdev, rates, args.serve_requests, nthreads,
-                                                       sat_requests=args.serve_sat_requests)
-        if sdev is not dev:
-            sdev.close()
+    # ---- the other configurations, each with its own clock record (rank 0)
+    legs = {}
+    want = [x for x in args.legs.split(",") if x]
+    if rank == 0:
+        if "sweep" in want:
+            sizes = [int(x) for x in args.sizes.split(",")]
+            legs["single_pair_sweep"] = timed_leg(local, lambda: sweep_leg(mg, wl, po, local, sizes, args.reps))
+        if "skewed" in want:
+            legs["skewed"] = timed_leg(local, lambda: skewed_leg(mg, wl, po, local, None, 1))
+        if "serve" in want:
+            rates = [float(r) for r in args.serve_rates.split(",") if r]
+            legs["serving"] = timed_leg(local, lambda: serve_config(mg, wl, po, local, rates, args.serve_requests,
+                                                                    args.serve_sat_requests, None))
+            sat = legs["serving"]["saturation"]
+            legs["serving"]["saturation_over_plain"] = sat["gcds_per_s"] / plain_rate if sat else None
+    barrier(pg)
 
     if rank != 0:
         return
@@ -378,7 +406,9 @@ def run_ours(args, rank, local, world, pg):
     ops = OPS_RESIDUE * work["residue_steps"] + OPS_EUCLID * work["euclid_updates"] + \
         OPS_RECOVERY * work["recovery_updates"]
     run_s = statistics.mean(run_ms) / 1e3
-    alg_bytes = work["operand_bytes"]
+    operand_bytes = work["operand_bytes"]
+    alg_bytes = work["algorithmic_bytes"]
+    counters = executed_counters(L)
     model_ops = lambda w: OPS_RESIDUE * w["residue_steps"] + OPS_EUCLID * w["euclid_updates"] + \
         OPS_RECOVERY * w["recovery_updates"]
     per_kernel = [{"size_class": kern_ms[0][b][0], "pairs": kern_ms[0][b][1], "ms": mean_ms[b],
@@ -399,23 +429,16 @@ def run_ours(args, rank, local, world, pg):
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u32", "data": "synthetic",
         "config": mixed_config(n, L, world),
-        "bit_exact": ok_dev and ok_e2e and ok_plain and all(r["bit_exact"] for r in serve_rows) and
-                     (serve_sat is None or serve_sat["bit_exact"]),
+        "bit_exact": ok_dev and ok_e2e and ok_plain and all(x["bit_exact"] for x in legs.values()),
         # operand bits (both operands of every pair) per second, device-resident and end to end
-        "operand_bits_per_s": {"value": 8.0 * alg_bytes * world * args.steps / tot_s,
-                               "e2e": 8.0 * alg_bytes * world * args.steps / e2e_s},
+        "operand_bits_per_s": {"value": 8.0 * operand_bytes * world * args.steps / tot_s,
+                               "e2e": 8.0 * operand_bytes * world * args.steps / e2e_s},
         "e2e": {"value": n * world * args.steps / e2e_s, "unit": "GCDs/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "plain": {"value": plain_rate, "unit": "GCDs/s", "sample_pairs": len(idx),
                   "p50_ms": lat_ms[len(lat_ms) // 2], "p99_ms": lat_ms[min(len(lat_ms) - 1, int(0.99 * len(lat_ms)))],
                   "batched_over_plain": value / world / plain_rate},
         "batch_latency_ms": {"p50": statistics.median(run_ms), "max": max(run_ms)},
-        "serving": {"rows": serve_rows, "server": serve_stats,
-                    "workload": "mixed 1k-64k-bit sizes + 1% 1M-bit, Poisson arrivals, 8 GB admission budget",
-                    "modulus_bits": SERVE_BITS,
-                    "saturation": serve_sat,
-                    "saturation_over_plain": (serve_sat["gcds_per_s"] / plain_rate) if serve_sat else None,
-                    "bit_exact": all(r["bit_exact"] for r in serve_rows) and (serve_sat is None or serve_sat["bit_exact"])},
         "tuning": tuning,
         "roofline": {"bound": "int", "achieved": achieved / 1e9, "peak": int_peak / 1e9, "unit": "Gop/s",
                      "frac": achieved / int_peak, "traffic": traffic,
@@ -426,8 +449,13 @@ def run_ours(args, rank, local, world, pg):
                               "formulation's integer ops per unit of algorithmic work)",
                      "peak_source": "in-repo IMAD microbenchmark (mgcd_int_peak), measured live",
                      "per_kernel": per_kernel,
+                     "executed": counters,
                      "hbm": {"achieved_gbs": alg_bytes / run_s / 1e9, "peak_gbs": peaks.get("hbm_gbs"),
                              "frac": alg_bytes / run_s / 1e9 / peaks.get("hbm_gbs", 6800.0),
+                             "algorithmic_bytes": alg_bytes,
+                             "bytes_model": "per pair 4 (limbs_u + limbs_v) + 12 N + 8 (k + 1): operands, a prime "
+                                            "and its constant per modulus used, the digits",
+                             "traffic_over_algorithmic": (traffic / alg_bytes) if traffic else None,
                              "peak_source": peaks_kind}},
         "work": work,
         "rerun_pairs_per_step": retried,
@@ -439,35 +467,44 @@ def run_ours(args, rank, local, world, pg):
         "clocks": clk,
         "wall_s_timed": wall,
     }
+    line.update(legs)
     print(json.dumps(line), flush=True)
 
 
-def run_sweep(args, rank, local):
-    """Single-pair latency sweep: n-bit operands with an n/4-bit planted gcd, at modulus
-    widths 22/27/32, one pair per call (the plain method), median over reps."""
-    if rank != 0:
-        return
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import pyoracle as po
-    mg = importlib.import_module("modgcd-onegpu_gb300")
-    wl = importlib.import_module("modgcd-onegpu_gb300.workloads")
-    sizes = [int(x) for x in args.sizes.split(",")]
+def timed_leg(local, fn):
+    """Runs fn() with nvidia-smi clock samples around it; adds them as the leg's `clocks`."""
+    clocks = Clocks(local)
+    clocks.start()
+    try:
+        res = fn()
+    finally:
+        clk = clocks.stop()
+    res["clocks"] = clk
+    return res
+
+
+def sweep_leg(mg, wl, po, local, sizes, reps, widths=(32, 27, 22)):
+    """Single-pair latency (the plain method, one pair per call): n-bit operands with an
+    n/4-bit planted gcd at each modulus width; device time (CUDA events around the pair's
+    launches) and wall time through the C ABI, median over reps, every result against
+    GMP; beside it the same pair in the reference's launch shape (256-thread CTAs of 256
+    moduli, one grid exchange per iteration) on the same kernels, and GMP on one core."""
     rows = []
-    for L in (32, 27, 22):
+    for L in widths:
         dev = mg.Device(local, L)
         for n in sizes:
             u, v = wl.size_sweep_pair(n, seed=1)
             packed = mg.pack_pairs([u], [v])
-            gsec = [po.cpu_gmp_gcd_batch(*packed, 1, want_results=False)[0] for _ in range(3)]
+            gsec = min(po.cpu_gmp_gcd_batch(*packed, 1, want_results=False)[0] for _ in range(3))
             _, gx, gxo, gxn = po.cpu_gmp_gcd_batch(*packed, 1)
             expect = po.from_limbs(gx[: int(gxn[0])])
             wall, dev_ms, ok = [], [], True
-            for r in range(args.reps + 1):
+            for r in range(reps + 1):
                 t0 = time.perf_counter()
                 try:
                     g = dev.gcd(u, v)
                 except mg.GcdError as e:
-                    rows.append({"L": L, "bits": n, "error": str(e)})
+                    rows.append({"L": L, "bits": n, "error": str(e), "bit_exact": False})
                     ok = None
                     break
                 t1 = time.perf_counter()
@@ -477,81 +514,150 @@ def run_sweep(args, rank, local):
                     dev_ms.append(dev.batch_elapsed_ms()[0])
             if ok is None:
                 continue
-            # the same pair in the reference's launch shape (256-thread CTAs, grid-wide exchange)
-            pol_ms = {}
-            for pol in (1, 2):   # the reference's launch shape; the grid of 8-CTA clusters
-                dev.set_single_pair_policy(pol)
-                pol_ms[pol] = []
-                for _ in range(max(1, args.reps - 1)):
-                    ok = ok and dev.gcd(u, v) == expect
-                    pol_ms[pol].append(dev.batch_elapsed_ms()[0])
+            dev.set_single_pair_policy(1)       # the reference's launch shape
+            ref_ms = []
+            for _ in range(max(1, reps - 2)):
+                ok = ok and dev.gcd(u, v) == expect
+                ref_ms.append(dev.batch_elapsed_ms()[0])
             dev.set_single_pair_policy(0)
             rows.append({"L": L, "bits": n, "moduli": mg.moduli_needed(n, L), "device_ms": statistics.median(dev_ms),
                          "wall_ms": statistics.median(wall), "p99_wall_ms": max(wall),
-                         "reference_shape_ms": statistics.median(pol_ms[1]),
-                         "cluster_grid_ms": statistics.median(pol_ms[2]), "gmp_ms": 1e3 * min(gsec),
+                         "reference_shape_ms": statistics.median(ref_ms), "gmp_1core_ms": 1e3 * gsec,
                          "bit_exact": bool(ok)})
             print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
         dev.close()
-    print(json.dumps({"metric": "single-pair gcd latency (plain method), n-bit operands, n/4-bit gcd",
-                      "unit": "ms", "higher_is_better": False, "data": "synthetic", "rows": rows}), flush=True)
+    return {"metric": "single-pair gcd latency (plain method), n-bit operands, n/4-bit planted gcd",
+            "unit": "ms", "reps": reps, "rows": rows, "bit_exact": all(r["bit_exact"] for r in rows)}
 
 
-def run_serve(args, rank, local):
-    """Serving sweep: Poisson arrivals at each rate (default 1k-200k req/s), sizes from the
-    mixed distribution plus 1% 1M-bit requests, 8 GB admission budget."""
-    if rank != 0:
-        return
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import pyoracle as po
-    mg = importlib.import_module("modgcd-onegpu_gb300")
-    wl = importlib.import_module("modgcd-onegpu_gb300.workloads")
-    dev = mg.Device(local, args.modulus_bits or SERVE_BITS)
-    tuning = apply_tuning(dev, args.tuning or mg.default_tuning_path(dev))
-    rates = [float(r) for r in (args.serve_rates if args.serve_rates != "10000" else
-                                "1000,10000,50000,100000,200000").split(",")]
-    rows, stats, sat = serve_leg(mg, wl, po, dev, rates, args.serve_requests, os.cpu_count() or 1,
-                                 sat_requests=args.serve_sat_requests)
-    print(json.dumps({"metric": "served GCDs/s and p50/p99 latency (enqueue -> result)", "unit": "GCDs/s, ms",
-                      "data": "synthetic", "workload": "mixed 1k-64k-bit + 1% 1M-bit requests, Poisson arrivals, "
-                      "8 GB admission budget", "tuning": tuning, "rows": rows, "saturation": sat, "server": stats,
-                      "bit_exact": all(r["bit_exact"] for r in rows) and (sat is None or sat["bit_exact"])}),
-          flush=True)
-
-
-def run_skewed(args, rank, local):
-    """The skewed batch (64 pairs at 1M bits + 16,384 pairs of 512-4096 bits) recorded into
-    one CUDA graph and replayed; device time per replay, results against GMP."""
-    if rank != 0:
-        return
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import pyoracle as po
-    mg = importlib.import_module("modgcd-onegpu_gb300")
-    wl = importlib.import_module("modgcd-onegpu_gb300.workloads")
+def skewed_leg(mg, wl, po, local, tuning_arg, steps):
+    """The skewed batch (64 pairs at 1M bits + 16,384 pairs of 512-4096 bits, 32-bit
+    moduli) recorded into one CUDA graph and replayed: device time per replay (CUDA events
+    on the library's stream), results against GMP."""
     us, vs = wl.skewed_batch()
     packed = mg.pack_pairs(us, vs)
     nthreads = os.cpu_count() or 1
     cpu_s, gx, gxo, gxn = po.cpu_gmp_gcd_batch(*packed, nthreads)
     dev = mg.Device(local, 32)
-    tuning = apply_tuning(dev, args.tuning or mg.default_tuning_path(dev))
+    tuning = apply_tuning(dev, tuning_arg or mg.default_tuning_path(dev))
     dev.batch_use_graph(True)
     dev.batch_upload(*packed)
     ms = []
-    for _ in range(max(1, args.steps) + 1):
+    for _ in range(max(1, steps) + 1):          # the first run records the graph
         dev.batch_run()
         dev.batch_sync()
         ms.append(dev.batch_elapsed_ms()[0])
     g, go, gn, st = dev.batch_download()
     ok = bool((st == 0).all()) and results_equal(mg, g, go, gn, gx, gxo, gxn)
+    launches = dev.batch_launches()
+    dev.close()
     n = len(us)
     t = statistics.median(ms[1:]) / 1e3
-    print(json.dumps({"metric": "GCDs/s (skewed batch in one CUDA graph launch)", "value": n / t, "unit": "GCDs/s",
-                      "ms_per_step": 1e3 * t, "graph_kernels": dev.batch_launches(), "steps": len(ms) - 1,
-                      "config": {"workload": "64 pairs at 1M bits + 16384 pairs of U[512,4096] bits, planted gcds",
-                                 "modulus_bits": 32},
-                      "tuning": tuning, "bit_exact": ok,
-                      "cpu_baseline": {"value": n / cpu_s, "unit": "GCDs/s", "cores": nthreads, "kind": "reference",
-                                       "sample": "GMP mpz_gcd over the whole batch"}}), flush=True)
+    return {"metric": "GCDs/s (skewed batch in one CUDA graph launch)", "value": n / t, "unit": "GCDs/s",
+            "ms_per_step": 1e3 * t, "steps": len(ms) - 1, "graph_kernels": launches,
+            "workload": "64 pairs at 1M bits + 16384 pairs of U[512,4096] bits, planted gcds",
+            "modulus_bits": 32, "tuning": tuning, "bit_exact": ok,
+            "cpu_baseline": {"value": n / cpu_s, "unit": "GCDs/s", "cores": nthreads, "kind": "reference",
+                             "sample": "GMP mpz_gcd over the whole batch"}}
+
+
+def serve_config(mg, wl, po, local, rates, n_req, sat_requests, tuning_arg, L=SERVE_BITS):
+    """The serving configuration on its own context (see serve_leg)."""
+    dev = mg.Device(local, L)
+    tuning = apply_tuning(dev, tuning_arg or mg.default_tuning_path(dev))
+    rows, stats, sat = serve_leg(mg, wl, po, dev, rates, n_req, os.cpu_count() or 1, sat_requests=sat_requests)
+    dev.close()
+    return {"metric": "served GCDs/s and p50/p99 latency (scheduled arrival -> result)", "unit": "GCDs/s, ms",
+            "workload": "mixed 1k-64k-bit + 1% 1M-bit requests, Poisson arrivals, 8 GB admission budget",
+            "modulus_bits": L, "tuning": tuning, "rows": rows, "saturation": sat, "server": stats,
+            "bit_exact": all(r["bit_exact"] for r in rows) and (sat is None or sat["bit_exact"])}
+
+
+def run_sweep(args, rank, local):
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    mg = importlib.import_module("modgcd-onegpu_gb300")
+    wl = importlib.import_module("modgcd-onegpu_gb300.workloads")
+    sizes = [int(x) for x in args.sizes.split(",")]
+    res = timed_leg(local, lambda: sweep_leg(mg, wl, po, local, sizes, args.reps))
+    res.update({"higher_is_better": False, "data": "synthetic"})
+    print(json.dumps(res), flush=True)
+
+
+def run_serve(args, rank, local):
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    mg = importlib.import_module("modgcd-onegpu_gb300")
+    wl = importlib.import_module("modgcd-onegpu_gb300.workloads")
+    rates = [float(r) for r in args.serve_rates.split(",") if r]
+    res = timed_leg(local, lambda: serve_config(mg, wl, po, local, rates, args.serve_requests,
+                                                args.serve_sat_requests, args.tuning,
+                                                args.modulus_bits or SERVE_BITS))
+    res["data"] = "synthetic"
+    print(json.dumps(res), flush=True)
+
+
+def run_skewed(args, rank, local):
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    mg = importlib.import_module("modgcd-onegpu_gb300")
+    wl = importlib.import_module("modgcd-onegpu_gb300.workloads")
+    res = timed_leg(local, lambda: skewed_leg(mg, wl, po, local, args.tuning, args.steps))
+    res["data"] = "synthetic"
+    print(json.dumps(res), flush=True)
+
+
+def run_seeds(args, rank, local):
+    """The mixed batch drawn from each of several seeds with one tuning table: device time
+    per step (median of --steps), pairs rerun with the reference count, every result against
+    GMP -- how far the tuned moduli fractions are from the certification cliff."""
+    if rank != 0:
+        return
+    import torch
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    mg = importlib.import_module("modgcd-onegpu_gb300")
+    wl = importlib.import_module("modgcd-onegpu_gb300.workloads")
+    L = args.modulus_bits or mg.tuned_width()
+    dev = mg.Device(local, L)
+    tuning = apply_tuning(dev, args.tuning or mg.default_tuning_path(dev))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    rows = []
+    clocks = Clocks(local)
+    clocks.start()
+    for seed in [int(x) for x in args.seeds.split(",") if x]:
+        us, vs, _ = wl.mixed_batch(args.pairs, seed=seed)
+        packed = mg.pack_pairs(us, vs)
+        _, gx, gxo, gxn = po.cpu_gmp_gcd_batch(*packed, os.cpu_count() or 1)
+        dev.batch_upload(*packed)
+        ms, rerun = [], 0
+        for i in range(max(1, args.warmup) + max(1, args.steps)):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            dev.batch_run()
+            dev.batch_sync()
+            if i >= max(1, args.warmup):
+                ms.append(dev.batch_elapsed_ms()[0])
+                rerun = max(rerun, dev.batch_retried())
+        g, go, gn, st = dev.batch_download()
+        ok = bool((st == 0).all()) and results_equal(mg, g, go, gn, gx, gxo, gxn)
+        rows.append({"seed": seed, "ms_per_step": statistics.median(ms), "rerun_pairs": rerun, "bit_exact": ok})
+        print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
+    clk = clocks.stop()
+    dev.close()
+    med = statistics.median(r["ms_per_step"] for r in rows)
+    print(json.dumps({"metric": "mixed-batch step time across batch seeds (one tuning table)", "unit": "ms",
+                      "higher_is_better": False, "data": "synthetic", "modulus_bits": L, "tuning": tuning,
+                      "pairs": args.pairs, "rows": rows, "median_ms": med,
+                      "max_over_median": max(r["ms_per_step"] for r in rows) / med,
+                      "spread": (max(r["ms_per_step"] for r in rows) - min(r["ms_per_step"] for r in rows)) / med,
+                      "clocks": clk, "bit_exact": all(r["bit_exact"] for r in rows)}), flush=True)
 
 
 # The reference paper's Table 1 (Weber & Brew, p.6): Tesla V100 mean wall time per call (ms),
@@ -607,6 +713,8 @@ def main():
         run_skewed(args, rank, local)
     elif args.workload == "table1":
         run_table1(args, rank, local)
+    elif args.workload == "seeds":
+        run_seeds(args, rank, local)
     elif args.impl == "reference":
         run_reference(args, rank, pg)
     else:

@@ -300,6 +300,12 @@ int mgcd_gcd_digits_noalloc(const uint32_t *d_limbs, size_t uSz, size_t vSz, mgc
    the surviving moduli), recovery updates (the same over digits) and operand bytes. */
 int mgcd_batch_work(const mgcd_context *ctx, double *residue_steps, double *euclid_updates,
                     double *recovery_updates, double *operand_bytes);
+/* Algorithmic bytes of the last downloaded batch, the unit of the memory roofline: per
+   pair, its operand limbs (4 bytes each), a prime and an 8-byte constant for every modulus
+   it used (12 bytes each; the reference reads the prime, GmpCudaDevice-getGcdKernel.cu:335,
+   and derives the constant) and its k + 1 result digits (8 bytes each, the pair_t list of
+   GmpCudaDevice-getGcdKernel.cu:437-443).  No counterpart in the reference. */
+int mgcd_batch_alg_bytes(const mgcd_context *ctx, double *alg_bytes);
 
 #ifdef __cplusplus
 }

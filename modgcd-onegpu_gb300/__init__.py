@@ -56,6 +56,7 @@ SIGNATURES = {
     "mgcd_batch_launches": (_c.c_int, [_P, _c.POINTER(_c.c_int)]),
     "mgcd_batch_work": (_c.c_int, [_P, _c.POINTER(_c.c_double), _c.POINTER(_c.c_double),
                                    _c.POINTER(_c.c_double), _c.POINTER(_c.c_double)]),
+    "mgcd_batch_alg_bytes": (_c.c_int, [_P, _c.POINTER(_c.c_double)]),
     "mgcd_batch_elapsed_ms": (_c.c_int, [_P, _c.POINTER(_c.c_float), _c.POINTER(_c.c_float),
                                          _c.POINTER(_c.c_int)]),
     "mgcd_batch_transfer_bytes": (_c.c_int, [_P, _c.POINTER(_c.c_uint64), _c.POINTER(_c.c_uint64)]),
@@ -409,8 +410,10 @@ class Device:
         r, e, m, b = (ctypes.c_double() for _ in range(4))
         _check(self._lib.mgcd_batch_kernel_work(self._h, int(i), ctypes.byref(r), ctypes.byref(e), ctypes.byref(m),
                                                 ctypes.byref(b)))
+        ab = ctypes.c_double()
+        _check(self._lib.mgcd_batch_alg_bytes(self._h, ctypes.byref(ab)))
         return {"residue_steps": r.value, "euclid_updates": e.value, "recovery_updates": m.value,
-                "operand_bytes": b.value}
+                "operand_bytes": b.value, "algorithmic_bytes": ab.value}
 
     def batch_retried(self):
         n = ctypes.c_int()
@@ -443,8 +446,10 @@ class Device:
         r, e, m, b = (ctypes.c_double() for _ in range(4))
         _check(self._lib.mgcd_batch_work(self._h, ctypes.byref(r), ctypes.byref(e), ctypes.byref(m),
                                          ctypes.byref(b)))
+        ab = ctypes.c_double()
+        _check(self._lib.mgcd_batch_alg_bytes(self._h, ctypes.byref(ab)))
         return {"residue_steps": r.value, "euclid_updates": e.value, "recovery_updates": m.value,
-                "operand_bytes": b.value}
+                "operand_bytes": b.value, "algorithmic_bytes": ab.value}
 
 
 class Server:

@@ -801,7 +801,7 @@ int mgcd::fetch(mgcd_context* c, Plan& P)
   const uint32_t* it = P.h_iters.as<uint32_t>();
   const uint32_t* cnt = P.h_count.as<uint32_t>();
   const int32_t* st = P.h_status.as<int32_t>();
-  double R = 0, E = 0, M = 0, B = 0;
+  double R = 0, E = 0, M = 0, B = 0, AB = 0;
   std::vector<double> pw(4 * ng, 0.0);    // per pair: R, E, M, B
   for (size_t k = 0; k < ng; ++k) {
     const PairDesc& d = P.descs[k];
@@ -812,10 +812,12 @@ int mgcd::fetch(mgcd_context* c, Plan& P)
       const double I = it[k], K = cnt[k], N = P.eff_nq[k];
       w[1] = I * N - I * (I + 1) / 2;
       w[2] = K * (N - I) - K * (K + 1) / 2;
+      AB += 12.0 * N + 8.0 * (K + 1);      // a prime and its 8-byte constant per modulus, digits
     }
     R += w[0]; E += w[1]; M += w[2]; B += w[3];
   }
   P.work[0] = R; P.work[1] = E; P.work[2] = M; P.work[3] = B;
+  P.alg_bytes = B + AB;
   P.bucket_work.assign(4 * P.buckets.size(), 0.0);
   for (size_t b = 0; b < P.buckets.size(); ++b)
     for (uint32_t i = 0; i < P.buckets[b].n; ++i) {
@@ -1175,6 +1177,13 @@ int mgcd_batch_work(const mgcd_context* c, double* r, double* e, double* m, doub
   if (e) *e = w[1];
   if (m) *m = w[2];
   if (b) *b = w[3];
+  return MGCD_OK;
+}
+
+int mgcd_batch_alg_bytes(const mgcd_context* c, double* alg_bytes)
+{
+  if (!c || !alg_bytes) return MGCD_ERR_INVALID_ARG;
+  *alg_bytes = c->main.alg_bytes;
   return MGCD_OK;
 }
 

@@ -86,6 +86,7 @@ struct Plan {
   int launches = 0, retried = 0;
   bool ran = false, synced = false, bucket_timed = false;
   double work[4] = {0, 0, 0, 0};       // residue steps, loop updates, recovery updates, operand bytes
+  double alg_bytes = 0;                // algorithmic bytes: operands + (prime, constant) per modulus + digits
   std::vector<double> bucket_work;     // the same per bucket kernel (4 per bucket)
   uint64_t h2d_bytes = 0, d2h_bytes = 0;
 

@@ -224,3 +224,15 @@ def test_operand_staging_alignment_and_tile_edges(mgcd, device):
     for nl in (1025, 9000):
         u, v = rand_pair(rng, 32 * nl, 8 * nl)
         assert device.gcd(u, v) == math.gcd(u, v)
+
+
+def test_one_megabit_pair_at_22bit_moduli(mgcd, oracle):
+    """The single-pair sweep's largest case at full size: 1M-bit operands with a 256k-bit
+    planted gcd, 22-bit moduli (96,256 of them), against GMP mpz_gcd."""
+    wl = __import__("importlib").import_module("modgcd-onegpu_gb300.workloads")
+    u, v = wl.size_sweep_pair(1 << 20, seed=1)
+    _, g, go, gn = oracle.cpu_gmp_gcd_batch(*mgcd.pack_pairs([u], [v]), 1)
+    expect = oracle.from_limbs(g[: int(gn[0])])
+    assert expect.bit_length() >= 1 << 18
+    with mgcd.Device(0, 22) as dev:
+        assert dev.gcd(u, v) == expect

@@ -167,6 +167,48 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0}, "fallback"
 
 
+def occupancy(rec, sms):
+    """SM-busy accounting of one traced run (mgcd_batch_cta_trace records): per SM the union
+    of its CTAs' intervals, over the span from the first CTA start to the last CTA end; per
+    size class the CTAs, their start and end spread, the longest CTA and, for the K-slot
+    CTAs, where thread 0's clock went (set-up, update, pivot step incl. the wait for the
+    slowest warp, finish; finish_replay: the certification and replay part of finish)."""
+    rec = rec[rec["ran"] != 0]
+    if not len(rec):
+        return None
+    span = float(rec["t_end_ms"].max() - rec["t_start_ms"].min())
+    busy = 0.0
+    for sm in set(int(x) for x in rec["sm"]):
+        iv = sorted((float(a), float(b)) for a, b in zip(rec["t_start_ms"][rec["sm"] == sm],
+                                                         rec["t_end_ms"][rec["sm"] == sm]))
+        cur_a, cur_b = iv[0]
+        for a, b in iv[1:]:
+            if a > cur_b:
+                busy += cur_b - cur_a
+                cur_a, cur_b = a, b
+            else:
+                cur_b = max(cur_b, b)
+        busy += cur_b - cur_a
+    classes = {}
+    for c in sorted(set(int(x) for x in rec["size_class"])):
+        r = rec[rec["size_class"] == c]
+        d = r["t_end_ms"] - r["t_start_ms"]
+        classes[str(c)] = {"ctas": int(len(r)), "pairs": int(r["pairs"].sum()),
+                           "start_ms_max": float(r["t_start_ms"].max()), "end_ms_min": float(r["t_end_ms"].min()),
+                           "end_ms_max": float(r["t_end_ms"].max()), "cta_ms_median": float(statistics.median(d)),
+                           "cta_ms_max": float(d.max())}
+        cyc = {k: float(r["cycles_" + k].sum()) for k in ("setup", "update", "pivot", "finish")}
+        tot = sum(cyc.values())
+        if tot > 0:
+            classes[str(c)]["phases"] = {k: v / tot for k, v in cyc.items()}
+            classes[str(c)]["phases"]["finish_replay"] = float(r["cycles_replay"].sum()) / tot
+            classes[str(c)]["iterations"] = int(r["iterations"].sum())
+            classes[str(c)]["cycles_per_round"] = cyc["update"] / max(1.0, float(r["rounds"].sum()))
+            classes[str(c)]["pivot_cycles_per_iteration"] = cyc["pivot"] / max(1.0, float(r["iterations"].sum()))
+    return {"span_ms": span, "sms": sms, "sm_busy_frac": busy / (sms * span) if span > 0 else None,
+            "by_class": classes}
+
+
 def executed_counters(L):
     """The dominant kernel's executed-instruction figures from its ncu capture (committed
     under profiles/): issue-slot and lane utilisation, i.e. the pipe-level fraction beside
@@ -235,6 +277,17 @@ def serve_leg(mg, wl, po, dev, rates, n_req, nthreads, seed=5, sat_requests=0):
                             "max_ms_1M": float(ms[big].max())})
             rows.append(row)
             print(json.dumps(row), file=sys.stderr, flush=True)
+        # the same 10k req/s stream through waves only (continuous lanes off), for comparison
+        srv.set_continuous(False)
+        g, go, gn, st, lat, mk = srv.replay_packed(*packed, np.asarray(arr1) / 10000.0)
+        ms = lat * 1e3
+        waves_row = {"rate_req_s": 10000.0, "requests": n_req, "gcds_per_s": n_req / mk,
+                     "p50_ms": float(np.percentile(ms, 50)), "p99_ms": float(np.percentile(ms, 99)),
+                     "p50_ms_small": float(np.percentile(ms[~big], 50)),
+                     "p99_ms_small": float(np.percentile(ms[~big], 99)),
+                     "bit_exact": bool((st == 0).all()) and results_equal(mg, g, go, gn, gx, gxo, gxn)}
+        print(json.dumps({"waves_only": waves_row}), file=sys.stderr, flush=True)
+        srv.set_continuous(True)
         if sat_requests:
             # saturation: mixed 1k-64k-bit requests only, all arriving within a few ms, so
             # the served rate is the server's throughput (comparable with the plain method's)
@@ -250,6 +303,7 @@ def serve_leg(mg, wl, po, dev, rates, n_req, nthreads, seed=5, sat_requests=0):
                    "bit_exact": bool((st == 0).all()) and results_equal(mg, g, go, gn, sx, sxo, sxn)}
             print(json.dumps(sat), file=sys.stderr, flush=True)
         stats = srv.stats()
+    stats["waves_only_10k"] = waves_row
     return rows, stats, sat
 
 
@@ -350,6 +404,14 @@ def run_ours(args, rank, local, world, pg):
     wall = time.perf_counter() - wall0
     tot_s = reduce_max(pg, sum(run_ms) / 1e3)
     clk = clocks.stop()
+    # one more (untimed) step with the per-CTA occupancy trace on
+    dev.set_cta_trace(True)
+    flush.fill_(1)
+    torch.cuda.synchronize()
+    dev.batch_run()
+    dev.batch_sync()
+    occ = occupancy(dev.batch_cta_trace(), torch.cuda.get_device_properties(local).multi_processor_count)
+    dev.set_cta_trace(False)
     # per size-class kernel: device time (CUDA events on its stream; the kernels of a step run
     # concurrently and share the SMs) and work (read now: the legs below replace the plan)
     nb = len(kern_ms[0])
@@ -460,6 +522,7 @@ def run_ours(args, rank, local, world, pg):
         "work": work,
         "rerun_pairs_per_step": retried,
         "longest_kernel_ms": statistics.mean(dom_ms), "longest_kernel_threads": dom_t,
+        "occupancy": occ,
         "cpu_baseline": {"value": n / min(cpu_times), "unit": "GCDs/s", "cores": nthreads, "kind": "reference",
                          "sample": "GMP %s mpz_gcd over the same %d pairs, best of %d, %d threads" %
                                    (po.gmp_version(), n, len(cpu_times), nthreads)},
@@ -570,7 +633,8 @@ def serve_config(mg, wl, po, local, rates, n_req, sat_requests, tuning_arg, L=SE
     return {"metric": "served GCDs/s and p50/p99 latency (scheduled arrival -> result)", "unit": "GCDs/s, ms",
             "workload": "mixed 1k-64k-bit + 1% 1M-bit requests, Poisson arrivals, 8 GB admission budget",
             "modulus_bits": L, "tuning": tuning, "rows": rows, "saturation": sat, "server": stats,
-            "bit_exact": all(r["bit_exact"] for r in rows) and (sat is None or sat["bit_exact"])}
+            "bit_exact": all(r["bit_exact"] for r in rows) and (sat is None or sat["bit_exact"]) and
+                         stats["waves_only_10k"]["bit_exact"]}
 
 
 def run_sweep(args, rank, local):

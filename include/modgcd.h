@@ -240,6 +240,13 @@ int mgcd_certify_inverse(mgcd_context *ctx, uint64_t *checked, uint64_t *failure
    with MGCD_ERR_BUSY.  While a server runs, the context's own calls return MGCD_ERR_BUSY. */
 typedef struct mgcd_server mgcd_server;
 int mgcd_serve_start(mgcd_context *ctx, size_t budget_bytes, mgcd_server **server);
+/* Continuous lanes (the default) for requests of size classes 0-1 (up to 4,096 reference
+   moduli): each class has a ring in pinned, mapped host memory and persistent kernels that
+   take new requests from it into the slots that free up while they run (no wave has to
+   form or drain); CTAs that stay idle for 0.3 ms leave.  Larger requests take waves.
+   enable = 0 routes every request through waves.  Only while no request is queued or in
+   flight (else MGCD_ERR_BUSY). */
+int mgcd_serve_set_continuous(mgcd_server *server, int enable);
 /* Answers every submitted request, then stops the server thread and frees the server. */
 int mgcd_serve_stop(mgcd_server *server);
 /* Queues gcd(u, v) (operands copied; either order; zero operands allowed). */
@@ -300,6 +307,26 @@ int mgcd_gcd_digits_noalloc(const uint32_t *d_limbs, size_t uSz, size_t vSz, mgc
    the surviving moduli), recovery updates (the same over digits) and operand bytes. */
 int mgcd_batch_work(const mgcd_context *ctx, double *residue_steps, double *euclid_updates,
                     double *recovery_updates, double *operand_bytes);
+/* Occupancy trace of the batched kernels (no counterpart in the reference, whose single
+   kernel has no such accounting): when enabled, every CTA of the next runs' size-class
+   kernels records its SM, its start and end times (the GPU's global timer) and the pairs
+   it took from its queue; mgcd_batch_cta_trace copies the last run's records (launch
+   order; times in ms from the earliest CTA start) after waiting for the run.  Off by
+   default; switching it drops a recorded graph. */
+typedef struct {
+  int32_t size_class;
+  uint32_t sm, pairs;
+  int32_t ran;         /* 0: the CTA never started (or the run has not completed) */
+  double t_start_ms, t_end_ms;
+  /* K-slot CTAs (0 elsewhere): SM clock cycles in set-up (residues, first pivot), the
+     reduction-loop updates, the pivot choice and bookkeeping (including the wait for the
+     slowest warp of the update), and finish (certification, replay, recovery); reduction
+     iterations; moduli rounds (sum over iterations of the update loop's trips per thread);
+     the part of finish spent in certification and replay */
+  uint64_t cycles_setup, cycles_update, cycles_pivot, cycles_finish, iterations, rounds, cycles_replay;
+} mgcd_cta_record;
+int mgcd_set_cta_trace(mgcd_context *ctx, int enable);
+int mgcd_batch_cta_trace(mgcd_context *ctx, mgcd_cta_record *out, size_t cap, size_t *n);
 /* Algorithmic bytes of the last downloaded batch, the unit of the memory roofline: per
    pair, its operand limbs (4 bytes each), a prime and an 8-byte constant for every modulus
    it used (12 bytes each; the reference reads the prime, GmpCudaDevice-getGcdKernel.cu:335,

@@ -57,6 +57,8 @@ SIGNATURES = {
     "mgcd_batch_work": (_c.c_int, [_P, _c.POINTER(_c.c_double), _c.POINTER(_c.c_double),
                                    _c.POINTER(_c.c_double), _c.POINTER(_c.c_double)]),
     "mgcd_batch_alg_bytes": (_c.c_int, [_P, _c.POINTER(_c.c_double)]),
+    "mgcd_set_cta_trace": (_c.c_int, [_P, _c.c_int]),
+    "mgcd_batch_cta_trace": (_c.c_int, [_P, _P, _c.c_size_t, _c.POINTER(_c.c_size_t)]),
     "mgcd_batch_elapsed_ms": (_c.c_int, [_P, _c.POINTER(_c.c_float), _c.POINTER(_c.c_float),
                                          _c.POINTER(_c.c_int)]),
     "mgcd_batch_transfer_bytes": (_c.c_int, [_P, _c.POINTER(_c.c_uint64), _c.POINTER(_c.c_uint64)]),
@@ -86,6 +88,7 @@ SIGNATURES = {
     "mgcd_load_tuning": (_c.c_int, [_P, _c.c_char_p]),
     "mgcd_save_tuning": (_c.c_int, [_P, _c.c_char_p]),
     "mgcd_serve_start": (_c.c_int, [_P, _c.c_size_t, _P]),
+    "mgcd_serve_set_continuous": (_c.c_int, [_P, _c.c_int]),
     "mgcd_serve_stop": (_c.c_int, [_P]),
     "mgcd_serve_submit": (_c.c_int, [_P, _P, _c.c_size_t, _P, _c.c_size_t, _c.POINTER(_c.c_uint64)]),
     "mgcd_serve_poll": (_c.c_int, [_P, _c.c_uint64, _c.POINTER(_c.c_int)]),
@@ -442,6 +445,19 @@ class Device:
         _check(self._lib.mgcd_int_peak(self._h, ctypes.byref(x)))
         return x.value
 
+    def set_cta_trace(self, enable=True):
+        """Record per-CTA occupancy of the batched kernels in later runs."""
+        _check(self._lib.mgcd_set_cta_trace(self._h, int(bool(enable))))
+
+    def batch_cta_trace(self):
+        """The last run's per-CTA records (structured array, CTA_RECORD)."""
+        n = ctypes.c_size_t()
+        _check(self._lib.mgcd_batch_cta_trace(self._h, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value, dtype=CTA_RECORD)
+        if n.value:
+            _check(self._lib.mgcd_batch_cta_trace(self._h, out.ctypes.data, n.value, ctypes.byref(n)))
+        return out
+
     def batch_work(self):
         r, e, m, b = (ctypes.c_double() for _ in range(4))
         _check(self._lib.mgcd_batch_work(self._h, ctypes.byref(r), ctypes.byref(e), ctypes.byref(m),
@@ -450,6 +466,12 @@ class Device:
         _check(self._lib.mgcd_batch_alg_bytes(self._h, ctypes.byref(ab)))
         return {"residue_steps": r.value, "euclid_updates": e.value, "recovery_updates": m.value,
                 "operand_bytes": b.value, "algorithmic_bytes": ab.value}
+
+
+CTA_RECORD = np.dtype([("size_class", "<i4"), ("sm", "<u4"), ("pairs", "<u4"), ("ran", "<i4"),
+                       ("t_start_ms", "<f8"), ("t_end_ms", "<f8"), ("cycles_setup", "<u8"),
+                       ("cycles_update", "<u8"), ("cycles_pivot", "<u8"), ("cycles_finish", "<u8"),
+                       ("iterations", "<u8"), ("rounds", "<u8"), ("cycles_replay", "<u8")])
 
 
 class Server:
@@ -479,6 +501,10 @@ class Server:
 
     def __exit__(self, *exc):
         self.close()
+
+    def set_continuous(self, enable=True):
+        """Continuous lanes for size classes 0-1 (default on) or waves for every request."""
+        _check(self._lib.mgcd_serve_set_continuous(self._h, int(bool(enable))))
 
     def submit(self, u, v):
         a, b = to_limbs(u), to_limbs(v)

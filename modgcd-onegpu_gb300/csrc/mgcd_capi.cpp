@@ -323,7 +323,8 @@ int mgcd_moduli(const mgcd_context* c, uint32_t* out, size_t n)
 // ------------------------------------------------------------------------- batch ----
 
 static int schedule(mgcd_context* c, Plan& P, const std::vector<PairDesc>& descs, const std::vector<uint32_t>& subset,
-                    bool plain, std::vector<Bucket>& buckets, std::vector<uint32_t>& grid_pairs, size_t& scratch);
+                    bool plain, std::vector<Bucket>& buckets, std::vector<uint32_t>& grid_pairs, size_t& scratch,
+                    bool latency = false);
 
 int mgcd::plan_batch(mgcd_context* c, Plan& P, size_t np, const uint32_t* limbs, const uint64_t* u_off,
                      const uint32_t* u_len, const uint64_t* v_off, const uint32_t* v_len, bool plain)
@@ -430,12 +431,42 @@ int mgcd::plan_batch(mgcd_context* c, Plan& P, size_t np, const uint32_t* limbs,
 
 // Groups the pairs `subset` (indices into descs) into size-class buckets (batches) or
 // single-pair launches (plain); appends the processing order to P.order and returns the
-// scratch words needed.
+// scratch words needed.  `latency`: the few pairs rerun after a scaled batch -- one
+// launch in which every pair has a thread-block cluster of its own (about 512 moduli per
+// CTA), so that they run side by side across the GPU instead of one CTA each.
 static int schedule(mgcd_context* c, Plan& P, const std::vector<PairDesc>& descs, const std::vector<uint32_t>& subset,
-                    bool plain, std::vector<Bucket>& buckets, std::vector<uint32_t>& grid_pairs, size_t& scratch)
+                    bool plain, std::vector<Bucket>& buckets, std::vector<uint32_t>& grid_pairs, size_t& scratch,
+                    bool latency)
 {
   buckets.clear();
   grid_pairs.clear();
+  if (latency && !subset.empty()) {
+    std::vector<uint32_t> v(subset);
+    std::sort(v.begin(), v.end(), [&](uint32_t x, uint32_t y) { return descs[x].nq > descs[y].nq; });
+    Bucket bk;
+    bk.threads = 512;
+    bk.k = 1;
+    bk.cls = CLUSTER_CLASS;
+    bk.first = (uint32_t)P.order.size();
+    bk.n = (uint32_t)v.size();
+    bk.nq_max = descs[v[0]].nq;
+    bk.scratch_off = scratch;
+    int cs = 2;
+    while (cs < MAX_CLUSTER && (bk.nq_max + cs - 1) / cs > 512u) cs *= 2;
+    const size_t room = c->smem_optin - 24576;
+    while (cs < MAX_CLUSTER && cluster_batch_smem_bytes(cs, bk.nq_max, 1) > room) cs *= 2;
+    bk.csize = cs;
+    bk.smem = cluster_batch_smem_bytes(cs, bk.nq_max, 1);
+    int nc = 0;
+    if (bk.smem > room || cluster_batch_max_clusters(bk.threads, 1, cs, bk.smem, &nc) != cudaSuccess || nc < 1)
+      return MGCD_ERR_GRID;
+    bk.grid = (int)std::min<size_t>(v.size(), (size_t)nc);
+    scratch += (size_t)bk.grid * 4 * bk.nq_max;
+    P.order.insert(P.order.end(), v.begin(), v.end());
+    buckets.push_back(bk);
+    P.grid_scratch_off = scratch;
+    return MGCD_OK;
+  }
   const uint32_t plain_cta_max = 256;   // single pairs: one CTA, else a cluster or a grid
   std::vector<uint32_t> byb[NSTREAMS];
   for (uint32_t k : subset) {
@@ -507,13 +538,40 @@ static int schedule(mgcd_context* c, Plan& P, const std::vector<PairDesc>& descs
 // first of the bucket work counters (zeroed here).
 static int launch_set(mgcd_context* c, Plan& P, const std::vector<Bucket>& buckets,
                       const std::vector<uint32_t>& grid_pairs, const std::vector<PairDesc>& descs, PairDesc* pairs,
-                      uint32_t* queue_base, bool time_buckets)
+                      uint32_t* queue_base, bool time_buckets, bool traced = true)
 {
   CK(cudaMemsetAsync(queue_base, 0, NSTREAMS * sizeof(uint32_t), P.stream));
+  unsigned long long* trace = nullptr;
+  unsigned long long* phases = nullptr;
+  if (c->trace && traced) {
+    size_t ctas = 0;
+    for (const Bucket& bk : buckets) ctas += (size_t)bk.grid * (bk.csize ? bk.csize : 1);
+    if (P.d_trace.bytes < std::max<size_t>(ctas, 1) * 4 * sizeof(unsigned long long) ||
+        P.d_phases.bytes < std::max<size_t>(ctas, 1) * 8 * sizeof(unsigned long long)) {
+      P.drop_graph();
+      P.d_trace.release(P.stream);
+      P.d_phases.release(P.stream);
+      CK(P.d_trace.grow(std::max<size_t>(ctas, 1) * 4 * sizeof(unsigned long long), c->pool, P.stream));
+      CK(P.d_phases.grow(std::max<size_t>(ctas, 1) * 8 * sizeof(unsigned long long), c->pool, P.stream));
+    }
+    CK(cudaMemsetAsync(P.d_trace.p, 0, ctas * 4 * sizeof(unsigned long long), P.stream));
+    CK(cudaMemsetAsync(P.d_phases.p, 0, ctas * 8 * sizeof(unsigned long long), P.stream));
+    trace = P.d_trace.as<unsigned long long>();
+    phases = P.d_phases.as<unsigned long long>();
+    P.trace_cls.clear();
+  }
   CK(cudaEventRecord(P.ev_start, P.stream));
   for (size_t b = 0; b < buckets.size(); ++b) {
     const Bucket& bk = buckets[b];
-    BatchArgs a;
+    BatchArgs a{};
+    a.trace = trace;
+    a.phases = phases;
+    if (trace) {
+      const int n = bk.grid * (bk.csize ? bk.csize : 1);
+      trace += 4 * (size_t)n;
+      phases += 8 * (size_t)n;
+      P.trace_cls.insert(P.trace_cls.end(), n, bk.cls);
+    }
     a.stage_fail = c->stage_fail_cta;
     a.inv = InvTab{c->d_invtab.as<uint32_t>(), c->invtab_n};
     a.limbs = P.d_limbs.as<uint32_t>();
@@ -719,7 +777,7 @@ int mgcd::sync_plan(mgcd_context* c, Plan& P)
   std::vector<uint32_t> gp;
   size_t scratch = 0;
   const size_t keep_grid_off = P.grid_scratch_off;
-  int rc = schedule(c, P, rd, redo, false, bks, gp, scratch);
+  int rc = schedule(c, P, rd, redo, false, bks, gp, scratch, true);
   if (rc != MGCD_OK) return rc;
   // device buffers: retry descriptors after the main ones, retry order after the main order
   cudaStream_t s = P.stream;
@@ -741,7 +799,8 @@ int mgcd::sync_plan(mgcd_context* c, Plan& P)
   CK(cudaMemcpyAsync(P.d_retry.p, rd.data(), ng * sizeof(PairDesc), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(P.d_order.as<uint32_t>() + main_order, P.order.data() + main_order,
                      (P.order.size() - main_order) * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
-  rc = launch_set(c, P, bks, gp, rd, P.d_retry.as<PairDesc>(), P.d_queue.as<uint32_t>() + NSTREAMS, false);
+  rc = launch_set(c, P, bks, gp, rd, P.d_retry.as<PairDesc>(), P.d_queue.as<uint32_t>() + NSTREAMS, false,
+                  false);                   // the trace keeps the main run
   P.order.resize(main_order);               // the plan itself is unchanged for later runs
   P.grid_scratch_off = keep_grid_off;
   if (rc == MGCD_OK) rc = launch_convert(c, P);   // same digit and limb slots: convert again
@@ -903,7 +962,7 @@ static bool valid_class_cfg(int cls, int threads, int k, float nq_scale)
 {
   if (cls < 0 || cls >= NSTREAMS || !(nq_scale >= 0.5f && nq_scale <= 1.0f)) return false;
   if (threads != 256 && threads != 512 && threads != 1024) return false;
-  if (k == 8) return threads == 512 && cls != CLUSTER_CLASS;
+  if (k == 8) return (threads == 512 || threads == 1024) && cls != CLUSTER_CLASS;
   return k == 1 || k == 2 || k == 4;
 }
 
@@ -1184,6 +1243,49 @@ int mgcd_batch_alg_bytes(const mgcd_context* c, double* alg_bytes)
 {
   if (!c || !alg_bytes) return MGCD_ERR_INVALID_ARG;
   *alg_bytes = c->main.alg_bytes;
+  return MGCD_OK;
+}
+
+int mgcd_set_cta_trace(mgcd_context* c, int enable)
+{
+  if (!c) return MGCD_ERR_INVALID_ARG;
+  if (c->trace != (enable != 0)) c->main.drop_graph();
+  c->trace = enable != 0;
+  return MGCD_OK;
+}
+
+int mgcd_batch_cta_trace(mgcd_context* c, mgcd_cta_record* out, size_t cap, size_t* n)
+{
+  if (!c || !n || (cap && !out)) return MGCD_ERR_INVALID_ARG;
+  Plan& P = c->main;
+  const size_t ctas = c->trace ? P.trace_cls.size() : 0;
+  *n = ctas;
+  if (!ctas || !cap) return MGCD_OK;
+  if (!P.ran) return MGCD_ERR_INVALID_ARG;
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(P.stream));
+  std::vector<unsigned long long> raw(4 * ctas), ph(8 * ctas);
+  CK(cudaMemcpy(raw.data(), P.d_trace.p, raw.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(ph.data(), P.d_phases.p, ph.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+  unsigned long long t0 = ~0ull;
+  for (size_t i = 0; i < ctas; ++i)
+    if (raw[4 * i]) t0 = std::min(t0, raw[4 * i]);
+  for (size_t i = 0; i < ctas && i < cap; ++i) {
+    mgcd_cta_record& r = out[i];
+    r.size_class = P.trace_cls[i];
+    r.sm = (uint32_t)raw[4 * i + 2];
+    r.pairs = (uint32_t)raw[4 * i + 3];
+    r.ran = raw[4 * i] != 0 && raw[4 * i + 1] != 0;
+    r.t_start_ms = r.ran ? (double)(raw[4 * i] - t0) * 1e-6 : 0.0;
+    r.t_end_ms = r.ran ? (double)(raw[4 * i + 1] - t0) * 1e-6 : 0.0;
+    r.cycles_setup = ph[8 * i];
+    r.cycles_update = ph[8 * i + 1];
+    r.cycles_pivot = ph[8 * i + 2];
+    r.cycles_finish = ph[8 * i + 3];
+    r.iterations = ph[8 * i + 4];
+    r.rounds = ph[8 * i + 5];
+    r.cycles_replay = ph[8 * i + 7];
+  }
   return MGCD_OK;
 }
 

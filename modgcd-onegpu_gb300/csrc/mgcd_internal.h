@@ -50,6 +50,24 @@ struct InvTab {
   uint32_t n;
 };
 
+// Continuous serving: a lane's persistent K-slot kernel (batchk_kernel in ring mode) takes
+// requests from this ring while it runs.  The ring lives in pinned, mapped host memory:
+// the host writes an entry's descriptor, operands and digit slots there and publishes it
+// by a release store of `tail`; a CTA with a free slot claims the next entry through the
+// device counter `head` (compare-and-swap below the tail it acquired), computes it and
+// writes its digits, count and status there, then releases done[i] = i + 1.
+constexpr uint32_t STREAM_RING = 2048;
+struct StreamRing {
+  uint32_t tail;                     // entries published (host release store, kernel acquire load)
+  uint32_t stop;                     // host: the lane's kernels leave as soon as they are idle
+  uint32_t pad_[30];
+  PairDesc desc[STREAM_RING];        // entry i at i % STREAM_RING
+  uint32_t done[STREAM_RING];        // i + 1 once entry i's results are written (kernel release store)
+  uint32_t count[STREAM_RING];
+  int32_t status[STREAM_RING];
+  uint32_t iters[STREAM_RING];
+};
+
 struct BatchArgs {
   InvTab inv;
   const uint32_t* limbs;
@@ -67,6 +85,13 @@ struct BatchArgs {
   uint32_t* iters;           // reduction iterations per pair (work accounting)
   int32_t* status;
   uint32_t stage_fail;       // test hook: this CTA reports an operand-staging failure (~0: none)
+  unsigned long long* trace; // per CTA: start and end (globaltimer ns), SM id, pairs taken (null: off)
+  unsigned long long* phases; // per CTA (K-slot kernel): clock cycles of thread 0 in set-up, update,
+                              // pivot choice and finish, reduction iterations, moduli rounds, pairs,
+                              // cycles of certification and replay (null: off)
+  StreamRing* ring;          // ring mode (device view of the mapped ring)
+  uint32_t* ring_head;       // entries claimed (device memory)
+  unsigned long long idle_ns;  // ring mode: a CTA whose slots are all empty leaves after this long idle
 };
 
 // State of the cross-CTA reduction used by a single pair spread over a cooperative grid.
@@ -113,6 +138,9 @@ struct GridArgs {
 size_t batch_smem_bytes(int threads, int k, uint32_t nq_max);
 cudaError_t batch_max_blocks_per_sm(int threads, int k, bool narrow, size_t smem, int* blocks);
 cudaError_t launch_batch(const BatchArgs& a, int threads, int k, int grid, size_t smem, cudaStream_t s);
+// The same K-slot kernel in ring mode (continuous serving, a.ring set): threads 512 or 1024,
+// k 2 or 4.
+cudaError_t launch_ring(const BatchArgs& a, int threads, int k, int grid, size_t smem, cudaStream_t s);
 
 // One pair on a cluster of `ctas` CTAs (<= 16) of `threads` threads; same arguments and
 // shared-memory size as the grid path.

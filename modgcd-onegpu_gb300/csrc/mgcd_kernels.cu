@@ -29,6 +29,67 @@
 
 namespace mgcd {
 
+// Occupancy trace of the persistent kernels (BatchArgs::trace): when and where each CTA
+// ran and how many pairs it took, for the step's SM-busy accounting.
+__device__ __forceinline__ void trace_begin(unsigned long long* t)
+{
+  if (t && threadIdx.x == 0) {
+    uint32_t sm;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(sm));
+    t[4 * blockIdx.x] = globaltimer_ns();
+    t[4 * blockIdx.x + 2] = sm;
+  }
+}
+
+__device__ __forceinline__ void trace_end(unsigned long long* t, uint32_t pairs)
+{
+  if (t && threadIdx.x == 0) {
+    t[4 * blockIdx.x + 1] = globaltimer_ns();
+    t[4 * blockIdx.x + 3] = pairs;
+  }
+}
+
+// ---- continuous serving: the ring of a lane kernel (StreamRing)
+constexpr uint32_t NO_ENTRY = 0xFFFFFFFFu;
+
+__device__ __forceinline__ uint32_t ld_acquire_sys_u32(const uint32_t* p)
+{
+  uint32_t v;
+  asm volatile("ld.acquire.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_release_sys_u32(uint32_t* p, uint32_t v)
+{
+  asm volatile("st.release.sys.global.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
+
+// Thread 0: the next published entry (claimed through the head counter below the acquired
+// tail), or NO_ENTRY.  With `wait`, polls (bounded by a.idle_ns, or until the host asks
+// the lane to stop) while nothing is published.
+__device__ uint32_t stream_claim(const BatchArgs& a, bool wait)
+{
+  const unsigned long long t0 = globaltimer_ns();
+  for (;;) {
+    const uint32_t tail = ld_acquire_sys_u32(&a.ring->tail);
+    uint32_t h = *reinterpret_cast<volatile uint32_t*>(a.ring_head);
+    while ((int32_t)(tail - h) > 0) {
+      const uint32_t got = atomicCAS(a.ring_head, h, h + 1u);
+      if (got == h) return h;
+      h = got;
+    }
+    if (!wait || ld_acquire_sys_u32(&a.ring->stop) != 0u) return NO_ENTRY;
+    if (globaltimer_ns() - t0 > a.idle_ns) return NO_ENTRY;
+    __nanosleep(256);
+  }
+}
+
+// Thread 0, after the entry's results (written by this thread) are out.
+__device__ __forceinline__ void stream_done(const BatchArgs& a, uint32_t k)
+{
+  st_release_sys_u32(&a.ring->done[k % STREAM_RING], k + 1u);
+}
+
 // Persistent batched kernel: each CTA repeatedly takes the next pair of the queue (pairs
 // ordered largest first) and computes its gcd alone.
 template <int T>
@@ -47,18 +108,22 @@ __global__ void __launch_bounds__(T) batch_kernel(const BatchArgs a)
   uint32_t* u0 = scr;
   uint32_t* v0 = scr + a.nq_max;
   int2* hist = reinterpret_cast<int2*>(scr + 2 * (size_t)a.nq_max);
+  trace_begin(a.trace);
+  uint32_t taken = 0;
   for (;;) {
     if (threadIdx.x == 0) next = atomicAdd(a.queue, 1u);
     __syncthreads();
     const uint32_t k = next;
     __syncthreads();
     if (k >= a.npairs) break;
+    ++taken;
     const uint32_t pi = a.order[k];
     const PairDesc d = a.pairs[pi];
     run_pair<T, SYNC_CTA>(a.limbs, d, a.mods, a.L, 0u, d.nq, st, acc2, stg, rs, u0, v0, hist, nullptr,
                        a.digits, a.count + pi, a.iters + pi, a.status + pi, a.inv);
     __syncthreads();
   }
+  trace_end(a.trace, taken);
 }
 
 // ------------------------------------------------------- K pairs per CTA, lockstep ----
@@ -120,48 +185,127 @@ __device__ __forceinline__ void put(V (&a)[K], int s, V v)
     if (t == s) a[t] = v;
 }
 
+// Per-slot loop state of batchk_kernel in shared memory.  Warp s owns slot s's entries
+// during the pivot step; every thread reads them only after a barrier that follows the
+// writes, and the next writes come only after a barrier that follows the reads.  Keeping it
+// out of the registers leaves the K pivots and the K running minima as the only per-slot
+// registers of the update loop.
+template <int K>
+struct SlotState {
+  unsigned long long key[K][32];     // per-warp minima per slot (read by warp s after the barrier)
+  PairDesc d[K];
+  uint32_t pi[K];                    // pair index of each slot
+  long long lu[K], lv[K];            // certification bounds (bound_step)
+  uint32_t p[K];                     // current pivot (modulus, signed value) of each slot
+  int32_t b[K];
+  int32_t rem[K], ubits[K], vbits[K];  // surviving moduli and the reference's size estimates
+  uint32_t iters[K];
+  uint32_t res[K];                   // slot_step's result for the slot's last pivot
+  uint32_t seq[K];                   // ring mode: the slot's entry number
+  uint32_t stop;                     // set-up: slot_step's result for the first pivot
+};
+
+// One reduction-loop step of slot s's bookkeeping for its current pivot (the reference's
+// per-iteration checks, GmpCudaDevice-getGcdKernel.cu:365-402): records (p, b) in the
+// history and steps the size bounds; returns 0 (continue), 1 (loop ended: b = INF) or 3
+// (ran out of moduli).  One thread per slot.
+template <int K>
+__device__ __forceinline__ uint32_t slot_step(SlotState<K>& ss, int s, int2* hist, int L)
+{
+  const uint32_t p = ss.p[s];
+  const int32_t b = ss.b[s];
+  if (b == MOD_INFINITY) return 1u;
+  hist[ss.iters[s]] = make_int2((int)p, b);
+  bound_step(ss.lu[s], ss.lv[s], p, b);
+  ss.iters[s] += 1u;
+  const int rem = ss.rem[s] - 1;
+  ss.rem[s] = rem;
+  const uint32_t ab = b < 0 ? 0u - (uint32_t)b : (uint32_t)b;
+  const int tbits = ss.ubits[s] - (L - 1) + __ffs((int)ab);
+  const int ub = ss.vbits[s];
+  ss.ubits[s] = ub;
+  ss.vbits[s] = tbits;
+  return rem * (L - 2) <= ub ? 3u : 0u;
+}
+
 // NARROW: moduli below 2^30 (widths up to 30 bits), lazily reduced Montgomery products.
-template <int T, int K, bool NARROW = false>
+// RING: continuous serving -- pairs come from a.ring instead of the batch queue, empty
+// slots take newly published entries while the others run, and a CTA whose slots stay
+// empty for a.idle_ns leaves.
+template <int T, int K, bool NARROW = false, bool RING = false>
 __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
 {
+  constexpr int NW = T / 32;
+  static_assert(NW >= K, "one warp per slot reduces the slot's pivot");
   extern __shared__ __align__(16) uint32_t smem[];
-  __shared__ SlotSmem<K> ss;
+  __shared__ SlotState<K> ss;
   __shared__ RedSmem rs;
   __shared__ uint32_t next;
   __shared__ unsigned long long stage_bar[2];
   __shared__ uint32_t stage_state;
-  const Stage stg{smem, stage_bar, &stage_state, blockIdx.x == a.stage_fail};   // at dynamic smem start
+  // at dynamic smem start; in ring mode the operands are in host memory: plain coherent loads
+  const Stage stg = RING ? Stage{smem, nullptr, nullptr, 0u, 1u}
+                         : Stage{smem, stage_bar, &stage_state, blockIdx.x == a.stage_fail, 0u};
   stage_init(stg);
   const uint32_t NQS = a.nq_max;
   uint32_t* const tS = smem + STAGE_SMEM_WORDS;       // K x NQS states
   uint32_t* const acc2 = tS + (size_t)K * NQS;        // residues of v during set-up
   uint32_t* const scr = a.scratch + (size_t)blockIdx.x * a.scratch_words;   // per slot u0, v0, hist
   const int L = a.L;
-  uint32_t kparity = 0, rparity = 0, repoch = 0;
-  uint32_t valid = 0, active = 0, redux = 0;          // slots holding a pair / in the loop / ran out
-  int rem[K], ubits[K], vbits[K];
-  uint32_t iters[K], p[K], kh[K], kl[K];
-  int32_t b[K];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t rparity = 0, repoch = 0;
+  uint32_t valid = 0, active = 0, redux = 0;          // slots holding a pair / in the loop / ran out (uniform)
+  trace_begin(a.trace);
+  uint32_t taken = 0;
+  auto hist_of = [&](int s) { return reinterpret_cast<int2*>(scr + (size_t)s * 4 * NQS + 2 * (size_t)NQS); };
+  // phase accounting (a.phases): thread 0's clock in each phase; the phases end at barriers,
+  // so thread 0's timeline is the CTA's
+  const bool prof = a.phases != nullptr && threadIdx.x == 0;
+  unsigned long long ph_load = 0, ph_update = 0, ph_pivot = 0, ph_finish = 0, ph_iters = 0, ph_rounds = 0;
+  unsigned long long ph_replay = 0;   // the part of ph_finish spent in certification and replay
+  long long ph_t = prof ? clock64() : 0;
+  auto ph_mark = [&](unsigned long long& acc) {
+    if (prof) { const long long t = clock64(); acc += (unsigned long long)(t - ph_t); ph_t = t; }
+  };
 
-  // Takes the next pair of the queue into slot s: residues, initial ratios, first pivot.
+  // Takes the next pair of the queue (ring mode: of the ring; `wait` = poll, bounded, while
+  // nothing is published) into slot s: residues, initial ratios, first pivot and its
+  // bookkeeping step (bits 1, 3 of the result as slot_step's; bit 4: a pair was loaded).
   // A pair whose operands could not be staged is answered with ST_TIMEOUT.
-  auto load = [&](int s) -> bool {
+  auto load = [&](int s, bool wait) -> uint32_t {
     uint32_t* ts = tS + (size_t)s * NQS;
     for (;;) {
-      if (threadIdx.x == 0) next = atomicAdd(a.queue, 1u);
+      if (threadIdx.x == 0) {
+        if constexpr (RING) next = stream_claim(a, wait);
+        else next = atomicAdd(a.queue, 1u);
+      }
       __syncthreads();
       const uint32_t k = next;
       __syncthreads();
-      if (k >= a.npairs) return false;
+      if (RING ? k == NO_ENTRY : k >= a.npairs) return 0u;
+      ++taken;
       if (threadIdx.x == 0) {
-        ss.pi[s] = a.order[k];
-        ss.d[s] = a.pairs[ss.pi[s]];
+        if constexpr (RING) {                         // volatile: the host rewrites ring entries
+          const volatile PairDesc* e = &a.ring->desc[k % STREAM_RING];
+          PairDesc d;
+          d.u_off = e->u_off; d.v_off = e->v_off; d.u_len = e->u_len; d.v_len = e->v_len;
+          d.nq = e->nq; d.out_off = e->out_off; d.g_off = e->g_off; d.g_cap = e->g_cap; d.pad_ = 0u;
+          ss.pi[s] = k % STREAM_RING;
+          ss.seq[s] = k;
+          ss.d[s] = d;
+        } else {
+          ss.pi[s] = a.order[k];
+          ss.d[s] = a.pairs[ss.pi[s]];
+        }
       }
       __syncthreads();
       const PairDesc& d = ss.d[s];
       const bool staged = residues<T>(a.limbs + d.u_off, d.u_len, a.mods, d.nq, ts, stg, NARROW);
       if (residues<T>(a.limbs + d.v_off, d.v_len, a.mods, d.nq, acc2, stg, NARROW) && staged) break;
-      if (threadIdx.x == 0) { a.status[ss.pi[s]] = ST_TIMEOUT; a.count[ss.pi[s]] = 0; a.iters[ss.pi[s]] = 0; }
+      if (threadIdx.x == 0) {
+        a.status[ss.pi[s]] = ST_TIMEOUT; a.count[ss.pi[s]] = 0; a.iters[ss.pi[s]] = 0;
+        if constexpr (RING) stream_done(a, ss.seq[s]);
+      }
       __syncthreads();
     }
     const PairDesc& d = ss.d[s];
@@ -178,26 +322,42 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
       t_key(t, c.q, h, l);
       if (key_less(h, l, h0, l0)) { h0 = h; l0 = l; }
     }
-    if (threadIdx.x == 32u * s) {
+    block_min_key<T>(h0, l0, rs, rparity);
+    if (threadIdx.x == 0) {
+      uint32_t p0;
+      int32_t b0;
+      key_pair(h0, l0, p0, b0);
+      ss.p[s] = p0;
+      ss.b[s] = b0;
+      ss.rem[s] = (int)d.nq;
+      ss.ubits[s] = ((int)d.u_len + 1) * 32;
+      ss.vbits[s] = ((int)d.v_len + 1) * 32;
+      ss.iters[s] = 0u;
       ss.lu[s] = bound_init(a.limbs + d.u_off, d.u_len);
       ss.lv[s] = bound_init(a.limbs + d.v_off, d.v_len);
+      ss.stop = 16u | slot_step<K>(ss, s, hist_of(s), L);
     }
-    block_min_key<T>(h0, l0, rs, rparity);
-    uint32_t p0;
-    int32_t b0;
-    key_pair(h0, l0, p0, b0);
-    put(p, s, p0);
-    put(b, s, b0);
-    put(rem, s, (int)d.nq);
-    put(ubits, s, ((int)d.u_len + 1) * 32);
-    put(vbits, s, ((int)d.v_len + 1) * 32);
-    put(iters, s, 0u);
-    return true;
+    __syncthreads();
+    const uint32_t r = ss.stop;
+    __syncthreads();                                  // everyone has read it before it changes
+    return r;
+  };
+  auto take_slot = [&](int s, bool wait) {
+    ph_mark(ph_finish);
+    const uint32_t r = load(s, wait);
+    ph_mark(ph_load);
+    if (r & 16u) {
+      valid |= 1u << s;
+      if (!(r & 1u)) active |= 1u << s;
+      if ((r & 3u) == 3u) redux |= 1u << s;
+    }
   };
 
 #pragma unroll 1
-  for (int s = 0; s < K; ++s)
-    if (load(s)) { valid |= 1u << s; active |= 1u << s; }
+  for (int s = 0; s < K; ++s) {
+    take_slot(s, RING && s == 0);
+    if (RING && !((valid >> s) & 1u)) break;         // nothing more published now
+  }
 
   for (;;) {
     // ---- pairs whose reduction loop ended: finish them and refill their slots
@@ -206,50 +366,48 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
     for (int s = 0; s < K; ++s) {
       if (!((done >> s) & 1u)) continue;
       const uint32_t pi = ss.pi[s];
-      const uint32_t it = pick(iters, s);
+      const uint32_t it = ss.iters[s];
       if (threadIdx.x == 0) a.iters[pi] = it;
       if ((redux >> s) & 1u) {
         if (threadIdx.x == 0) { a.status[pi] = ST_REDUX; a.count[pi] = 0; }
       } else {
         uint32_t* u0 = scr + (size_t)s * 4 * NQS;
         finish_pair<T, SYNC_CTA>(a.mods, ss.d[s], L, 0u, ss.d[s].nq, tS + (size_t)s * NQS, rs, rparity, repoch, nullptr,
-                              u0, u0 + NQS, reinterpret_cast<const int2*>(u0 + 2 * (size_t)NQS), it, pick(rem, s),
-                              ss.lu[s], ss.lv[s], a.digits, a.count + pi, a.status + pi, a.inv);
+                              u0, u0 + NQS, reinterpret_cast<const int2*>(u0 + 2 * (size_t)NQS), it, ss.rem[s],
+                              ss.lu[s], ss.lv[s], a.digits, a.count + pi, a.status + pi, a.inv, smem,
+                              a.phases ? &ph_replay : nullptr);
       }
+      if (RING && threadIdx.x == 0) stream_done(a, ss.seq[s]);   // results written by this thread
       __syncthreads();
       valid &= ~(1u << s);
       redux &= ~(1u << s);
-      if (load(s)) { valid |= 1u << s; active |= 1u << s; }
+      if (!RING) take_slot(s, false);
+    }
+    if constexpr (RING) {
+      // empty slots take newly published entries while the others run; with every slot
+      // empty, wait (bounded) for one, else leave
+#pragma unroll 1
+      for (int s = 0; s < K; ++s) {
+        if ((valid >> s) & 1u) continue;
+        take_slot(s, valid == 0u);
+        if (!((valid >> s) & 1u)) break;
+      }
     }
     if (!valid) break;
+    ph_mark(ph_finish);
 
-    // ---- per-pair bookkeeping for this iteration's pivots (GmpCudaDevice-getGcdKernel.cu:365-402)
-#pragma unroll
-    for (int s = 0; s < K; ++s) {
-      if (!((active >> s) & 1u)) continue;
-      if (b[s] == MOD_INFINITY) { active &= ~(1u << s); continue; }
-      int2* hist = reinterpret_cast<int2*>(scr + (size_t)s * 4 * NQS + 2 * (size_t)NQS);
-      if (threadIdx.x == 32u * s) {   // one warp per slot keeps the history and the size bounds
-        hist[iters[s]] = make_int2((int)p[s], b[s]);
-        bound_step(ss.lu[s], ss.lv[s], p[s], b[s]);
-      }
-      ++iters[s];
-      rem[s] -= 1;
-      const uint32_t ab = b[s] < 0 ? 0u - (uint32_t)b[s] : (uint32_t)b[s];
-      const int tbits = ubits[s] - (L - 1) + __ffs((int)ab);
-      ubits[s] = vbits[s];
-      vbits[s] = tbits;
-      if (rem[s] * (L - 2) <= ubits[s]) { redux |= 1u << s; active &= ~(1u << s); }
-    }
-    if (!active) continue;
-
-    // ---- one update of every active pair, then the next pivots
+    // ---- one update of every active pair with its current pivot
+    uint32_t p[K], kh[K], kl[K];
+    int32_t b[K];
     uint32_t nq_max = 0;
 #pragma unroll
     for (int s = 0; s < K; ++s) {
+      p[s] = ss.p[s];
+      b[s] = ss.b[s];
       if ((active >> s) & 1u) nq_max = max(nq_max, ss.d[s].nq);
       kh[s] = kl[s] = 0xFFFFFFFFu;
     }
+    if (prof) { ++ph_iters; ph_rounds += (nq_max + T - 1) / T; }
     for (uint32_t j = threadIdx.x; j < nq_max; j += T) {
       uint32_t m = 0, tv[K];
 #pragma unroll
@@ -271,11 +429,44 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
         if (key_less(h, l, kh[s], kl[s])) { kh[s] = h; kl[s] = l; }
       }
     }
-    block_min_keys<T, K>(kh, kl, ss, kparity);
+    ph_mark(ph_update);
+    // ---- the next pivots (GmpCudaDevice-getGcdKernel.cu:365-402): warp minima, one
+    // barrier, then warp s reduces slot s's minima, stores its pivot and steps its
+    // bookkeeping (the K slots in parallel)
 #pragma unroll
-    for (int s = 0; s < K; ++s)
-      if ((active >> s) & 1u) key_pair(kh[s], kl[s], p[s], b[s]);
+    for (int s = 0; s < K; ++s) {
+      warp_min_key(kh[s], kl[s]);
+      if (lane == 0) ss.key[s][w] = ((unsigned long long)kh[s] << 32) | kl[s];
+    }
+    __syncthreads();
+    if (w < K && ((active >> w) & 1u)) {
+      const unsigned long long k = (lane < NW) ? ss.key[w][lane] : ~0ull;
+      uint32_t h = (uint32_t)(k >> 32), l = (uint32_t)k;
+      warp_min_key(h, l);
+      if (lane == 0) {
+        key_pair(h, l, ss.p[w], ss.b[w]);
+        ss.res[w] = slot_step<K>(ss, w, hist_of(w), L);
+      }
+    }
+    __syncthreads();
+    // ss.res changes next after the next iteration's first barrier (or inside a refill,
+    // after its barriers): every thread has read it by then
+#pragma unroll
+    for (int s = 0; s < K; ++s) {
+      if (!((active >> s) & 1u)) continue;
+      const uint32_t r = ss.res[s];
+      if (r & 1u) active &= ~(1u << s);
+      if (r & 2u) redux |= 1u << s;
+    }
+    ph_mark(ph_pivot);
   }
+  ph_mark(ph_finish);
+  if (prof) {
+    unsigned long long* o = a.phases + 8 * (size_t)blockIdx.x;
+    o[0] = ph_load; o[1] = ph_update; o[2] = ph_pivot; o[3] = ph_finish; o[4] = ph_iters; o[5] = ph_rounds;
+    o[6] = taken; o[7] = ph_replay;
+  }
+  trace_end(a.trace, taken);
 }
 
 // ------------------------------------------- K pairs per thread-block cluster, lockstep ----
@@ -346,6 +537,8 @@ __global__ void __launch_bounds__(T) cluster_batchk_kernel(const BatchArgs a)
   int rem[K], ubits[K], vbits[K];
   uint32_t iters[K], p[K], kh[K], kl[K];
   int32_t b[K];
+  trace_begin(a.trace);
+  uint32_t taken = 0;
 
   cluster_sync_all();
   // Takes the next pair of the queue into slot s.  A CTA whose operands could not be staged
@@ -365,6 +558,7 @@ __global__ void __launch_bounds__(T) cluster_batchk_kernel(const BatchArgs a)
       const uint32_t k = ck.next;
       cluster_sync_all();                             // everyone has read next before it changes
       if (k >= a.npairs) return false;
+      ++taken;
       if (threadIdx.x == 0) {
         ss.pi[s] = a.order[k];
         ss.d[s] = a.pairs[ss.pi[s]];
@@ -439,7 +633,7 @@ __global__ void __launch_bounds__(T) cluster_batchk_kernel(const BatchArgs a)
         finish_pair<T, SYNC_CLUSTER>(a.mods, ss.d[s], L, j0, ck.nloc[s], tS + (size_t)s * per, rs, rparity, repoch,
                                      gcs, u0 + j0, u0 + NQS + j0, reinterpret_cast<const int2*>(u0 + 2 * (size_t)NQS),
                                      it, pick(rem, s), ss.lu[s], ss.lv[s], a.digits, a.count + pi, a.status + pi,
-                                     a.inv);
+                                     a.inv, smem);
       }
       cluster_sync_all();                             // the slot's scratch is free in every CTA
       valid &= ~(1u << s);
@@ -501,6 +695,7 @@ __global__ void __launch_bounds__(T) cluster_batchk_kernel(const BatchArgs a)
       if ((active >> s) & 1u) key_pair(kh[s], kl[s], p[s], b[s]);
   }
   cluster_sync_all();   // no CTA leaves while others may still address its shared memory
+  trace_end(a.trace, taken);
 }
 
 // One pair over a cooperative grid of GRID_THREADS-thread CTAs; CTA c owns moduli
@@ -604,6 +799,8 @@ __global__ void __launch_bounds__(T) cluster_batch_kernel(const BatchArgs a)
   uint32_t* st = smem + STAGE_SMEM_WORDS;
   uint32_t* acc2 = st + per_max;
   uint32_t* scr = a.scratch + (size_t)(blockIdx.x / C) * a.scratch_words;
+  trace_begin(a.trace);
+  uint32_t taken = 0;
   cluster_sync_all();
   for (;;) {
     if (r == 0 && threadIdx.x < C) {
@@ -616,6 +813,7 @@ __global__ void __launch_bounds__(T) cluster_batch_kernel(const BatchArgs a)
     cluster_sync_all();
     const uint32_t k = next;
     if (k >= a.npairs) break;
+    ++taken;
     const uint32_t pi = a.order[k];
     const PairDesc d = a.pairs[pi];
     const uint32_t per = (d.nq + C - 1) / C;
@@ -627,6 +825,7 @@ __global__ void __launch_bounds__(T) cluster_batch_kernel(const BatchArgs a)
     cluster_sync_all();   // every CTA is done with `next` and with the pair's scratch
   }
   cluster_sync_all();     // no CTA leaves while others may still address its shared memory
+  trace_end(a.trace, taken);
 }
 
 // Integer-pipe microbenchmark: eight independent IMAD chains per thread.
@@ -717,7 +916,13 @@ static const void* batchk_fn_for(int threads, int k)
       default: return nullptr;
     }
   }
-  if (k == 8 && threads == 512) return reinterpret_cast<const void*>(&batchk_kernel<512, 8, NARROW>);
+  if (k == 8) {
+    switch (threads) {
+      case 512: return reinterpret_cast<const void*>(&batchk_kernel<512, 8, NARROW>);
+      case 1024: return reinterpret_cast<const void*>(&batchk_kernel<1024, 8, NARROW>);
+      default: return nullptr;
+    }
+  }
   return nullptr;
 }
 
@@ -742,6 +947,33 @@ cudaError_t batch_max_blocks_per_sm(int threads, int k, bool narrow, size_t smem
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, fn, threads, smem);
+}
+
+static const void* ring_fn_for(int threads, int k, bool narrow)
+{
+  if (threads == 1024 && k == 4)
+    return narrow ? reinterpret_cast<const void*>(&batchk_kernel<1024, 4, true, true>)
+                  : reinterpret_cast<const void*>(&batchk_kernel<1024, 4, false, true>);
+  if (threads == 1024 && k == 2)
+    return narrow ? reinterpret_cast<const void*>(&batchk_kernel<1024, 2, true, true>)
+                  : reinterpret_cast<const void*>(&batchk_kernel<1024, 2, false, true>);
+  if (threads == 512 && k == 4)
+    return narrow ? reinterpret_cast<const void*>(&batchk_kernel<512, 4, true, true>)
+                  : reinterpret_cast<const void*>(&batchk_kernel<512, 4, false, true>);
+  if (threads == 512 && k == 2)
+    return narrow ? reinterpret_cast<const void*>(&batchk_kernel<512, 2, true, true>)
+                  : reinterpret_cast<const void*>(&batchk_kernel<512, 2, false, true>);
+  return nullptr;
+}
+
+cudaError_t launch_ring(const BatchArgs& a, int threads, int k, int grid, size_t smem, cudaStream_t s)
+{
+  const void* fn = ring_fn_for(threads, k, a.L <= 30);
+  if (!fn || !a.ring) return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  void* args[] = {const_cast<BatchArgs*>(&a)};
+  return cudaLaunchKernel(fn, dim3(grid), dim3(threads), args, smem, s);
 }
 
 cudaError_t launch_batch(const BatchArgs& a, int threads, int k, int grid, size_t smem, cudaStream_t s)

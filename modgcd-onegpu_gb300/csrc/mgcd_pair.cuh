@@ -11,6 +11,8 @@
 namespace mgcd {
 
 constexpr int CHUNK = 1024;  // operand limbs staged per residue pass
+constexpr uint32_t REPLAY_CHUNK = 512;   // history entries per replay chunk (2 x 512 words of
+                                         // the operand staging area, which every kernel has)
 
 // How the CTAs that share one pair synchronise.
 enum SyncMode : int {
@@ -378,6 +380,8 @@ struct Stage {
   uint32_t* state;               // shared: bit b = parity of buffer b's next phase;
                                  // STAGE_BROKEN once a wait ran out
   uint32_t inject;               // test hook: report a failure after staging normally
+  uint32_t coherent;             // plain loads that bypass the non-coherent caches (operands in
+                                 // host memory that the host rewrites between requests)
 };
 constexpr uint32_t STAGE_BROKEN = 0x80000000u;
 
@@ -468,7 +472,12 @@ __device__ bool residues(const uint32_t* __restrict__ x, uint32_t n, const ModCo
       int lo, hi;
       stage_tile(t, (int)n, lo, hi);
       __syncthreads();
-      for (int i = lo + (int)threadIdx.x; i < hi; i += T) chunk[i - lo] = __ldg(x + i);
+      if (stg.coherent) {
+        const volatile uint32_t* xv = x;
+        for (int i = lo + (int)threadIdx.x; i < hi; i += T) chunk[i - lo] = xv[i];
+      } else {
+        for (int i = lo + (int)threadIdx.x; i < hi; i += T) chunk[i - lo] = __ldg(x + i);
+      }
       __syncthreads();
       const int len = hi - lo;
       for (uint32_t j = threadIdx.x; j < nloc; j += T) acc[j] = horner_tile(acc[j], chunk, len, mods[j], narrow);
@@ -525,7 +534,7 @@ __device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d
                             uint32_t* st, RedSmem& rs, uint32_t& parity, uint32_t& epoch, GridSync* gs,
                             const uint32_t* u0g, const uint32_t* v0g, const int2* hist, uint32_t iters, int remaining,
                             long long lu, long long lv, mgcd_pair* digits, uint32_t* count, int32_t* status,
-                            InvTab inv);
+                            InvTab inv, uint32_t* hbuf, unsigned long long* prof_replay = nullptr);
 
 // The whole gcd of one pair by this CTA (GRID = false) or by the cooperative grid, the
 // calling CTA owning global moduli [j0, j0 + nloc).
@@ -620,7 +629,7 @@ __device__ void run_pair(const uint32_t* __restrict__ limbs, const PairDesc& d, 
   }
   if (writer) *iters_out = iters;
   finish_pair<T, MODE>(mods, d, L, j0, nloc, st, rs, parity, epoch, gs, u0g, v0g, hist, iters, remaining, lu, lv,
-                       digits, count, status, inv);
+                       digits, count, status, inv, stg.buf);
 }
 
 // Recovery (MGCD4, GmpCudaDevice-getGcdKernel.cu:404-443) for a pair spread over several
@@ -813,11 +822,12 @@ __device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d
                             uint32_t* st, RedSmem& rs, uint32_t& parity, uint32_t& epoch, GridSync* gs,
                             const uint32_t* u0g, const uint32_t* v0g, const int2* hist, uint32_t iters, int remaining,
                             long long lu, long long lv, mgcd_pair* digits, uint32_t* count, int32_t* status,
-                            InvTab inv)
+                            InvTab inv, uint32_t* hbuf, unsigned long long* prof_replay)
 {
   const bool writer = threadIdx.x == 0 && lead_cta<MODE>();
   const ModConst* __restrict__ my = mods + j0;
   uint32_t p, kh, kl;
+  const long long t_begin = prof_replay ? clock64() : 0;   // phase accounting: certification + replay
   // Certify the result: all surviving residues of v are 0, so v = 0 if the surviving
   // moduli (each > 2^(L-1)) multiply to more than |v|; recovery is exact if they exceed
   // 2|u| (symmetric digits).  Otherwise report that more moduli are needed.
@@ -841,23 +851,82 @@ __device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d
 
   // ---- replay: u mod q of the surviving moduli from (u0, v0) and the (p, b) history.
   // Invariant (U, V) = s * (u_i, v_i) mod q; each step (U, V, s) <- (V p, U - b V, s p) / R.
-  for (uint32_t j = threadIdx.x; j < nloc; j += T) {
-    if (st[j] == T_RETIRED) { st[j] = U_RETIRED; continue; }
-    const ModConst c = my[j];
-    const uint32_t q = c.q, qi = c.qinv;
-    uint32_t U = u0g[j], V = v0g[j], s = 1u;
-    for (uint32_t i = 0; i < iters; ++i) {
-      const int2 h = hist[i];
-      const uint32_t pp = (uint32_t)h.x;
-      const uint32_t pm = pp > q ? pp - q : pp;
-      const uint32_t bn = from_signed(-h.y, q);                 // -b mod q
-      const uint32_t U2 = mont_mul(V, pm, q, qi);
-      const uint32_t V2 = redc((uint64_t)bn * V + U, q, qi);
-      s = mont_mul(s, pm, q, qi);
-      U = U2;
-      V = V2;
+  // Moduli below 2^30 keep U, V, s lazily in [0, 2q) (bn V + U < 2q^2 + 2q < q 2^32, so the
+  // REDC without its final subtraction stays below 2q).  The history is read from global
+  // memory in chunks of REPLAY_CHUNK entries staged into shared memory (hbuf) by the whole
+  // CTA, so every step reads a broadcast from shared memory instead of waiting on a global
+  // load; a thread replays its surviving moduli one per pass (passes = the CTA's largest
+  // survivor count of one thread).
+  const bool narrow = L <= 30;
+  {
+    __shared__ uint32_t npass;
+    uint32_t mine = 0;
+    for (uint32_t j = threadIdx.x; j < nloc; j += T) mine += st[j] != T_RETIRED;
+    if (threadIdx.x == 0) npass = 0u;
+    __syncthreads();
+    if (mine) atomicMax(&npass, mine);
+    __syncthreads();
+    const uint32_t passes = npass;
+    int2* const hb = reinterpret_cast<int2*>(hbuf);
+    uint32_t jn = threadIdx.x;                         // next candidate modulus of this thread
+    for (uint32_t pass = 0; pass < passes; ++pass) {
+      uint32_t j = jn;
+      while (j < nloc && st[j] == T_RETIRED) j += T;
+      const bool have = j < nloc;
+      jn = j + T;
+      const ModConst c = my[have ? j : 0u];
+      const uint32_t q = c.q, qi = c.qinv;
+      uint32_t U = have ? u0g[j] : 0u, V = have ? v0g[j] : 0u, sc = 1u;
+      for (uint32_t c0 = 0; c0 < iters; c0 += REPLAY_CHUNK) {
+        const uint32_t n = iters - c0 < REPLAY_CHUNK ? iters - c0 : REPLAY_CHUNK;
+        __syncthreads();                               // the previous chunk is consumed
+        for (uint32_t e = threadIdx.x; e < n; e += T) hb[e] = hist[c0 + e];
+        __syncthreads();
+        if (!have) continue;
+        if (narrow) {
+#pragma unroll 4
+          for (uint32_t e = 0; e < n; ++e) {
+            const int2 h = hb[e];
+            const uint32_t pp = (uint32_t)h.x;
+            const uint32_t pm = pp > q ? pp - q : pp;
+            const uint32_t bn = from_signed(-h.y, q);
+            const uint64_t T2 = (uint64_t)bn * V + U;
+            const uint32_t U2 = mont_mul_lazy(V, pm, q, qi);
+            const uint32_t lo = (uint32_t)T2, hi = (uint32_t)(T2 >> 32);
+            V = hi + __umulhi(lo * qi, q) + (lo != 0u);
+            sc = mont_mul_lazy(sc, pm, q, qi);
+            U = U2;
+          }
+        } else {
+#pragma unroll 4
+          for (uint32_t e = 0; e < n; ++e) {
+            const int2 h = hb[e];
+            const uint32_t pp = (uint32_t)h.x;
+            const uint32_t pm = pp > q ? pp - q : pp;
+            const uint32_t bn = from_signed(-h.y, q);               // -b mod q
+            const uint32_t U2 = mont_mul(V, pm, q, qi);
+            const uint32_t V2 = redc((uint64_t)bn * V + U, q, qi);
+            sc = mont_mul(sc, pm, q, qi);
+            U = U2;
+            V = V2;
+          }
+        }
+      }
+      if (have) {
+        if (narrow) {
+          U = mod_canon(U, q);
+          sc = mod_canon(sc, q);
+        }
+        st[j] = mont_mul(U, inv_mod(redc((uint64_t)sc, q, qi), q, qi), q, qi);   // U / s
+      }
     }
-    st[j] = mont_mul(U, inv_mod(redc((uint64_t)s, q, qi), q, qi), q, qi);   // U / s
+    __syncthreads();                                   // hbuf and the replayed values
+    for (uint32_t j = threadIdx.x; j < nloc; j += T)
+      if (st[j] == T_RETIRED) st[j] = U_RETIRED;
+  }
+  if (prof_replay) {                   // non-null in every thread of the CTA or in none
+    __syncthreads();
+    if (threadIdx.x == 0) *prof_replay += (unsigned long long)(clock64() - t_begin);
   }
 
   if constexpr (MODE != SYNC_CTA) {   // several CTAs: recovery in panels

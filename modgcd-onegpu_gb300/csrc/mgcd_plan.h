@@ -82,6 +82,9 @@ struct Plan {
 
   DevBuf d_limbs, d_pairs, d_order, d_digits, d_count, d_iters, d_status, d_queue, d_scratch, d_gsync, d_retry;
   DevBuf d_glimbs, d_glen;             // binary gcds converted on the device
+  DevBuf d_trace;                      // per-CTA occupancy trace of the bucket kernels (4 words each)
+  DevBuf d_phases;                     // per-CTA phase accounting of the K-slot kernels (8 words each)
+  std::vector<int> trace_cls;          // size class of each traced CTA (launch order)
   HostBuf h_count, h_iters, h_status, h_digits, h_glimbs, h_glen;
   int launches = 0, retried = 0;
   bool ran = false, synced = false, bucket_timed = false;
@@ -123,6 +126,7 @@ struct mgcd_context {
   uint32_t withhold_cta = 0xFFFFFFFFu;                  // test hook (mgcd_test_withhold_cta)
   uint32_t stage_fail_cta = 0xFFFFFFFFu;                // test hook (mgcd_test_fail_staging)
   uint32_t force_nq = 0;                                // test hook (mgcd_test_force_moduli)
+  bool trace = false;                                   // record per-CTA occupancy (mgcd_set_cta_trace)
 };
 
 namespace mgcd {

@@ -1,20 +1,34 @@
 // mgcd_serve.cpp -- request server: continuous batching of single gcd requests on one GPU.
 // No counterpart in the reference (its GmpCudaDevice::gcd is one blocking call per pair).
 //
-// Requests are queued per lane (the batched path's size class of the pair).  A server
-// thread turns the queued requests of a lane into a wave -- one plan of the batched path
-// with its own streams and buffers -- as soon as that lane has a free wave slot and the
-// HBM admission budget allows, and launches it without waiting for the waves already on
-// the GPU: their persistent kernels are still draining while the new wave's CTAs take the
-// SMs they free, so the work of requests that arrived later overlaps with the earlier
-// ones'.  The moduli table, its Montgomery constants and the pairwise inverse table stay
-// resident in the context; a wave holds only its operands, residues, scratch and digits.
-// When a wave's completion event fires, its digits are copied back and converted and
-// every request of the wave is answered.
+// Requests are queued per lane (the batched path's size class of the pair).
+//
+// Continuous lanes (size classes 0-1, the default): each lane has a ring in pinned, mapped
+// host memory and persistent K-slot kernels (batchk_kernel in ring mode) that take entries
+// from it while they run.  The server thread admits a request by writing its operands and
+// descriptor into a free ring entry and publishing it (a release store of the tail); a CTA
+// whose slot frees up claims it at the next iteration of its reduction loop, so a request
+// joins kernels that are already running instead of waiting for a batch to form or to
+// drain.  A CTA releases done[i] once the entry's digits are written (to host memory); the
+// server converts them and answers.  A lane launches more CTAs while its requests in
+// flight and queued outnumber its running slots; CTAs whose slots stay empty leave after a
+// short idle time, so idle lanes hold no SMs.
+//
+// Waves (size classes 2-3, requests beyond a continuous lane's limits, and every lane when
+// continuous lanes are switched off): the server thread turns the queued requests of a
+// lane into a wave -- one plan of the batched path with its own streams and buffers -- as
+// soon as that lane has a free wave slot and the HBM admission budget allows, and launches
+// it without waiting for the waves already on the GPU.  When a wave's completion event
+// fires, its digits are copied back and converted and every request of the wave is
+// answered.
+//
+// The moduli table, its Montgomery constants and the pairwise inverse table stay resident
+// in the context for both.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -26,6 +40,7 @@
 #include "../../include/modgcd.h"
 #include "mgcd_moduli.h"
 #include "mgcd_plan.h"
+#include "mgcd_radix.h"
 
 using namespace mgcd;
 
@@ -51,11 +66,54 @@ struct Request {
   std::vector<uint32_t> limbs;         // u then v
   uint32_t ul = 0, vl = 0;
   int lane = 0;
+  int ref_nq = 0;                      // the reference's moduli count
+  bool stream = false;                 // served by the lane's continuous kernels
+  bool full = false;                   // (continuous) runs with the reference count
+  uint32_t seq = 0;                    // (continuous) ring entry number
   size_t bytes = 0;                    // device bytes while admitted
   double t_submit = 0, t_done = 0;
   std::vector<uint32_t> g;
   int status = -1;
   bool done = false;
+};
+
+// ---- continuous lanes
+// Size classes 0-1.  Class 2 (4,096-16,384 moduli) stays on waves: its pairs take ~100 ms on
+// one CTA of a K-slot kernel, ~45 ms on the 4-CTA clusters its waves use, and that latency,
+// not the wait for a slot, dominates its requests (measured: p99 of requests below 1M bits
+// 124-156 ms with class 2 continuous, against 82 ms with waves for every class).
+constexpr int STREAM_LANES = 2;
+constexpr uint32_t STREAM_NQ_CAP[STREAM_LANES] = {1024, 4096};   // largest reference count taken
+constexpr int STREAM_MAX_CTAS[STREAM_LANES] = {48, 112};         // CTAs a lane may run at once
+constexpr int STREAM_LANE_STREAMS = 8;                                 // instances of a lane in flight
+constexpr unsigned long long STREAM_IDLE_NS = 300000;                  // an idle CTA leaves after 0.3 ms
+
+struct StreamInstance {
+  cudaEvent_t done = nullptr;
+  int first = 0, ctas = 0;             // its CTAs' scratch slots
+  int stream = 0;                      // index into the lane's streams
+};
+
+struct StreamLane {
+  int lane = 0, k = 4, threads = 1024;
+  uint32_t nq_cap = 0, limb_cap = 0;   // per ring entry: moduli, operand limbs (u + v)
+  size_t smem = 0, scratch_words = 0;  // per CTA
+  StreamRing* ring_h = nullptr;        // pinned, mapped: host and device views
+  StreamRing* ring_d = nullptr;
+  uint32_t* limbs_h = nullptr;
+  uint32_t* limbs_d = nullptr;
+  mgcd_pair* dig_h = nullptr;
+  mgcd_pair* dig_d = nullptr;
+  uint32_t* d_head = nullptr;          // entries claimed (device counter)
+  uint32_t* d_scratch = nullptr;       // STREAM_MAX_CTAS slots of scratch_words
+  cudaStream_t streams[STREAM_LANE_STREAMS] = {};   // one per instance in flight: a launch on a
+  bool stream_busy[STREAM_LANE_STREAMS] = {};       // busy stream would queue behind it
+  uint32_t tail = 0;                   // entries published
+  std::vector<Request*> entry;         // by ring slot: the request in flight there
+  std::vector<uint32_t> live;          // entry numbers in flight
+  std::vector<char> slot_used;         // scratch slots held by running instances
+  std::vector<StreamInstance> inst;    // launched, not yet seen complete
+  int ctas = 0;                        // CTAs of those instances
 };
 
 struct Wave {
@@ -96,6 +154,11 @@ struct mgcd_server {
   std::mutex mu;
   std::condition_variable cv_done, cv_work;
   std::deque<Request*> pending[NLANES];
+  bool continuous = true;              // continuous lanes for size classes 0-1
+  StreamLane sl[STREAM_LANES];
+  std::deque<Request*> spending[STREAM_LANES];   // queued for the continuous lanes
+  std::deque<Request*> retry[STREAM_LANES];      // uncertified with a scaled count: rerun in full
+  size_t stream_live = 0;
   size_t queued = 0;
   std::unordered_map<uint64_t, Request*> table;
   uint64_t next_ticket = 1;
@@ -159,12 +222,267 @@ int finish_wave(mgcd_server* S, Wave& w)
   return MGCD_OK;
 }
 
+// ---- continuous lanes
+
+int cmp_limbs(const uint32_t* a, size_t an, const uint32_t* b, size_t bn)
+{
+  if (an != bn) return an < bn ? -1 : 1;
+  for (size_t i = an; i-- > 0;)
+    if (a[i] != b[i]) return a[i] < b[i] ? -1 : 1;
+  return 0;
+}
+
+// Ring, operand and digit areas (pinned, mapped), the claim counter and scratch of lane l.
+int lane_init(mgcd_server* S, StreamLane& L, int l, int priority)
+{
+  mgcd_context* c = S->c;
+  L.lane = l;
+  L.threads = c->cfg[l].threads >= 512 ? c->cfg[l].threads : 512;
+  L.k = c->cfg[l].k >= 4 ? 4 : 2;
+  L.nq_cap = STREAM_NQ_CAP[l];
+  while (L.k > 2 && batch_smem_bytes(L.threads, L.k, L.nq_cap) > c->smem_optin - 16384) L.k /= 2;
+  L.smem = batch_smem_bytes(L.threads, L.k, L.nq_cap);
+  if (L.smem > c->smem_optin - 16384) return MGCD_ERR_GRID;
+  // operand limbs of the largest pair whose reference count fits the cap
+  size_t lo = 2, hi = (size_t)32 * L.nq_cap * 4;
+  while (lo < hi) {
+    const size_t mid = (lo + hi + 1) / 2;
+    if (moduli_needed(c->L, mid) <= (int)L.nq_cap) lo = mid; else hi = mid - 1;
+  }
+  L.limb_cap = 2 * (uint32_t)((lo + 31) / 32);
+  L.scratch_words = 4 * (size_t)L.k * L.nq_cap;
+  L.entry.assign(STREAM_RING, nullptr);
+  L.slot_used.assign(STREAM_MAX_CTAS[l], 0);
+  const unsigned flags = cudaHostAllocMapped | cudaHostAllocPortable;
+  void* p = nullptr;
+  if (cudaHostAlloc(&p, sizeof(StreamRing), flags) != cudaSuccess) return MGCD_ERR_CUDA;
+  L.ring_h = static_cast<StreamRing*>(p);
+  std::memset(L.ring_h, 0, sizeof(StreamRing));
+  if (cudaHostAlloc(&p, (size_t)STREAM_RING * L.limb_cap * sizeof(uint32_t), flags) != cudaSuccess)
+    return MGCD_ERR_CUDA;
+  L.limbs_h = static_cast<uint32_t*>(p);
+  if (cudaHostAlloc(&p, (size_t)STREAM_RING * (L.nq_cap + 1) * sizeof(mgcd_pair), flags) != cudaSuccess)
+    return MGCD_ERR_CUDA;
+  L.dig_h = static_cast<mgcd_pair*>(p);
+  if (cudaHostGetDevicePointer(reinterpret_cast<void**>(&L.ring_d), L.ring_h, 0) != cudaSuccess ||
+      cudaHostGetDevicePointer(reinterpret_cast<void**>(&L.limbs_d), L.limbs_h, 0) != cudaSuccess ||
+      cudaHostGetDevicePointer(reinterpret_cast<void**>(&L.dig_d), L.dig_h, 0) != cudaSuccess)
+    return MGCD_ERR_CUDA;
+  if (cudaMalloc(reinterpret_cast<void**>(&L.d_head), sizeof(uint32_t)) != cudaSuccess ||
+      cudaMemset(L.d_head, 0, sizeof(uint32_t)) != cudaSuccess ||
+      cudaMalloc(reinterpret_cast<void**>(&L.d_scratch),
+                 (size_t)STREAM_MAX_CTAS[l] * L.scratch_words * sizeof(uint32_t)) != cudaSuccess)
+    return MGCD_ERR_CUDA;
+  for (cudaStream_t& st : L.streams)
+    if (cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, priority) != cudaSuccess) return MGCD_ERR_CUDA;
+  return MGCD_OK;
+}
+
+void lane_free(StreamLane& L)
+{
+  for (cudaStream_t st : L.streams)
+    if (st) cudaStreamSynchronize(st);
+  for (StreamInstance& x : L.inst)
+    if (x.done) cudaEventDestroy(x.done);
+  L.inst.clear();
+  for (cudaStream_t st : L.streams)
+    if (st) cudaStreamDestroy(st);
+  if (L.d_scratch) cudaFree(L.d_scratch);
+  if (L.d_head) cudaFree(L.d_head);
+  if (L.dig_h) cudaFreeHost(L.dig_h);
+  if (L.limbs_h) cudaFreeHost(L.limbs_h);
+  if (L.ring_h) cudaFreeHost(L.ring_h);
+  L = StreamLane();
+}
+
+bool lane_fits(const StreamLane& L, const Request* r)
+{
+  return L.ring_h && r->ul && r->vl && (uint32_t)r->ref_nq <= L.nq_cap && r->ul + r->vl <= L.limb_cap;
+}
+
+// Writes r into the next ring entry and publishes it; false if that entry is still in use.
+bool lane_publish(mgcd_server* S, StreamLane& L, Request* r)
+{
+  const uint32_t slot = L.tail % STREAM_RING;
+  if (L.entry[slot]) return false;
+  const uint32_t* u = r->limbs.data();
+  const uint32_t* v = u + r->ul;
+  uint32_t* dst = L.limbs_h + (size_t)slot * L.limb_cap;
+  PairDesc d;
+  const bool u_big = cmp_limbs(u, r->ul, v, r->vl) >= 0;
+  d.u_len = u_big ? r->ul : r->vl;
+  d.v_len = u_big ? r->vl : r->ul;
+  std::memcpy(dst, u_big ? u : v, d.u_len * sizeof(uint32_t));
+  std::memcpy(dst + d.u_len, u_big ? v : u, d.v_len * sizeof(uint32_t));
+  d.u_off = (uint64_t)slot * L.limb_cap;
+  d.v_off = d.u_off + d.u_len;
+  int nq = r->ref_nq;
+  const float scale = S->c->cfg[L.lane].nq_scale;
+  if (!r->full && scale < 1.0f) nq = std::min(nq, std::max(256, ((int)std::ceil(scale * nq) + 31) / 32 * 32));
+  d.nq = (uint32_t)nq;
+  d.out_off = slot * (L.nq_cap + 1);
+  d.g_off = 0;
+  d.g_cap = 0;
+  d.pad_ = 0;
+  L.ring_h->desc[slot] = d;
+  L.ring_h->done[slot] = 0u;
+  r->seq = L.tail;
+  r->full = r->full || nq == r->ref_nq;
+  L.entry[slot] = r;
+  L.live.push_back(L.tail);
+  ++L.tail;
+  __atomic_store_n(&L.ring_h->tail, L.tail, __ATOMIC_RELEASE);   // orders the entry before it
+  ++S->stream_live;
+  return true;
+}
+
+// Answers the lane's completed entries (called with the server lock held).
+bool lane_poll(mgcd_server* S, StreamLane& L)
+{
+  bool any = false;
+  for (size_t i = 0; i < L.live.size();) {
+    const uint32_t seq = L.live[i];
+    const uint32_t slot = seq % STREAM_RING;
+    if (__atomic_load_n(&L.ring_h->done[slot], __ATOMIC_ACQUIRE) != seq + 1u) {
+      ++i;
+      continue;
+    }
+    Request* r = L.entry[slot];
+    const int32_t st = L.ring_h->status[slot];
+    L.entry[slot] = nullptr;
+    L.live[i] = L.live.back();
+    L.live.pop_back();
+    --S->stream_live;
+    any = true;
+    if ((st == ST_INSUFFICIENT || st == ST_REDUX) && !r->full) {
+      r->full = true;                  // rerun with the reference count (as a batch does)
+      S->retry[L.lane].push_back(r);
+      continue;
+    }
+    int rc = to_status(st);
+    if (rc == MGCD_OK) {
+      const size_t cap = std::max<size_t>(1, std::max(r->ul, r->vl));
+      r->g.resize(cap);
+      size_t len = 0;
+      if (mixed_radix_to_limbs(L.dig_h + (size_t)slot * (L.nq_cap + 1), L.ring_h->count[slot], r->g.data(), cap, &len))
+        rc = MGCD_ERR_CAPACITY;
+      r->g.resize(rc == MGCD_OK ? len : 0);
+    }
+    r->status = rc;
+    r->t_done = now_s();
+    r->done = true;
+    r->limbs.clear();
+    r->limbs.shrink_to_fit();
+    S->n_done += 1;
+    S->in_flight -= r->bytes;
+  }
+  return any;
+}
+
+// Instances whose CTAs have all left give back their scratch slots and stream.
+void lane_reap(StreamLane& L)
+{
+  for (size_t i = 0; i < L.inst.size();) {
+    StreamInstance& x = L.inst[i];
+    if (cudaEventQuery(x.done) != cudaSuccess) {
+      ++i;
+      continue;
+    }
+    for (int j = 0; j < x.ctas; ++j) L.slot_used[x.first + j] = 0;
+    L.ctas -= x.ctas;
+    L.stream_busy[x.stream] = false;
+    cudaEventDestroy(x.done);
+    L.inst[i] = L.inst.back();
+    L.inst.pop_back();
+  }
+}
+
+// More CTAs while the entries in flight and queued outnumber the running slots.  An added
+// instance is at least as large as the CTAs already running (capped by the lane's share),
+// so a lane reaches its full size in a few launches even when its load grows slowly; the
+// instances stay resident while they find work.
+bool lane_launch(mgcd_server* S, StreamLane& L, size_t queued)
+{
+  const int cap = STREAM_MAX_CTAS[L.lane];
+  const size_t want = std::min<size_t>((L.live.size() + queued + L.k - 1) / L.k, (size_t)cap);
+  if (L.live.empty() || want <= (size_t)L.ctas) return false;
+  const int need = std::min(cap - L.ctas, std::max((int)want - L.ctas, L.ctas));
+  if (need <= 0) return false;
+  int si = 0;
+  while (si < STREAM_LANE_STREAMS && L.stream_busy[si]) ++si;
+  if (si == STREAM_LANE_STREAMS) return false;
+  // the longest run of free scratch slots, up to `need`
+  int best = -1, best_len = 0;
+  for (int j = 0; j < cap;) {
+    if (L.slot_used[j]) { ++j; continue; }
+    int e = j;
+    while (e < cap && !L.slot_used[e] && e - j < need) ++e;
+    if (e - j > best_len) { best = j; best_len = e - j; }
+    j = e + 1;
+  }
+  if (best < 0) return false;
+  mgcd_context* c = S->c;
+  BatchArgs a{};
+  a.inv = InvTab{c->d_invtab.as<uint32_t>(), c->invtab_n};
+  a.limbs = L.limbs_d;
+  a.pairs = L.ring_d->desc;
+  a.mods = c->mods.as<ModConst>();
+  a.L = c->L;
+  a.scratch = L.d_scratch + (size_t)best * L.scratch_words;
+  a.scratch_words = L.scratch_words;
+  a.nq_max = L.nq_cap;
+  a.digits = L.dig_d;
+  a.count = L.ring_d->count;
+  a.iters = L.ring_d->iters;
+  a.status = L.ring_d->status;
+  a.stage_fail = 0xFFFFFFFFu;
+  a.ring = L.ring_d;
+  a.ring_head = L.d_head;
+  a.idle_ns = STREAM_IDLE_NS;
+  StreamInstance x;
+  x.first = best;
+  x.ctas = best_len;
+  x.stream = si;
+  if (cudaEventCreateWithFlags(&x.done, cudaEventDisableTiming) != cudaSuccess) return false;
+  if (launch_ring(a, L.threads, L.k, best_len, L.smem, L.streams[si]) != cudaSuccess ||
+      cudaEventRecord(x.done, L.streams[si]) != cudaSuccess) {
+    cudaEventDestroy(x.done);
+    return false;
+  }
+  L.stream_busy[si] = true;
+  for (int j = 0; j < best_len; ++j) L.slot_used[best + j] = 1;
+  L.ctas += best_len;
+  L.inst.push_back(x);
+  ++S->n_launches;
+  return true;
+}
+
 void serve_loop(mgcd_server* S)
 {
   cudaSetDevice(S->c->device);
   std::unique_lock<std::mutex> lk(S->mu);
   for (;;) {
     bool progressed = false;
+    // ---- continuous lanes: answer completed entries, admit queued requests into free
+    // ring entries (reruns first), add CTAs while entries outnumber running slots
+    for (int l = 0; l < STREAM_LANES; ++l) {
+      StreamLane& L = S->sl[l];
+      if (!L.ring_h) continue;
+      if (lane_poll(S, L)) { progressed = true; S->cv_done.notify_all(); }
+      lane_reap(L);
+      while (!S->retry[l].empty() && lane_publish(S, L, S->retry[l].front())) S->retry[l].pop_front();
+      auto& q = S->spending[l];
+      while (!q.empty() && S->retry[l].empty() && S->in_flight + q.front()->bytes <= S->budget) {
+        Request* r = q.front();
+        if (!lane_publish(S, L, r)) break;
+        q.pop_front();
+        --S->queued;
+        S->in_flight += r->bytes;
+        S->peak_bytes = std::max(S->peak_bytes, S->in_flight);
+        progressed = true;
+      }
+      while (lane_launch(S, L, q.size() + S->retry[l].size())) progressed = true;
+    }
     // ---- completed waves: answer their requests
     for (Wave& w : S->waves) {
       if (!w.busy) continue;
@@ -246,7 +564,8 @@ void serve_loop(mgcd_server* S)
       }
       progressed = true;
     }
-    bool any_busy = false;
+    bool any_busy = S->stream_live > 0;
+    for (int l = 0; l < STREAM_LANES; ++l) any_busy = any_busy || !S->retry[l].empty();
     for (const Wave& w : S->waves) any_busy = any_busy || w.busy;
     if (S->stop && S->queued == 0 && !any_busy) break;
     if (!progressed) S->cv_work.wait_for(lk, std::chrono::microseconds(any_busy ? 20 : 500));
@@ -275,6 +594,7 @@ int submit_at(mgcd_server* S, const uint32_t* u, size_t uSz, const uint32_t* v, 
   r->ul = (uint32_t)ul;
   r->vl = (uint32_t)vl;
   r->lane = size_class((uint32_t)nq);
+  r->ref_nq = nq;
   // device bytes while admitted: operands, descriptor and order entry, digit slots, status
   // words, and the pair's share of the reduction scratch (u0, v0, (p, b) history)
   r->bytes = 4 * (ul + vl) + sizeof(PairDesc) + 4 + 8 * ((size_t)nq + 1) + 12 + 16 * (size_t)nq;
@@ -295,7 +615,9 @@ int submit_at(mgcd_server* S, const uint32_t* u, size_t uSz, const uint32_t* v, 
     r->ticket = S->next_ticket++;
     r->t_submit = t_submit > 0 ? t_submit : now_s();
     S->table[r->ticket] = r;
-    S->pending[r->lane].push_back(r);
+    r->stream = S->continuous && r->lane < STREAM_LANES && lane_fits(S->sl[r->lane], r);
+    if (r->stream) S->spending[r->lane].push_back(r);
+    else S->pending[r->lane].push_back(r);
     ++S->queued;
     *ticket = r->ticket;
   }
@@ -370,6 +692,16 @@ int mgcd_serve_start(mgcd_context* c, size_t budget_bytes, mgcd_server** out)
     delete S;
     return rc;
   }
+  for (int l = 0; l < STREAM_LANES && rc == MGCD_OK; ++l) rc = lane_init(S, S->sl[l], l, greatest);
+  if (rc != MGCD_OK) {
+    for (int l = 0; l < STREAM_LANES; ++l) lane_free(S->sl[l]);
+    for (Wave& w : S->waves) {
+      w.plan.destroy(c->pool);
+      if (w.done) cudaEventDestroy(w.done);
+    }
+    delete S;
+    return rc;
+  }
   // Reserve pool memory up front so that waves allocate from it without the driver mapping
   // new memory while kernels run (the pool keeps freed memory).
   {
@@ -395,6 +727,10 @@ int mgcd_serve_stop(mgcd_server* S)
   S->cv_work.notify_all();
   if (S->th.joinable()) S->th.join();
   cudaSetDevice(S->c->device);
+  for (int l = 0; l < STREAM_LANES; ++l) {
+    if (S->sl[l].ring_h) __atomic_store_n(&S->sl[l].ring_h->stop, 1u, __ATOMIC_RELEASE);   // idle CTAs leave
+    lane_free(S->sl[l]);
+  }
   for (Wave& w : S->waves) {
     w.plan.destroy(S->c->pool);
     w.staging.release();
@@ -410,6 +746,15 @@ int mgcd_serve_submit(mgcd_server* S, const uint32_t* u, size_t uSz, const uint3
                       uint64_t* ticket)
 {
   return submit_at(S, u, uSz, v, vSz, 0.0, ticket);
+}
+
+int mgcd_serve_set_continuous(mgcd_server* S, int enable)
+{
+  if (!S) return MGCD_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> g(S->mu);
+  if (!S->table.empty()) return MGCD_ERR_BUSY;
+  S->continuous = enable != 0;
+  return MGCD_OK;
 }
 
 int mgcd_serve_poll(mgcd_server* S, uint64_t ticket, int* done)

@@ -129,7 +129,7 @@ def test_tuning_table_roundtrip_and_bad_tables(mgcd, tmp_path):
         assert (t, k) == (256, 2) and abs(s - 0.9) < 1e-6
         assert dev.get_cluster_size() == 4
         before = [dev.get_size_class(c) for c in range(4)]
-        for bad in ("1 256 2 0.9 0\n2 1024 8 1.0 0\n",      # k = 8 needs 512 threads
+        for bad in ("1 256 2 0.9 0\n2 256 8 1.0 0\n",       # k = 8 needs 512 or 1024 threads
                     "3 1024 1 1.0 0\n",                       # class 3 needs a cluster size
                     "0 256 4 0.4 0\n",                        # scale below 0.5
                     "0 256 4\n"):                             # short line
@@ -164,7 +164,7 @@ def test_cluster_class_k_pairs_per_cluster(mgcd, threads, k, ctas, scale):
         assert dev.gcd_batch(us, vs) == [math.gcd(a, b) for a, b in zip(us, vs)]
 
 
-@pytest.mark.parametrize("threads,k", [(512, 4), (512, 8), (1024, 4)])
+@pytest.mark.parametrize("threads,k", [(512, 4), (512, 8), (1024, 4), (1024, 8)])
 def test_pairs_per_cta_step_down_when_shared_memory_is_short(mgcd, threads, k):
     """A size-class-2 pair near 16,384 moduli with k pairs per CTA would need more than one
     CTA's shared memory; the bucket runs with fewer pairs per CTA instead of failing."""
@@ -199,3 +199,32 @@ def test_size_classes_on_clusters(mgcd, cls_cfg):
             dev.batch_run()
             dev.batch_sync()
             assert _results(mgcd, dev) == exp
+
+
+@pytest.mark.parametrize("L,scale", [(27, 0.76), (32, 0.8)])
+def test_eight_pairs_per_cta(mgcd, L, scale):
+    """K = 8 pairs per 1024-thread CTA share one inverse per modulus: the mixed batch (with
+    scaled moduli counts, so some pairs may be rerun) gives every gcd exactly."""
+    us, vs, _ = importlib.import_module("modgcd-onegpu_gb300.workloads").mixed_batch(400, seed=81)
+    exp = [math.gcd(a, b) for a, b in zip(us, vs)]
+    with mgcd.Device(0, L) as dev:
+        for cls in (0, 1, 2):
+            dev.set_size_class(cls, 1024, 8, scale)
+        assert dev.gcd_batch(us, vs) == exp
+
+
+def test_cta_trace_accounts_every_pair(mgcd):
+    """The occupancy trace: one record per CTA of the run, every pair counted once, phases
+    recorded for the K-slot CTAs, and the results unchanged with the trace on."""
+    us, vs, _ = importlib.import_module("modgcd-onegpu_gb300.workloads").mixed_batch(300, seed=82)
+    exp = [math.gcd(a, b) for a, b in zip(us, vs)]
+    with mgcd.Device(0, 27) as dev:
+        dev.load_tuning(mgcd.default_tuning_path(dev))
+        dev.set_cta_trace(True)
+        assert dev.gcd_batch(us, vs) == exp
+        rec = dev.batch_cta_trace()
+    assert len(rec) > 0 and (rec["ran"] != 0).all()
+    assert int(rec["pairs"].sum()) == len(us)
+    assert (rec["t_end_ms"] >= rec["t_start_ms"]).all()
+    kslot = rec[rec["iterations"] > 0]
+    assert len(kslot) > 0 and (kslot["cycles_update"] > 0).all()

@@ -2,6 +2,8 @@
 
 - Each result is the same alone (one request on an idle server) and in the mix (the same
   request among a Poisson stream of others of mixed sizes), and equals Python's gcd.
+- Continuous lanes take requests into running kernels (far fewer launches than requests)
+  and answer exactly what the wave path answers.
 - The admission budget is never exceeded and an oversize request is refused.
 - While a server runs, the context's own calls are refused; afterwards they work again.
 """
@@ -57,7 +59,7 @@ def test_admission_budget(mgcd):
             stats = srv.stats()
         assert got == [math.gcd(u, v) for u, v in zip(us, vs)]
         assert 0 < stats["peak_admitted_bytes"] <= budget
-        assert stats["waves"] > 1
+        assert stats["launches"] > 1
 
 
 def test_take_timeout_keeps_the_ticket(mgcd):
@@ -115,3 +117,36 @@ def test_many_threads_submit_and_take(mgcd):
     assert not errors, errors
     assert len(results) == 360
     assert all(got == exp for got, exp in results.values())
+
+
+def test_continuous_lanes_take_requests_while_running(mgcd):
+    """Requests arriving over ~40 ms (Poisson at 10k req/s, 1k-16k bits) are taken by the
+    lanes' running kernels as their slots free up: far fewer kernel launches than requests,
+    no wave at all, and every answer equals the wave path's and Python's gcd."""
+    us, vs, arr = wl.serve_requests(400, 10000.0, seed=17, big_frac=0.0, hi_bits=16384)
+    exp = [math.gcd(u, v) for u, v in zip(us, vs)]
+    with mgcd.Device(0, 32) as dev:
+        with mgcd.Server(dev) as srv:
+            got, st, lat, _ = srv.replay(us, vs, arr)
+            stats = srv.stats()
+        with mgcd.Server(dev) as srv:
+            srv.set_continuous(False)
+            got_w, st_w, _, _ = srv.replay(us, vs, arr)
+            stats_w = srv.stats()
+    assert got == exp and got_w == exp
+    assert (st == 0).all() and (st_w == 0).all()
+    assert stats["waves"] == 0 and 0 < stats["launches"] < len(us) // 4
+    assert stats_w["waves"] > 0
+
+
+def test_continuous_lanes_rerun_uncertified_pairs(mgcd):
+    """With moduli counts scaled far below the reference's, many requests cannot be
+    certified; the continuous lanes rerun them with the reference count and every answer
+    stays exact."""
+    us, vs, arr = wl.serve_requests(200, 20000.0, seed=18, big_frac=0.0, hi_bits=30000)
+    with mgcd.Device(0, 32) as dev:
+        dev.set_nq_scale(0.5)
+        with mgcd.Server(dev) as srv:
+            got, st, _, _ = srv.replay(us, vs, arr)
+    assert (st == 0).all()
+    assert got == [math.gcd(u, v) for u, v in zip(us, vs)]

@@ -374,7 +374,7 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
         uint32_t* u0 = scr + (size_t)s * 4 * NQS;
         finish_pair<T, SYNC_CTA>(a.mods, ss.d[s], L, 0u, ss.d[s].nq, tS + (size_t)s * NQS, rs, rparity, repoch, nullptr,
                               u0, u0 + NQS, reinterpret_cast<const int2*>(u0 + 2 * (size_t)NQS), it, ss.rem[s],
-                              ss.lu[s], ss.lv[s], a.digits, a.count + pi, a.status + pi, a.inv, smem,
+                              ss.lu[s], ss.lv[s], a.digits, a.count + pi, a.status + pi, a.inv, smem, acc2,
                               a.phases ? &ph_replay : nullptr);
       }
       if (RING && threadIdx.x == 0) stream_done(a, ss.seq[s]);   // results written by this thread
@@ -633,7 +633,7 @@ __global__ void __launch_bounds__(T) cluster_batchk_kernel(const BatchArgs a)
         finish_pair<T, SYNC_CLUSTER>(a.mods, ss.d[s], L, j0, ck.nloc[s], tS + (size_t)s * per, rs, rparity, repoch,
                                      gcs, u0 + j0, u0 + NQS + j0, reinterpret_cast<const int2*>(u0 + 2 * (size_t)NQS),
                                      it, pick(rem, s), ss.lu[s], ss.lv[s], a.digits, a.count + pi, a.status + pi,
-                                     a.inv, smem);
+                                     a.inv, smem, acc2);
       }
       cluster_sync_all();                             // the slot's scratch is free in every CTA
       valid &= ~(1u << s);

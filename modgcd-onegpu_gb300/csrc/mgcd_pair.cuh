@@ -534,7 +534,7 @@ __device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d
                             uint32_t* st, RedSmem& rs, uint32_t& parity, uint32_t& epoch, GridSync* gs,
                             const uint32_t* u0g, const uint32_t* v0g, const int2* hist, uint32_t iters, int remaining,
                             long long lu, long long lv, mgcd_pair* digits, uint32_t* count, int32_t* status,
-                            InvTab inv, uint32_t* hbuf, unsigned long long* prof_replay = nullptr);
+                            InvTab inv, uint32_t* hbuf, uint32_t* ibuf, unsigned long long* prof_replay = nullptr);
 
 // The whole gcd of one pair by this CTA (GRID = false) or by the cooperative grid, the
 // calling CTA owning global moduli [j0, j0 + nloc).
@@ -629,7 +629,7 @@ __device__ void run_pair(const uint32_t* __restrict__ limbs, const PairDesc& d, 
   }
   if (writer) *iters_out = iters;
   finish_pair<T, MODE>(mods, d, L, j0, nloc, st, rs, parity, epoch, gs, u0g, v0g, hist, iters, remaining, lu, lv,
-                       digits, count, status, inv, stg.buf);
+                       digits, count, status, inv, stg.buf, acc2);
 }
 
 // Recovery (MGCD4, GmpCudaDevice-getGcdKernel.cu:404-443) for a pair spread over several
@@ -822,7 +822,7 @@ __device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d
                             uint32_t* st, RedSmem& rs, uint32_t& parity, uint32_t& epoch, GridSync* gs,
                             const uint32_t* u0g, const uint32_t* v0g, const int2* hist, uint32_t iters, int remaining,
                             long long lu, long long lv, mgcd_pair* digits, uint32_t* count, int32_t* status,
-                            InvTab inv, uint32_t* hbuf, unsigned long long* prof_replay)
+                            InvTab inv, uint32_t* hbuf, uint32_t* ibuf, unsigned long long* prof_replay)
 {
   const bool writer = threadIdx.x == 0 && lead_cta<MODE>();
   const ModConst* __restrict__ my = mods + j0;
@@ -852,29 +852,25 @@ __device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d
   // ---- replay: u mod q of the surviving moduli from (u0, v0) and the (p, b) history.
   // Invariant (U, V) = s * (u_i, v_i) mod q; each step (U, V, s) <- (V p, U - b V, s p) / R.
   // Moduli below 2^30 keep U, V, s lazily in [0, 2q) (bn V + U < 2q^2 + 2q < q 2^32, so the
-  // REDC without its final subtraction stays below 2q).  The history is read from global
-  // memory in chunks of REPLAY_CHUNK entries staged into shared memory (hbuf) by the whole
-  // CTA, so every step reads a broadcast from shared memory instead of waiting on a global
-  // load; a thread replays its surviving moduli one per pass (passes = the CTA's largest
-  // survivor count of one thread).
+  // REDC without its final subtraction stays below 2q).  The surviving moduli are first
+  // listed in ibuf (shared, nloc words), so that thread t replays survivors t, t + T, ...
+  // with every lane busy; the history is read in chunks of REPLAY_CHUNK entries that the
+  // whole CTA stages into shared memory (hbuf), so every step reads a broadcast from shared
+  // memory instead of waiting on a global load.
   const bool narrow = L <= 30;
   {
-    __shared__ uint32_t npass;
-    uint32_t mine = 0;
-    for (uint32_t j = threadIdx.x; j < nloc; j += T) mine += st[j] != T_RETIRED;
-    if (threadIdx.x == 0) npass = 0u;
+    __shared__ uint32_t nsurv;
+    if (threadIdx.x == 0) nsurv = 0u;
     __syncthreads();
-    if (mine) atomicMax(&npass, mine);
+    for (uint32_t j = threadIdx.x; j < nloc; j += T)
+      if (st[j] != T_RETIRED) ibuf[atomicAdd(&nsurv, 1u)] = j;
     __syncthreads();
-    const uint32_t passes = npass;
+    const uint32_t ns = nsurv;
     int2* const hb = reinterpret_cast<int2*>(hbuf);
-    uint32_t jn = threadIdx.x;                         // next candidate modulus of this thread
-    for (uint32_t pass = 0; pass < passes; ++pass) {
-      uint32_t j = jn;
-      while (j < nloc && st[j] == T_RETIRED) j += T;
-      const bool have = j < nloc;
-      jn = j + T;
-      const ModConst c = my[have ? j : 0u];
+    for (uint32_t base = 0; base < ns; base += T) {
+      const bool have = base + threadIdx.x < ns;
+      const uint32_t j = have ? ibuf[base + threadIdx.x] : 0u;
+      const ModConst c = my[j];
       const uint32_t q = c.q, qi = c.qinv;
       uint32_t U = have ? u0g[j] : 0u, V = have ? v0g[j] : 0u, sc = 1u;
       for (uint32_t c0 = 0; c0 < iters; c0 += REPLAY_CHUNK) {
@@ -920,7 +916,7 @@ __device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d
         st[j] = mont_mul(U, inv_mod(redc((uint64_t)sc, q, qi), q, qi), q, qi);   // U / s
       }
     }
-    __syncthreads();                                   // hbuf and the replayed values
+    __syncthreads();                                   // hbuf, ibuf and the replayed values
     for (uint32_t j = threadIdx.x; j < nloc; j += T)
       if (st[j] == T_RETIRED) st[j] = U_RETIRED;
   }

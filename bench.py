@@ -21,12 +21,12 @@ Every result is compared bit for bit with GMP mpz_gcd.
 The default run then measures the other benchmark configurations, each with its own clock
 record and bit-exact check, as extra keys of the same line (--legs):
   single_pair_sweep  n-bit operands with an n/4-bit gcd, n = 4k .. 1M, at 22/27/32-bit moduli
+  paper_table1       random pairs of 16-352 Kibit, the setting of the reference paper's Table 1
   skewed             64 x 1M-bit + 16,384 pairs of 512-4096 bits in one CUDA graph launch
   serving            Poisson arrivals at 1k-200k req/s (1% 1M-bit requests) + a saturation replay
 
-Each of these also runs alone (--workload sweep|skewed|serve); --workload table1 runs single
-pairs in the setting of the reference paper's Table 1, --workload seeds the mixed batch of
-several seeds with one tuning table.
+Each of these also runs alone (--workload sweep|table1|skewed|serve); --workload seeds runs
+the mixed batch of several seeds with one tuning table.
 """
 import argparse
 import importlib
@@ -75,9 +75,9 @@ def parse():
     ap.add_argument("--reps", type=int, default=5, help="timed calls per size of the single-pair sweep")
     ap.add_argument("--serve-rates", default="1000,10000,50000,100000,200000",
                     help="arrival rates (req/s) of the serving leg")
-    ap.add_argument("--legs", default="sweep,skewed,serve",
+    ap.add_argument("--legs", default="sweep,table1,skewed,serve",
                     help="configurations measured after the mixed batch in the default run, each with its own "
-                         "clock record (comma list of sweep, skewed, serve; empty: none)")
+                         "clock record (comma list of sweep, table1, skewed, serve; empty: none)")
     ap.add_argument("--serve-requests", type=int, default=1000)
     ap.add_argument("--serve-sat-requests", type=int, default=8192,
                     help="requests of the serving saturation replay (1k-64k bits at 1M req/s; 0: none)")
@@ -450,6 +450,8 @@ def run_ours(args, rank, local, world, pg):
         if "sweep" in want:
             sizes = [int(x) for x in args.sizes.split(",")]
             legs["single_pair_sweep"] = timed_leg(local, lambda: sweep_leg(mg, wl, po, local, sizes, args.reps))
+        if "table1" in want:
+            legs["paper_table1"] = timed_leg(local, lambda: table1_leg(mg, wl, po, local))
         if "skewed" in want:
             legs["skewed"] = timed_leg(local, lambda: skewed_leg(mg, wl, po, local, None, 1))
         if "serve" in want:
@@ -711,7 +713,10 @@ def run_seeds(args, rank, local):
                 rerun = max(rerun, dev.batch_retried())
         g, go, gn, st = dev.batch_download()
         ok = bool((st == 0).all()) and results_equal(mg, g, go, gn, gx, gxo, gxn)
-        rows.append({"seed": seed, "ms_per_step": statistics.median(ms), "rerun_pairs": rerun, "bit_exact": ok})
+        w = dev.batch_work()
+        rows.append({"seed": seed, "ms_per_step": statistics.median(ms), "rerun_pairs": rerun, "bit_exact": ok,
+                     "euclid_updates": w["euclid_updates"],
+                     "ns_per_update": 1e6 * statistics.median(ms) / max(1.0, w["euclid_updates"])})
         print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
     clk = clocks.stop()
     dev.close()
@@ -721,6 +726,11 @@ def run_seeds(args, rank, local):
                       "pairs": args.pairs, "rows": rows, "median_ms": med,
                       "max_over_median": max(r["ms_per_step"] for r in rows) / med,
                       "spread": (max(r["ms_per_step"] for r in rows) - min(r["ms_per_step"] for r in rows)) / med,
+                      # the batches differ in work; time per reduction-loop update isolates the
+                      # tuning's behaviour (a rerun after the main launch would show here)
+                      "spread_per_update": (max(r["ns_per_update"] for r in rows) -
+                                            min(r["ns_per_update"] for r in rows)) /
+                                           statistics.median(r["ns_per_update"] for r in rows),
                       "clocks": clk, "bit_exact": all(r["bit_exact"] for r in rows)}), flush=True)
 
 
@@ -729,17 +739,11 @@ def run_seeds(args, rank, local):
 PAPER_V100_MS = {16: 7, 32: 13, 64: 25, 128: 46, 192: 73, 256: 118, 352: 184}
 
 
-def run_table1(args, rank, local):
+def table1_leg(mg, wl, po, local):
     """Single-pair latency in the setting of the reference paper's Table 1: 10 random pairs
     per size (planted gcd of 1 bit, i.e. random operands), 32-bit moduli, one pair per call,
     mean wall time per call with the context set up beforehand; beside it the paper's V100
     figure and GMP mpz_gcd on one host core (the paper's CPU column)."""
-    if rank != 0:
-        return
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import pyoracle as po
-    mg = importlib.import_module("modgcd-onegpu_gb300")
-    wl = importlib.import_module("modgcd-onegpu_gb300.workloads")
     dev = mg.Device(local, 32)
     rows = []
     for kib, v100 in sorted(PAPER_V100_MS.items()):
@@ -760,10 +764,22 @@ def run_table1(args, rank, local):
                      "bit_exact": bool(ok)})
         print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
     dev.close()
-    print(json.dumps({"metric": "single-pair gcd latency, the reference paper's Table 1 setting", "unit": "ms",
-                      "higher_is_better": False, "data": "synthetic (random pairs, seeds 1-10)",
-                      "config": {"modulus_bits": 32, "method": "plain (one pair per call)"},
-                      "rows": rows, "bit_exact": all(r["bit_exact"] for r in rows)}), flush=True)
+    return {"metric": "single-pair gcd latency, the reference paper's Table 1 setting", "unit": "ms",
+            "config": {"modulus_bits": 32, "method": "plain (one pair per call)",
+                       "pairs": "random operands, seeds 1-10 per size"},
+            "rows": rows, "bit_exact": all(r["bit_exact"] for r in rows)}
+
+
+def run_table1(args, rank, local):
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    mg = importlib.import_module("modgcd-onegpu_gb300")
+    wl = importlib.import_module("modgcd-onegpu_gb300.workloads")
+    res = timed_leg(local, lambda: table1_leg(mg, wl, po, local))
+    res.update({"higher_is_better": False, "data": "synthetic"})
+    print(json.dumps(res), flush=True)
 
 
 def main():

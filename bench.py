@@ -205,6 +205,13 @@ def occupancy(rec, sms):
             classes[str(c)]["iterations"] = int(r["iterations"].sum())
             classes[str(c)]["cycles_per_round"] = cyc["update"] / max(1.0, float(r["rounds"].sum()))
             classes[str(c)]["pivot_cycles_per_iteration"] = cyc["pivot"] / max(1.0, float(r["iterations"].sum()))
+            ur, ri, fs = (float(r[k].sum()) for k in ("update_rounds", "rounds_with_inverse", "finite_slot_updates"))
+            if ur > 0:
+                # liveness of the update loop: rounds where every slot's modulus was retired
+                # (or beyond its pair), and finite slot states per slot position of the rounds
+                # that computed an inverse
+                classes[str(c)]["update_liveness"] = {"rounds_without_inverse": 1.0 - ri / ur,
+                                                      "finite_slots_per_inverse": fs / max(1.0, ri)}
     return {"span_ms": span, "sms": sms, "sm_busy_frac": busy / (sms * span) if span > 0 else None,
             "by_class": classes}
 

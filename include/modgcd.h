@@ -322,8 +322,11 @@ typedef struct {
      reduction-loop updates, the pivot choice and bookkeeping (including the wait for the
      slowest warp of the update), and finish (certification, replay, recovery); reduction
      iterations; moduli rounds (sum over iterations of the update loop's trips per thread);
-     the part of finish spent in certification and replay */
+     the part of finish spent in certification and replay; summed over the CTA's threads:
+     update rounds (one modulus of every slot), the rounds in which some slot needed an
+     inverse, and the slot states updated through the inverse */
   uint64_t cycles_setup, cycles_update, cycles_pivot, cycles_finish, iterations, rounds, cycles_replay;
+  uint64_t update_rounds, rounds_with_inverse, finite_slot_updates;
 } mgcd_cta_record;
 int mgcd_set_cta_trace(mgcd_context *ctx, int enable);
 int mgcd_batch_cta_trace(mgcd_context *ctx, mgcd_cta_record *out, size_t cap, size_t *n);

@@ -547,15 +547,15 @@ static int launch_set(mgcd_context* c, Plan& P, const std::vector<Bucket>& bucke
     size_t ctas = 0;
     for (const Bucket& bk : buckets) ctas += (size_t)bk.grid * (bk.csize ? bk.csize : 1);
     if (P.d_trace.bytes < std::max<size_t>(ctas, 1) * 4 * sizeof(unsigned long long) ||
-        P.d_phases.bytes < std::max<size_t>(ctas, 1) * 8 * sizeof(unsigned long long)) {
+        P.d_phases.bytes < std::max<size_t>(ctas, 1) * PHASE_WORDS * sizeof(unsigned long long)) {
       P.drop_graph();
       P.d_trace.release(P.stream);
       P.d_phases.release(P.stream);
       CK(P.d_trace.grow(std::max<size_t>(ctas, 1) * 4 * sizeof(unsigned long long), c->pool, P.stream));
-      CK(P.d_phases.grow(std::max<size_t>(ctas, 1) * 8 * sizeof(unsigned long long), c->pool, P.stream));
+      CK(P.d_phases.grow(std::max<size_t>(ctas, 1) * PHASE_WORDS * sizeof(unsigned long long), c->pool, P.stream));
     }
     CK(cudaMemsetAsync(P.d_trace.p, 0, ctas * 4 * sizeof(unsigned long long), P.stream));
-    CK(cudaMemsetAsync(P.d_phases.p, 0, ctas * 8 * sizeof(unsigned long long), P.stream));
+    CK(cudaMemsetAsync(P.d_phases.p, 0, ctas * PHASE_WORDS * sizeof(unsigned long long), P.stream));
     trace = P.d_trace.as<unsigned long long>();
     phases = P.d_phases.as<unsigned long long>();
     P.trace_cls.clear();
@@ -569,7 +569,7 @@ static int launch_set(mgcd_context* c, Plan& P, const std::vector<Bucket>& bucke
     if (trace) {
       const int n = bk.grid * (bk.csize ? bk.csize : 1);
       trace += 4 * (size_t)n;
-      phases += 8 * (size_t)n;
+      phases += PHASE_WORDS * (size_t)n;
       P.trace_cls.insert(P.trace_cls.end(), n, bk.cls);
     }
     a.stage_fail = c->stage_fail_cta;
@@ -1264,7 +1264,7 @@ int mgcd_batch_cta_trace(mgcd_context* c, mgcd_cta_record* out, size_t cap, size
   if (!P.ran) return MGCD_ERR_INVALID_ARG;
   CK(cudaSetDevice(c->device));
   CK(cudaStreamSynchronize(P.stream));
-  std::vector<unsigned long long> raw(4 * ctas), ph(8 * ctas);
+  std::vector<unsigned long long> raw(4 * ctas), ph(PHASE_WORDS * ctas);
   CK(cudaMemcpy(raw.data(), P.d_trace.p, raw.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
   CK(cudaMemcpy(ph.data(), P.d_phases.p, ph.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
   unsigned long long t0 = ~0ull;
@@ -1278,13 +1278,16 @@ int mgcd_batch_cta_trace(mgcd_context* c, mgcd_cta_record* out, size_t cap, size
     r.ran = raw[4 * i] != 0 && raw[4 * i + 1] != 0;
     r.t_start_ms = r.ran ? (double)(raw[4 * i] - t0) * 1e-6 : 0.0;
     r.t_end_ms = r.ran ? (double)(raw[4 * i + 1] - t0) * 1e-6 : 0.0;
-    r.cycles_setup = ph[8 * i];
-    r.cycles_update = ph[8 * i + 1];
-    r.cycles_pivot = ph[8 * i + 2];
-    r.cycles_finish = ph[8 * i + 3];
-    r.iterations = ph[8 * i + 4];
-    r.rounds = ph[8 * i + 5];
-    r.cycles_replay = ph[8 * i + 7];
+    r.cycles_setup = ph[PHASE_WORDS * i];
+    r.cycles_update = ph[PHASE_WORDS * i + 1];
+    r.cycles_pivot = ph[PHASE_WORDS * i + 2];
+    r.cycles_finish = ph[PHASE_WORDS * i + 3];
+    r.iterations = ph[PHASE_WORDS * i + 4];
+    r.rounds = ph[PHASE_WORDS * i + 5];
+    r.cycles_replay = ph[PHASE_WORDS * i + 7];
+    r.update_rounds = ph[PHASE_WORDS * i + 8];
+    r.rounds_with_inverse = ph[PHASE_WORDS * i + 9];
+    r.finite_slot_updates = ph[PHASE_WORDS * i + 10];
   }
   return MGCD_OK;
 }

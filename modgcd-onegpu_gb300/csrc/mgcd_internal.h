@@ -68,6 +68,8 @@ struct StreamRing {
   uint32_t iters[STREAM_RING];
 };
 
+constexpr int PHASE_WORDS = 12;
+
 struct BatchArgs {
   InvTab inv;
   const uint32_t* limbs;
@@ -86,9 +88,10 @@ struct BatchArgs {
   int32_t* status;
   uint32_t stage_fail;       // test hook: this CTA reports an operand-staging failure (~0: none)
   unsigned long long* trace; // per CTA: start and end (globaltimer ns), SM id, pairs taken (null: off)
-  unsigned long long* phases; // per CTA (K-slot kernel): clock cycles of thread 0 in set-up, update,
-                              // pivot choice and finish, reduction iterations, moduli rounds, pairs,
-                              // cycles of certification and replay (null: off)
+  unsigned long long* phases; // per CTA (K-slot kernel, PHASE_WORDS each): clock cycles of thread 0 in
+                              // set-up, update, pivot choice and finish, reduction iterations, moduli
+                              // rounds, pairs, cycles of certification and replay; over all threads:
+                              // update rounds, rounds that needed an inverse, finite slot states (null: off)
   StreamRing* ring;          // ring mode (device view of the mapped ring)
   uint32_t* ring_head;       // entries claimed (device memory)
   unsigned long long idle_ns;  // ring mode: a CTA whose slots are all empty leaves after this long idle

@@ -207,8 +207,9 @@ struct SlotState {
 
 // One reduction-loop step of slot s's bookkeeping for its current pivot (the reference's
 // per-iteration checks, GmpCudaDevice-getGcdKernel.cu:365-402): records (p, b) in the
-// history and steps the size bounds; returns 0 (continue), 1 (loop ended: b = INF) or 3
-// (ran out of moduli).  One thread per slot.
+// history; returns 0 (continue), 1 (loop ended: b = INF) or 3 (ran out of moduli).  One
+// thread per slot.  The certification bounds are stepped for this pivot during the update
+// that uses it, by the last warp (below), off the path between the two barriers.
 template <int K>
 __device__ __forceinline__ uint32_t slot_step(SlotState<K>& ss, int s, int2* hist, int L)
 {
@@ -216,7 +217,6 @@ __device__ __forceinline__ uint32_t slot_step(SlotState<K>& ss, int s, int2* his
   const int32_t b = ss.b[s];
   if (b == MOD_INFINITY) return 1u;
   hist[ss.iters[s]] = make_int2((int)p, b);
-  bound_step(ss.lu[s], ss.lv[s], p, b);
   ss.iters[s] += 1u;
   const int rem = ss.rem[s] - 1;
   ss.rem[s] = rem;
@@ -263,6 +263,8 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
   const bool prof = a.phases != nullptr && threadIdx.x == 0;
   unsigned long long ph_load = 0, ph_update = 0, ph_pivot = 0, ph_finish = 0, ph_iters = 0, ph_rounds = 0;
   unsigned long long ph_replay = 0;   // the part of ph_finish spent in certification and replay
+  unsigned long long lv_rounds = 0, lv_inv = 0, lv_slots = 0;   // every thread: its update rounds, those
+                                                                  // with an inverse, finite slot states
   long long ph_t = prof ? clock64() : 0;
   auto ph_mark = [&](unsigned long long& acc) {
     if (prof) { const long long t = clock64(); acc += (unsigned long long)(t - ph_t); ph_t = t; }
@@ -408,6 +410,9 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
       kh[s] = kl[s] = 0xFFFFFFFFu;
     }
     if (prof) { ++ph_iters; ph_rounds += (nq_max + T - 1) / T; }
+    // size bounds for this update's pivots (log2f/exp2f on one lane per slot): the last warp
+    // has the fewest moduli rounds whenever nq_max is not a multiple of T
+    if (w == NW - 1 && lane < K && ((active >> lane) & 1u)) bound_step(ss.lu[lane], ss.lv[lane], ss.p[lane], ss.b[lane]);
     for (uint32_t j = threadIdx.x; j < nq_max; j += T) {
       uint32_t m = 0, tv[K];
 #pragma unroll
@@ -415,6 +420,14 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
         const bool on = ((active >> s) & 1u) && j < ss.d[s].nq;
         m |= (uint32_t)on << s;
         tv[s] = on ? tS[(size_t)s * NQS + j] : T_RETIRED;
+      }
+      if (a.phases) {                                 // liveness accounting (thread-rounds)
+        uint32_t fin = 0;
+#pragma unroll
+        for (int s = 0; s < K; ++s) fin += ((m >> s) & 1u) && tv[s] < T_MARK;
+        ++lv_rounds;
+        lv_inv += fin != 0u;
+        lv_slots += fin;
       }
       if (!m) continue;
       const ModConst c = a.mods[j];
@@ -462,9 +475,15 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
   }
   ph_mark(ph_finish);
   if (prof) {
-    unsigned long long* o = a.phases + 8 * (size_t)blockIdx.x;
+    unsigned long long* o = a.phases + PHASE_WORDS * (size_t)blockIdx.x;
     o[0] = ph_load; o[1] = ph_update; o[2] = ph_pivot; o[3] = ph_finish; o[4] = ph_iters; o[5] = ph_rounds;
     o[6] = taken; o[7] = ph_replay;
+  }
+  if (a.phases) {
+    unsigned long long* o = a.phases + PHASE_WORDS * (size_t)blockIdx.x;
+    atomicAdd(o + 8, lv_rounds);
+    atomicAdd(o + 9, lv_inv);
+    atomicAdd(o + 10, lv_slots);
   }
   trace_end(a.trace, taken);
 }

@@ -6,8 +6,12 @@
 // reciprocal and the exact remainder r = r0 - Q r1; the step makes progress (|r| < r1) iff
 // Q is within 1 of r0 / r1:
 //   phase A (2^22 <= r1 < r0 < 2^32): Q = rn(rn(r0) * rcp(rn(r1)));
+//   phase A of inv_mod_narrow (2^22 <= r1 < r0 < 2^30): Q from
+//                                      fma_rn(rn(r0), rcp(rn(r1)), 1.5 * 2^23);
 //   phase C (2 <= r1 < r0 < 2^22):    Q from fma_rn(r0, rcp(r1), 1.5 * 2^23), remainder
-//                                      fma_rn(-Q, r1, r0).
+//                                      fma_rn(-Q, r1, r0);
+//   phase C with r0 < r1 (the step after inv_mod_narrow's phase B may start there):
+//                                      Q of 0 or 1, exact remainder.
 // On [k r1, (k+1) r1 - 1] the allowed quotients are k at r0 = k r1 and {k, k + 1} above.
 // For a fixed r1 both estimates are non-decreasing in r0 (every operation is monotone and
 // rcp(r1) is fixed), so the estimate is allowed on the whole interval iff it is at the two
@@ -72,6 +76,22 @@ __global__ void __launch_bounds__(256) certify_kernel(CertOut* out)
       n += 2;
       if (!step_c_ok(lo, r1, k)) fail(out, lo, r1);
       if (!step_c_ok(hi, r1, k)) fail(out, hi, r1);
+    }
+    n += 2;                                            // k = 0: r0 in [1, r1 - 1]
+    if (!step_c_ok(1u, r1, 0u)) fail(out, 1u, r1);
+    if (!step_c_ok(r1 - 1u, r1, 0u)) fail(out, r1 - 1u, r1);
+  }
+  // phase A of inv_mod_narrow: 2^22 <= r1 < r0 < 2^30
+  constexpr uint32_t AN_TOP = (1u << 30) - 1u;
+  for (uint32_t r1 = (1u << 22) + blockIdx.x * blockDim.x + threadIdx.x; r1 < AN_TOP; r1 += stride) {
+    const float g1 = __uint2float_rn(r1);
+    for (uint32_t k = 1; k <= AN_TOP / r1; ++k) {
+      const uint32_t lo = k == 1 ? r1 + 1u : k * r1;
+      const uint32_t hi = min((k + 1) * r1 - 1u, AN_TOP);
+      if (lo > hi) continue;
+      n += 2;
+      if (!quot_ok(lo, r1, k, inv_quot_an(__uint2float_rn(lo), g1))) fail(out, lo, r1);
+      if (!quot_ok(hi, r1, k, inv_quot_an(__uint2float_rn(hi), g1))) fail(out, hi, r1);
     }
   }
   // phase A: 2^22 <= r1 < r0 < 2^32

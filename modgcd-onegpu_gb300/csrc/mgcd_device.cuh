@@ -163,6 +163,71 @@ __device__ __forceinline__ uint32_t inv_mod(uint32_t x, uint32_t q, uint32_t qin
   return inv_mod_slow(x, q);
 }
 
+// Phase A quotient of inv_mod_narrow (2^22 <= r1 < r0 < 2^30, so Q < 2^8): the nearest
+// integer to rn(r0) * rcp(rn(r1)), read from the mantissa (one rounding) instead of a
+// float-to-integer conversion; g0, g1 are the operands already converted.
+__device__ __forceinline__ uint32_t inv_quot_an(float g0, float g1)
+{
+  return __float_as_uint(__fmaf_rn(g0, rcp_approx(g1), INV_MAGIC)) - INV_MAGIC_BITS;
+}
+
+// x^{-1} mod q for 0 < x < q < 2^30 (the moduli of widths up to 30 bits): inv_mod's Euclid
+// with cheaper steps where the narrower operands allow them.
+//   phase A (r1 >= 2^22): quotient estimate as inv_quot_an, each remainder converted once;
+//            |r0 - Q r1| < r1 < 2^30, so the remainder and its sign come from 32-bit
+//            wrapping arithmetic read as signed;
+//   phase B (r0 >= 2^22 > r1): a float quotient estimate instead of an integer division.
+//            Its error is below (r0 / r1) 2^-22 + 1/2 (operand rounding 2^-24, reciprocal
+//            2^-23, product 2^-24), so the exact signed remainder r0 - Q r1 is below
+//            2^8 + r1 / 2 < 2^22 in magnitude: exact in float, as phase C requires (its
+//            first step may then see |r0| < |r1|, a quotient of 0 or +-1);
+//   phase C: inv_mod's, two steps per loop trip with the roles of the registers
+//            alternating, at most 64 steps (never reached: 22-bit operands take ~32 at most).
+// The result is checked as inv_mod's is, with the same integer-only fallback.
+__device__ __forceinline__ uint32_t inv_mod_narrow(uint32_t x, uint32_t q, uint32_t qinv)
+{
+  uint32_t r0 = q, r1 = x, s0 = 0, s1 = 1;
+  float g0 = __uint2float_rn(r0), g1 = __uint2float_rn(r1);
+  while (r1 >= (1u << 22)) {
+    const uint32_t Q = inv_quot_an(g0, g1);
+    const uint32_t d = r0 - Q * r1;
+    const uint32_t s = s0 - Q * s1;
+    const bool neg = (int32_t)d < 0;
+    r0 = r1; s0 = s1; g0 = g1;
+    r1 = neg ? 0u - d : d;
+    s1 = neg ? 0u - s : s;
+    g1 = __uint2float_rn(r1);
+  }
+  if (r1 > 1u) {
+    int32_t i0 = (int32_t)r0, i1 = (int32_t)r1;
+    if (r0 >= (1u << 22)) {
+      const uint32_t Q = __float2uint_rn(__fmul_rn(g0, rcp_approx(g1)));
+      const int32_t r = (int32_t)(r0 - Q * r1);
+      const uint32_t s = s0 - Q * s1;
+      i0 = i1; i1 = r; s0 = s1; s1 = s;
+    }
+    float f0 = (float)i0, f1 = (float)i1;
+    for (int trips = 32; trips > 0 && fabsf(f1) > 1.0f; --trips) {
+      {
+        const float qm = inv_quot_c(f0, f1);
+        f0 = __fmaf_rn(INV_MAGIC - qm, f1, f0);
+        s0 = s0 - (__float_as_uint(qm) - INV_MAGIC_BITS) * s1;
+      }
+      if (!(fabsf(f0) > 1.0f)) { f1 = f0; s1 = s0; break; }
+      {
+        const float qm = inv_quot_c(f1, f0);
+        f1 = __fmaf_rn(INV_MAGIC - qm, f0, f1);
+        s1 = s1 - (__float_as_uint(qm) - INV_MAGIC_BITS) * s0;
+      }
+    }
+    if (f1 < 0.0f) s1 = 0u - s1;                   // s1 x == -1
+  }
+  const uint32_t one = redc(1ull, q, qinv);
+  const uint32_t inv = (int32_t)s1 < 0 ? s1 + q : s1;
+  if (redc((uint64_t)inv * x, q, qinv) == one) return inv;
+  return inv_mod_slow(x, q);
+}
+
 // Key of the reduction loop's pivot choice (postMinPair, GmpCudaDevice-getGcdKernel.cu:152-154):
 // high word |value| (0x80000000 for MOD_INFINITY), low word modulus - (value >= 0).
 __device__ __forceinline__ void t_key(uint32_t t, uint32_t q, uint32_t& hi, uint32_t& lo)
@@ -267,7 +332,10 @@ __device__ __forceinline__ uint32_t mod_canon(uint32_t x, uint32_t q)
 }
 
 // t_update_k for moduli below 2^30: the prefix products, the scaled inverse and the walk
-// back stay lazy; the inverse's input and the new states are canonical.
+// back stay lazy; the inverse's input and the new states are canonical.  Every modulus of a
+// width-L table is an L-bit prime, so a pivot p < 2^L <= 2q enters the products as it is,
+// and |b| <= p / 2 < q puts t - b in (-q, 2q): one conditional add of q makes it a lazy
+// value in [0, 2q), which is 0 mod q exactly at 0 and q.
 template <int K>
 __device__ __forceinline__ void t_update_k_narrow(uint32_t (&t)[K], const ModConst& c, const uint32_t (&p)[K],
                                                   const int32_t (&b)[K], uint32_t mask)
@@ -282,8 +350,9 @@ __device__ __forceinline__ void t_update_k_narrow(uint32_t (&t)[K], const ModCon
     const uint32_t ts = t[s];
     if (ts >= T_MARK) { t[s] = (ts == T_INF) ? 0u : ts; continue; }
     if (q == p[s]) { t[s] = T_RETIRED; continue; }
-    const uint32_t d = mod_sub(ts, from_signed(b[s], q), q);
-    if (d == 0u) { t[s] = T_INF; continue; }
+    const uint32_t dr = ts - (uint32_t)b[s];
+    const uint32_t d = min(dr, dr + q);               // dr < 0 wraps above 2^31; dr + q < 3q
+    if (d == 0u || d == q) { t[s] = T_INF; continue; }
     x[s] = d;
     need |= 1u << s;
   }
@@ -292,14 +361,14 @@ __device__ __forceinline__ void t_update_k_narrow(uint32_t (&t)[K], const ModCon
   P[0] = x[0];
 #pragma unroll
   for (int s = 1; s < K; ++s) P[s] = mont_mul_lazy(P[s - 1], x[s], q, qinv);
-  uint32_t Z = mont_mul_lazy(inv_mod(mod_canon(P[K - 1], q), q, qinv), c.r2, q, qinv);   // times R
+  uint32_t Z = mont_mul_lazy(inv_mod_narrow(mod_canon(P[K - 1], q), q, qinv), c.r2, q, qinv);   // times R
 #pragma unroll
   for (int s = K - 1; s >= 1; --s) {
     const uint32_t y = mont_mul_lazy(Z, P[s - 1], q, qinv);
     Z = mont_mul_lazy(Z, x[s], q, qinv);
-    if ((need >> s) & 1u) t[s] = mod_canon(mont_mul_lazy(p[s] > q ? p[s] - q : p[s], y, q, qinv), q);
+    if ((need >> s) & 1u) t[s] = mod_canon(mont_mul_lazy(p[s], y, q, qinv), q);
   }
-  if (need & 1u) t[0] = mod_canon(mont_mul_lazy(p[0] > q ? p[0] - q : p[0], Z, q, qinv), q);
+  if (need & 1u) t[0] = mod_canon(mont_mul_lazy(p[0], Z, q, qinv), q);
 }
 
 // Size bounds of the reduction loop, for certifying its result: lu >= log2|u_i| and

@@ -205,6 +205,11 @@ struct SlotState {
   uint32_t stop;                     // set-up: slot_step's result for the first pivot
 };
 
+// Words of a K-slot CTA's phase record (BatchArgs::phases, PHASE_WORDS per CTA): clock cycles
+// of thread 0 per phase, loop iterations, moduli rounds, pairs taken, the replay's share of
+// the finish; words 8-10 are the update loop's liveness counters (every thread).
+enum { PH_LOAD = 0, PH_UPDATE, PH_PIVOT, PH_FINISH, PH_ITERS, PH_ROUNDS, PH_TAKEN, PH_REPLAY };
+
 // One reduction-loop step of slot s's bookkeeping for its current pivot (the reference's
 // per-iteration checks, GmpCudaDevice-getGcdKernel.cu:365-402): records (p, b) in the
 // history; returns 0 (continue), 1 (loop ended: b = INF) or 3 (ran out of moduli).  One
@@ -244,9 +249,13 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
   __shared__ unsigned long long stage_bar[2];
   __shared__ uint32_t stage_state;
   // at dynamic smem start; in ring mode the operands are in host memory: plain coherent loads
-  const Stage stg = RING ? Stage{smem, nullptr, nullptr, 0u, 1u}
-                         : Stage{smem, stage_bar, &stage_state, blockIdx.x == a.stage_fail, 0u};
-  stage_init(stg);
+  // (built where it is used: its fields are cheap to form and would otherwise stay in
+  // registers through the update loop)
+  auto stage = [&]() {
+    return RING ? Stage{smem, nullptr, nullptr, 0u, 1u}
+                : Stage{smem, stage_bar, &stage_state, blockIdx.x == a.stage_fail, 0u};
+  };
+  stage_init(stage());
   const uint32_t NQS = a.nq_max;
   uint32_t* const tS = smem + STAGE_SMEM_WORDS;       // K x NQS states
   uint32_t* const acc2 = tS + (size_t)K * NQS;        // residues of v during set-up
@@ -260,14 +269,21 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
   auto hist_of = [&](int s) { return reinterpret_cast<int2*>(scr + (size_t)s * 4 * NQS + 2 * (size_t)NQS); };
   // phase accounting (a.phases): thread 0's clock in each phase; the phases end at barriers,
   // so thread 0's timeline is the CTA's
+  // (in shared memory, so that no thread carries them in registers through the loop)
   const bool prof = a.phases != nullptr && threadIdx.x == 0;
-  unsigned long long ph_load = 0, ph_update = 0, ph_pivot = 0, ph_finish = 0, ph_iters = 0, ph_rounds = 0;
-  unsigned long long ph_replay = 0;   // the part of ph_finish spent in certification and replay
-  unsigned long long lv_rounds = 0, lv_inv = 0, lv_slots = 0;   // every thread: its update rounds, those
-                                                                  // with an inverse, finite slot states
-  long long ph_t = prof ? clock64() : 0;
-  auto ph_mark = [&](unsigned long long& acc) {
-    if (prof) { const long long t = clock64(); acc += (unsigned long long)(t - ph_t); ph_t = t; }
+  __shared__ unsigned long long phs[8];   // PH_* below; PH_REPLAY is the part of PH_FINISH spent
+  __shared__ long long ph_t;              // in certification and replay
+  if (prof) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) phs[i] = 0ull;
+    ph_t = clock64();
+  }
+  __shared__ unsigned long long lvs[3];   // liveness of the update loop: thread-rounds, those with
+                                          // a finite slot state, finite slot states (per-iteration
+                                          // warp sums, so no counter is carried through the loop)
+  if (a.phases && threadIdx.x == 0) lvs[0] = lvs[1] = lvs[2] = 0ull;
+  auto ph_mark = [&](int i) {
+    if (prof) { const long long t = clock64(); phs[i] += (unsigned long long)(t - ph_t); ph_t = t; }
   };
 
   // Takes the next pair of the queue (ring mode: of the ring; `wait` = poll, bounded, while
@@ -302,6 +318,7 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
       }
       __syncthreads();
       const PairDesc& d = ss.d[s];
+      const Stage stg = stage();
       const bool staged = residues<T>(a.limbs + d.u_off, d.u_len, a.mods, d.nq, ts, stg, NARROW);
       if (residues<T>(a.limbs + d.v_off, d.v_len, a.mods, d.nq, acc2, stg, NARROW) && staged) break;
       if (threadIdx.x == 0) {
@@ -345,9 +362,9 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
     return r;
   };
   auto take_slot = [&](int s, bool wait) {
-    ph_mark(ph_finish);
+    ph_mark(PH_FINISH);
     const uint32_t r = load(s, wait);
-    ph_mark(ph_load);
+    ph_mark(PH_LOAD);
     if (r & 16u) {
       valid |= 1u << s;
       if (!(r & 1u)) active |= 1u << s;
@@ -377,7 +394,7 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
         finish_pair<T, SYNC_CTA>(a.mods, ss.d[s], L, 0u, ss.d[s].nq, tS + (size_t)s * NQS, rs, rparity, repoch, nullptr,
                               u0, u0 + NQS, reinterpret_cast<const int2*>(u0 + 2 * (size_t)NQS), it, ss.rem[s],
                               ss.lu[s], ss.lv[s], a.digits, a.count + pi, a.status + pi, a.inv, smem, acc2,
-                              a.phases ? &ph_replay : nullptr);
+                              a.phases ? &phs[PH_REPLAY] : nullptr);
       }
       if (RING && threadIdx.x == 0) stream_done(a, ss.seq[s]);   // results written by this thread
       __syncthreads();
@@ -396,7 +413,7 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
       }
     }
     if (!valid) break;
-    ph_mark(ph_finish);
+    ph_mark(PH_FINISH);
 
     // ---- one update of every active pair with its current pivot
     uint32_t p[K], kh[K], kl[K];
@@ -409,7 +426,8 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
       if ((active >> s) & 1u) nq_max = max(nq_max, ss.d[s].nq);
       kh[s] = kl[s] = 0xFFFFFFFFu;
     }
-    if (prof) { ++ph_iters; ph_rounds += (nq_max + T - 1) / T; }
+    if (prof) { phs[PH_ITERS] += 1u; phs[PH_ROUNDS] += (nq_max + T - 1) / T; lvs[0] += nq_max; }
+    uint32_t lv_any = 0, lv_fin = 0;
     // size bounds for this update's pivots (log2f/exp2f on one lane per slot): the last warp
     // has the fewest moduli rounds whenever nq_max is not a multiple of T
     if (w == NW - 1 && lane < K && ((active >> lane) & 1u)) bound_step(ss.lu[lane], ss.lv[lane], ss.p[lane], ss.b[lane]);
@@ -425,9 +443,8 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
         uint32_t fin = 0;
 #pragma unroll
         for (int s = 0; s < K; ++s) fin += ((m >> s) & 1u) && tv[s] < T_MARK;
-        ++lv_rounds;
-        lv_inv += fin != 0u;
-        lv_slots += fin;
+        lv_any += fin != 0u;
+        lv_fin += fin;
       }
       if (!m) continue;
       const ModConst c = a.mods[j];
@@ -442,7 +459,11 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
         if (key_less(h, l, kh[s], kl[s])) { kh[s] = h; kl[s] = l; }
       }
     }
-    ph_mark(ph_update);
+    if (a.phases) {
+      const uint32_t wa = __reduce_add_sync(0xFFFFFFFFu, lv_any), wf = __reduce_add_sync(0xFFFFFFFFu, lv_fin);
+      if (lane == 0 && wf) { atomicAdd(&lvs[1], (unsigned long long)wa); atomicAdd(&lvs[2], (unsigned long long)wf); }
+    }
+    ph_mark(PH_UPDATE);
     // ---- the next pivots (GmpCudaDevice-getGcdKernel.cu:365-402): warp minima, one
     // barrier, then warp s reduces slot s's minima, stores its pivot and steps its
     // bookkeeping (the K slots in parallel)
@@ -471,19 +492,18 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
       if (r & 1u) active &= ~(1u << s);
       if (r & 2u) redux |= 1u << s;
     }
-    ph_mark(ph_pivot);
+    ph_mark(PH_PIVOT);
   }
-  ph_mark(ph_finish);
+  ph_mark(PH_FINISH);
   if (prof) {
     unsigned long long* o = a.phases + PHASE_WORDS * (size_t)blockIdx.x;
-    o[0] = ph_load; o[1] = ph_update; o[2] = ph_pivot; o[3] = ph_finish; o[4] = ph_iters; o[5] = ph_rounds;
-    o[6] = taken; o[7] = ph_replay;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) o[i] = phs[i];
+    o[PH_TAKEN] = taken;
   }
-  if (a.phases) {
+  if (prof) {                                          // every warp's sums are in (barriers since)
     unsigned long long* o = a.phases + PHASE_WORDS * (size_t)blockIdx.x;
-    atomicAdd(o + 8, lv_rounds);
-    atomicAdd(o + 9, lv_inv);
-    atomicAdd(o + 10, lv_slots);
+    o[8] = lvs[0]; o[9] = lvs[1]; o[10] = lvs[2];
   }
   trace_end(a.trace, taken);
 }

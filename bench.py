@@ -172,7 +172,8 @@ def occupancy(rec, sms):
     of its CTAs' intervals, over the span from the first CTA start to the last CTA end; per
     size class the CTAs, their start and end spread, the longest CTA and, for the K-slot
     CTAs, where thread 0's clock went (set-up, update, pivot step incl. the wait for the
-    slowest warp, finish; finish_replay: the certification and replay part of finish)."""
+    slowest warp, finish, layout: re-sorting the positions by live slots; finish_replay: the
+    certification and replay part of finish)."""
     rec = rec[rec["ran"] != 0]
     if not len(rec):
         return None
@@ -197,7 +198,7 @@ def occupancy(rec, sms):
                            "start_ms_max": float(r["t_start_ms"].max()), "end_ms_min": float(r["t_end_ms"].min()),
                            "end_ms_max": float(r["t_end_ms"].max()), "cta_ms_median": float(statistics.median(d)),
                            "cta_ms_max": float(d.max())}
-        cyc = {k: float(r["cycles_" + k].sum()) for k in ("setup", "update", "pivot", "finish")}
+        cyc = {k: float(r["cycles_" + k].sum()) for k in ("setup", "update", "pivot", "finish", "layout")}
         tot = sum(cyc.values())
         if tot > 0:
             classes[str(c)]["phases"] = {k: v / tot for k, v in cyc.items()}
@@ -207,9 +208,9 @@ def occupancy(rec, sms):
             classes[str(c)]["pivot_cycles_per_iteration"] = cyc["pivot"] / max(1.0, float(r["iterations"].sum()))
             ur, ri, fs = (float(r[k].sum()) for k in ("update_rounds", "rounds_with_inverse", "finite_slot_updates"))
             if ur > 0:
-                # liveness of the update loop: rounds where every slot's modulus was retired
-                # (or beyond its pair), and finite slot states per slot position of the rounds
-                # that computed an inverse
+                # liveness of the update loop: rounds (positions visited) where every slot's
+                # modulus was retired (or beyond its pair), and finite slot states per slot
+                # position of the rounds that computed an inverse
                 classes[str(c)]["update_liveness"] = {"rounds_without_inverse": 1.0 - ri / ur,
                                                       "finite_slots_per_inverse": fs / max(1.0, ri)}
     return {"span_ms": span, "sms": sms, "sm_busy_frac": busy / (sms * span) if span > 0 else None,

@@ -323,10 +323,12 @@ typedef struct {
      slowest warp of the update), and finish (certification, replay, recovery); reduction
      iterations; moduli rounds (sum over iterations of the update loop's trips per thread);
      the part of finish spent in certification and replay; summed over the CTA's threads:
-     update rounds (one modulus of every slot), the rounds in which some slot needed an
-     inverse, and the slot states updated through the inverse */
+     update rounds (one position of every slot), the rounds in which some slot needed an
+     inverse, and the slot states updated through the inverse; clock cycles spent re-laying
+     out the positions (sorted by the slots live there, so that dead positions leave the
+     update loop) */
   uint64_t cycles_setup, cycles_update, cycles_pivot, cycles_finish, iterations, rounds, cycles_replay;
-  uint64_t update_rounds, rounds_with_inverse, finite_slot_updates;
+  uint64_t update_rounds, rounds_with_inverse, finite_slot_updates, cycles_layout;
 } mgcd_cta_record;
 int mgcd_set_cta_trace(mgcd_context *ctx, int enable);
 int mgcd_batch_cta_trace(mgcd_context *ctx, mgcd_cta_record *out, size_t cap, size_t *n);

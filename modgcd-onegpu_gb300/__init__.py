@@ -472,7 +472,8 @@ CTA_RECORD = np.dtype([("size_class", "<i4"), ("sm", "<u4"), ("pairs", "<u4"), (
                        ("t_start_ms", "<f8"), ("t_end_ms", "<f8"), ("cycles_setup", "<u8"),
                        ("cycles_update", "<u8"), ("cycles_pivot", "<u8"), ("cycles_finish", "<u8"),
                        ("iterations", "<u8"), ("rounds", "<u8"), ("cycles_replay", "<u8"),
-                       ("update_rounds", "<u8"), ("rounds_with_inverse", "<u8"), ("finite_slot_updates", "<u8")])
+                       ("update_rounds", "<u8"), ("rounds_with_inverse", "<u8"), ("finite_slot_updates", "<u8"),
+                       ("cycles_layout", "<u8")])
 
 
 class Server:

@@ -1288,6 +1288,7 @@ int mgcd_batch_cta_trace(mgcd_context* c, mgcd_cta_record* out, size_t cap, size
     r.update_rounds = ph[PHASE_WORDS * i + 8];
     r.rounds_with_inverse = ph[PHASE_WORDS * i + 9];
     r.finite_slot_updates = ph[PHASE_WORDS * i + 10];
+    r.cycles_layout = ph[PHASE_WORDS * i + 11];
   }
   return MGCD_OK;
 }

@@ -208,7 +208,14 @@ struct SlotState {
 // Words of a K-slot CTA's phase record (BatchArgs::phases, PHASE_WORDS per CTA): clock cycles
 // of thread 0 per phase, loop iterations, moduli rounds, pairs taken, the replay's share of
 // the finish; words 8-10 are the update loop's liveness counters (every thread).
-enum { PH_LOAD = 0, PH_UPDATE, PH_PIVOT, PH_FINISH, PH_ITERS, PH_ROUNDS, PH_TAKEN, PH_REPLAY };
+// Word 11: cycles spent re-laying out the positions.
+enum { PH_LOAD = 0, PH_UPDATE, PH_PIVOT, PH_FINISH, PH_ITERS, PH_ROUNDS, PH_TAKEN, PH_REPLAY, PH_LAYOUT };
+constexpr int PH_WORDS_T0 = 9;          // words kept by thread 0
+
+// Iterations between two re-layouts of a K-slot CTA's positions (besides those after a pair
+// finishes or is loaded).  Each iteration retires one position per slot, so a layout stays
+// close to sorted; one re-layout moves (K + 1) x nq_max words twice.
+constexpr uint32_t RELAYOUT_EVERY = 16;
 
 // One reduction-loop step of slot s's bookkeeping for its current pivot (the reference's
 // per-iteration checks, GmpCudaDevice-getGcdKernel.cu:365-402): records (p, b) in the
@@ -233,6 +240,19 @@ __device__ __forceinline__ uint32_t slot_step(SlotState<K>& ss, int s, int2* his
   return rem * (L - 2) <= ub ? 3u : 0u;
 }
 
+// Position layout.  The K slots share every modulus's inverse, so their states sit at common
+// positions: slot s's state of modulus pmod[pos] at tS[s][pos].  A slot's states die as the
+// loop retires its pivots (about one per iteration; most of its moduli by the end) and
+// beyond its own moduli count, and a warp pays for a slot's work wherever one of its lanes
+// needs it.  So the CTA re-lays its positions out, sorted by the set of slots that are live
+// there (finite or infinite ratio): warps then see one live set, skip a dead slot's work
+// together, and positions dead in every slot go to the end, where the update loop no longer
+// visits them.  Dead states never change, so the loop result is the same; the pivot is the
+// minimum key, whose tie-break is the modulus, not the position.  A slot's states are put
+// back into modulus order before its pair finishes (the replay and recovery index moduli),
+// and a newly loaded pair's states, computed in modulus order, are taken in by the next
+// re-layout (`fresh`).
+//
 // NARROW: moduli below 2^30 (widths up to 30 bits), lazily reduced Montgomery products.
 // RING: continuous serving -- pairs come from a.ring instead of the batch queue, empty
 // slots take newly published entries while the others run, and a CTA whose slots stay
@@ -258,7 +278,10 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
   stage_init(stage());
   const uint32_t NQS = a.nq_max;
   uint32_t* const tS = smem + STAGE_SMEM_WORDS;       // K x NQS states
-  uint32_t* const acc2 = tS + (size_t)K * NQS;        // residues of v during set-up
+  uint32_t* const acc2 = tS + (size_t)K * NQS;        // residues of v during set-up; the
+                                                      // re-layout's and un-permute's buffer
+  uint16_t* const pmod = reinterpret_cast<uint16_t*>(acc2 + NQS);   // modulus at each position
+  uint16_t* const aux = pmod + NQS;                   // re-layout: live set, then new position
   uint32_t* const scr = a.scratch + (size_t)blockIdx.x * a.scratch_words;   // per slot u0, v0, hist
   const int L = a.L;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -271,11 +294,11 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
   // so thread 0's timeline is the CTA's
   // (in shared memory, so that no thread carries them in registers through the loop)
   const bool prof = a.phases != nullptr && threadIdx.x == 0;
-  __shared__ unsigned long long phs[8];   // PH_* below; PH_REPLAY is the part of PH_FINISH spent
-  __shared__ long long ph_t;              // in certification and replay
+  __shared__ unsigned long long phs[PH_WORDS_T0];   // PH_*; PH_REPLAY is the part of PH_FINISH
+  __shared__ long long ph_t;                        // spent in certification and replay
   if (prof) {
 #pragma unroll
-    for (int i = 0; i < 8; ++i) phs[i] = 0ull;
+    for (int i = 0; i < PH_WORDS_T0; ++i) phs[i] = 0ull;
     ph_t = clock64();
   }
   __shared__ unsigned long long lvs[3];   // liveness of the update loop: thread-rounds, those with
@@ -361,15 +384,87 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
     __syncthreads();                                  // everyone has read it before it changes
     return r;
   };
+  uint32_t npos = 0, fresh = 0, since = 0;             // positions visited; slots in modulus order
   auto take_slot = [&](int s, bool wait) {
     ph_mark(PH_FINISH);
     const uint32_t r = load(s, wait);
     ph_mark(PH_LOAD);
     if (r & 16u) {
       valid |= 1u << s;
+      fresh |= 1u << s;
       if (!(r & 1u)) active |= 1u << s;
       if ((r & 3u) == 3u) redux |= 1u << s;
     }
+  };
+
+  // ---- position layout
+  __shared__ uint32_t bucket[1u << K];
+  __shared__ uint32_t live_pos;
+  for (uint32_t pos = threadIdx.x; pos < NQS; pos += T) pmod[pos] = (uint16_t)pos;
+  auto state_at = [&](int s, uint32_t pos, uint32_t m) -> uint32_t {
+    const uint32_t* ts = tS + (size_t)s * NQS;
+    if ((fresh >> s) & 1u) return m < ss.d[s].nq ? ts[m] : T_RETIRED;
+    return ts[pos];
+  };
+  // Counting sort of the positions by live set (full sets first, the empty set last);
+  // warp-aggregated shared-memory atomics give the ranks.  Every thread calls it.
+  auto relayout = [&]() {
+    if (threadIdx.x < (1u << K)) bucket[threadIdx.x] = 0u;
+    __syncthreads();
+    const uint32_t below = (1u << lane) - 1u;
+    for (uint32_t base = 0; base < NQS; base += T) {
+      const uint32_t pos = base + threadIdx.x;
+      const bool in = pos < NQS;
+      uint32_t set = 0xFFFFu;
+      if (in) {
+        const uint32_t m = pmod[pos];
+        set = 0u;
+#pragma unroll
+        for (int s = 0; s < K; ++s) {
+          if (!((active >> s) & 1u)) continue;
+          const uint32_t v = state_at(s, pos, m);
+          set |= (uint32_t)(v < T_MARK || v == T_INF) << s;
+        }
+        aux[pos] = (uint16_t)set;
+      }
+      const uint32_t grp = __match_any_sync(0xFFFFFFFFu, set);
+      if (in && lane == __ffs((int)grp) - 1) atomicAdd(&bucket[set], (uint32_t)__popc(grp));
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint32_t off = 0;
+      for (uint32_t m = (1u << K) - 1u; m >= 1u; --m) { const uint32_t c = bucket[m]; bucket[m] = off; off += c; }
+      live_pos = off;
+      bucket[0] = off;
+    }
+    __syncthreads();
+    for (uint32_t base = 0; base < NQS; base += T) {
+      const uint32_t pos = base + threadIdx.x;
+      const bool in = pos < NQS;
+      const uint32_t set = in ? aux[pos] : 0xFFFFu;
+      const uint32_t grp = __match_any_sync(0xFFFFFFFFu, set);
+      const int lead = __ffs((int)grp) - 1;
+      uint32_t r0 = 0u;
+      if (in && lane == lead) r0 = atomicAdd(&bucket[set], (uint32_t)__popc(grp));
+      r0 = __shfl_sync(0xFFFFFFFFu, r0, lead);
+      if (in) aux[pos] = (uint16_t)(r0 + __popc(grp & below));
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int s = 0; s < K; ++s) {
+      if (!((valid >> s) & 1u)) continue;
+      for (uint32_t pos = threadIdx.x; pos < NQS; pos += T) acc2[aux[pos]] = state_at(s, pos, pmod[pos]);
+      __syncthreads();
+      uint32_t* ts = tS + (size_t)s * NQS;
+      for (uint32_t pos = threadIdx.x; pos < NQS; pos += T) ts[pos] = acc2[pos];
+      __syncthreads();
+    }
+    for (uint32_t pos = threadIdx.x; pos < NQS; pos += T) acc2[aux[pos]] = pmod[pos];
+    __syncthreads();
+    for (uint32_t pos = threadIdx.x; pos < NQS; pos += T) pmod[pos] = (uint16_t)acc2[pos];
+    __syncthreads();
+    npos = live_pos;
+    fresh = 0u;
   };
 
 #pragma unroll 1
@@ -381,6 +476,7 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
   for (;;) {
     // ---- pairs whose reduction loop ended: finish them and refill their slots
     const uint32_t done = valid & ~active;
+    bool changed = fresh != 0u;
 #pragma unroll 1
     for (int s = 0; s < K; ++s) {
       if (!((done >> s) & 1u)) continue;
@@ -390,6 +486,17 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
       if ((redux >> s) & 1u) {
         if (threadIdx.x == 0) { a.status[pi] = ST_REDUX; a.count[pi] = 0; }
       } else {
+        if (!((fresh >> s) & 1u)) {                  // back to modulus order
+          const uint32_t nq = ss.d[s].nq;
+          uint32_t* ts = tS + (size_t)s * NQS;
+          for (uint32_t pos = threadIdx.x; pos < NQS; pos += T) {
+            const uint32_t m = pmod[pos];
+            if (m < nq) acc2[m] = ts[pos];
+          }
+          __syncthreads();
+          for (uint32_t j = threadIdx.x; j < nq; j += T) ts[j] = acc2[j];
+          __syncthreads();
+        }
         uint32_t* u0 = scr + (size_t)s * 4 * NQS;
         finish_pair<T, SYNC_CTA>(a.mods, ss.d[s], L, 0u, ss.d[s].nq, tS + (size_t)s * NQS, rs, rparity, repoch, nullptr,
                               u0, u0 + NQS, reinterpret_cast<const int2*>(u0 + 2 * (size_t)NQS), it, ss.rem[s],
@@ -400,6 +507,8 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
       __syncthreads();
       valid &= ~(1u << s);
       redux &= ~(1u << s);
+      fresh &= ~(1u << s);
+      changed = true;
       if (!RING) take_slot(s, false);
     }
     if constexpr (RING) {
@@ -410,32 +519,37 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
         if ((valid >> s) & 1u) continue;
         take_slot(s, valid == 0u);
         if (!((valid >> s) & 1u)) break;
+        changed = true;
       }
     }
     if (!valid) break;
     ph_mark(PH_FINISH);
+    if (changed || since >= RELAYOUT_EVERY) {
+      relayout();
+      since = 0;
+      ph_mark(PH_LAYOUT);
+    }
+    ++since;
 
     // ---- one update of every active pair with its current pivot
     uint32_t p[K], kh[K], kl[K];
     int32_t b[K];
-    uint32_t nq_max = 0;
 #pragma unroll
     for (int s = 0; s < K; ++s) {
       p[s] = ss.p[s];
       b[s] = ss.b[s];
-      if ((active >> s) & 1u) nq_max = max(nq_max, ss.d[s].nq);
       kh[s] = kl[s] = 0xFFFFFFFFu;
     }
-    if (prof) { phs[PH_ITERS] += 1u; phs[PH_ROUNDS] += (nq_max + T - 1) / T; lvs[0] += nq_max; }
+    if (prof) { phs[PH_ITERS] += 1u; phs[PH_ROUNDS] += (npos + T - 1) / T; lvs[0] += npos; }
     uint32_t lv_any = 0, lv_fin = 0;
     // size bounds for this update's pivots (log2f/exp2f on one lane per slot): the last warp
-    // has the fewest moduli rounds whenever nq_max is not a multiple of T
+    // has the fewest moduli rounds whenever npos is not a multiple of T
     if (w == NW - 1 && lane < K && ((active >> lane) & 1u)) bound_step(ss.lu[lane], ss.lv[lane], ss.p[lane], ss.b[lane]);
-    for (uint32_t j = threadIdx.x; j < nq_max; j += T) {
+    for (uint32_t j = threadIdx.x; j < npos; j += T) {
       uint32_t m = 0, tv[K];
 #pragma unroll
-      for (int s = 0; s < K; ++s) {
-        const bool on = ((active >> s) & 1u) && j < ss.d[s].nq;
+      for (int s = 0; s < K; ++s) {                   // (states beyond a pair's moduli are retired)
+        const bool on = (active >> s) & 1u;
         m |= (uint32_t)on << s;
         tv[s] = on ? tS[(size_t)s * NQS + j] : T_RETIRED;
       }
@@ -447,7 +561,7 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
         lv_fin += fin;
       }
       if (!m) continue;
-      const ModConst c = a.mods[j];
+      const ModConst c = a.mods[pmod[j]];
       if constexpr (NARROW) t_update_k_narrow<K>(tv, c, p, b, m);
       else t_update_k<K>(tv, c, p, b, m);
 #pragma unroll
@@ -478,6 +592,9 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
       uint32_t h = (uint32_t)(k >> 32), l = (uint32_t)k;
       warp_min_key(h, l);
       if (lane == 0) {
+        // no position visited holds the slot's states (every ratio retired or degenerate):
+        // the infinite key, which ends the slot's loop
+        if (h == 0xFFFFFFFFu) { h = KEY_INF_HI; l = 0xFFFFFFFFu; }
         key_pair(h, l, ss.p[w], ss.b[w]);
         ss.res[w] = slot_step<K>(ss, w, hist_of(w), L);
       }
@@ -500,10 +617,8 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
 #pragma unroll
     for (int i = 0; i < 8; ++i) o[i] = phs[i];
     o[PH_TAKEN] = taken;
-  }
-  if (prof) {                                          // every warp's sums are in (barriers since)
-    unsigned long long* o = a.phases + PHASE_WORDS * (size_t)blockIdx.x;
-    o[8] = lvs[0]; o[9] = lvs[1]; o[10] = lvs[2];
+    o[8] = lvs[0]; o[9] = lvs[1]; o[10] = lvs[2];      // every warp's sums are in (barriers since)
+    o[11] = phs[PH_LAYOUT];
   }
   trace_end(a.trace, taken);
 }
@@ -933,7 +1048,8 @@ cudaError_t launch_build_invtab(const ModConst* mods, uint32_t n, uint32_t* tab,
 
 size_t batch_smem_bytes(int /*threads*/, int k, uint32_t nq_max)
 {
-  return sizeof(uint32_t) * ((size_t)(k > 1 ? k + 1 : 2) * nq_max + STAGE_SMEM_WORDS);
+  // K-slot kernels: K state arrays, the set-up / re-layout buffer and two 16-bit position arrays
+  return sizeof(uint32_t) * ((size_t)(k > 1 ? k + 2 : 2) * nq_max + STAGE_SMEM_WORDS);
 }
 
 template <bool NARROW>

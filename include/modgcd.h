@@ -126,6 +126,21 @@ int mgcd_batch_download(mgcd_context *ctx, uint32_t *g, const uint64_t *g_off, c
    that cannot be certified is rerun with the reference's count, so results do not change.
    Single-pair calls always use the reference's count. */
 int mgcd_set_nq_scale(mgcd_context *ctx, float scale);
+/* Moduli grown on demand in batches (pairs of up to 16,384 moduli that run K per CTA):
+   each pair starts its reduction loop with `start` times the reference's count (rounded up
+   to a multiple of 32, at least 64) and, whenever the loop runs out of moduli (the
+   reference's check, GmpCudaDevice-getGcdKernel.cu:393-399), has fewer than 64 surviving
+   moduli, or ends with a result that the surviving moduli less one cannot certify, takes
+   the next step_permille / 1000 of its cap from the table, up to the cap (the reference's
+   count plus an eighth, rounded up to 32, at most 16,384).  A new modulus joins in the
+   state it would have had from the start (residues of the operands, then the pivots so far
+   replayed on it), so the result is the pair's gcd as before; the pivots after a growth may
+   differ from a run with the larger set from the start.  A pair that still fails is rerun
+   with the reference's count.  start in [0.1, 1] with step_permille in [10, 500], or
+   start = 0 (off: the class fractions of mgcd_set_nq_scale apply).  Default 0.4, 50.
+   No counterpart in the reference (its count is fixed per call, GmpCudaDevice-gcd.cu:49-55). */
+int mgcd_set_growth(mgcd_context *ctx, float start, unsigned step_permille);
+int mgcd_get_growth(const mgcd_context *ctx, float *start, unsigned *step_permille);
 /* Launch shape of single pairs too large for one CTA:
      MGCD_SINGLE_AUTO              a thread-block cluster of up to 16 CTAs (pivot exchange
                                    through distributed shared memory) while the pair's
@@ -326,11 +341,18 @@ typedef struct {
      update rounds (one position of every slot), the rounds in which some slot needed an
      inverse, and the slot states updated through the inverse; clock cycles spent re-laying
      out the positions (sorted by the slots live there, so that dead positions leave the
-     update loop) */
+     update loop); clock cycles spent growing moduli sets and the number of growth steps
+     (mgcd_set_growth) */
   uint64_t cycles_setup, cycles_update, cycles_pivot, cycles_finish, iterations, rounds, cycles_replay;
   uint64_t update_rounds, rounds_with_inverse, finite_slot_updates, cycles_layout;
+  uint64_t cycles_grow, grow_steps;
 } mgcd_cta_record;
 int mgcd_set_cta_trace(mgcd_context *ctx, int enable);
+/* Digits of pair i of the last downloaded batch (the pair_t list the reference kernel
+   writes, GmpCudaDevice-getGcdKernel.cu:437-443): *n digits into out (MGCD_ERR_CAPACITY,
+   with *n set, when cap is too small), and in *nq_final the moduli count the pair ended
+   with (grown sets included).  Diagnostics and tests; copies from the device. */
+int mgcd_batch_pair_digits(mgcd_context *ctx, size_t i, mgcd_pair *out, size_t cap, size_t *n, uint32_t *nq_final);
 int mgcd_batch_cta_trace(mgcd_context *ctx, mgcd_cta_record *out, size_t cap, size_t *n);
 /* Algorithmic bytes of the last downloaded batch, the unit of the memory roofline: per
    pair, its operand limbs (4 bytes each), a prime and an 8-byte constant for every modulus

@@ -24,6 +24,7 @@ LIB_PATH = os.path.join(LIB_DIR, "libmodgcd.so")
 
 MGCD_OK = 0
 MGCD_ERR_NO_DEVICE = 2
+MGCD_ERR_CAPACITY = 10
 STATUS_NAMES = {
     0: "MGCD_OK", 1: "MGCD_ERR_INVALID_ARG", 2: "MGCD_ERR_NO_DEVICE", 3: "MGCD_ERR_CUDA",
     4: "MGCD_ERR_NOT_ENOUGH_MODULI", 5: "MGCD_ERR_GRID", 6: "MGCD_ERR_REDUX", 7: "MGCD_ERR_RECOVERY",
@@ -99,6 +100,10 @@ SIGNATURES = {
     "mgcd_serve_stats": (_c.c_int, [_P, _c.POINTER(_c.c_uint64), _c.POINTER(_c.c_uint64),
                                     _c.POINTER(_c.c_uint64), _c.POINTER(_c.c_uint64)]),
     "mgcd_serve_trace": (_c.c_int, [_P, _P, _c.c_size_t, _c.POINTER(_c.c_size_t)]),
+    "mgcd_set_growth": (_c.c_int, [_P, _c.c_float, _c.c_uint]),
+    "mgcd_get_growth": (_c.c_int, [_P, _c.POINTER(_c.c_float), _c.POINTER(_c.c_uint)]),
+    "mgcd_batch_pair_digits": (_c.c_int, [_P, _c.c_size_t, _P, _c.c_size_t, _c.POINTER(_c.c_size_t),
+                                          _c.POINTER(_c.c_uint32)]),
 }
 
 _lib = None
@@ -328,6 +333,26 @@ class Device:
         """Fraction of the reference moduli count batches use (results are certified)."""
         _check(self._lib.mgcd_set_nq_scale(self._h, float(scale)))
 
+    def set_growth(self, start, step_permille=50):
+        """Moduli grown on demand in batches (mgcd_set_growth; start 0 turns it off)."""
+        _check(self._lib.mgcd_set_growth(self._h, float(start), int(step_permille)))
+
+    def growth(self):
+        st, pm = ctypes.c_float(), ctypes.c_uint()
+        _check(self._lib.mgcd_get_growth(self._h, ctypes.byref(st), ctypes.byref(pm)))
+        return st.value, pm.value
+
+    def batch_pair_digits(self, i):
+        """Digits [(modulus, value), ...] of pair i of the last batch and its final moduli count."""
+        n, nqf = ctypes.c_size_t(), ctypes.c_uint32()
+        rc = self._lib.mgcd_batch_pair_digits(self._h, i, None, 0, ctypes.byref(n), ctypes.byref(nqf))
+        if rc not in (MGCD_OK, MGCD_ERR_CAPACITY):
+            _check(rc)
+        d = np.zeros(max(1, n.value), dtype=[("modulus", "<u4"), ("value", "<i4")])
+        _check(self._lib.mgcd_batch_pair_digits(self._h, i, d.ctypes.data, n.value, ctypes.byref(n),
+                                                ctypes.byref(nqf)))
+        return [(int(m), int(x)) for m, x in d[: n.value]], int(nqf.value)
+
     def set_size_class(self, cls, threads, k, nq_scale):
         """Launch configuration of size class cls (0: <= 1024 moduli, 1: <= 4096,
         2: <= 16384, 3: larger, one thread-block cluster per pair)."""
@@ -473,7 +498,7 @@ CTA_RECORD = np.dtype([("size_class", "<i4"), ("sm", "<u4"), ("pairs", "<u4"), (
                        ("cycles_update", "<u8"), ("cycles_pivot", "<u8"), ("cycles_finish", "<u8"),
                        ("iterations", "<u8"), ("rounds", "<u8"), ("cycles_replay", "<u8"),
                        ("update_rounds", "<u8"), ("rounds_with_inverse", "<u8"), ("finite_slot_updates", "<u8"),
-                       ("cycles_layout", "<u8")])
+                       ("cycles_layout", "<u8"), ("cycles_grow", "<u8"), ("grow_steps", "<u8")])
 
 
 class Server:

@@ -104,10 +104,10 @@ void Plan::destroy(cudaMemPool_t)
   if (stream) cudaStreamSynchronize(stream);
   drop_graph();
   for (DevBuf* b : {&d_limbs, &d_pairs, &d_order, &d_digits, &d_count, &d_iters, &d_status, &d_queue, &d_scratch,
-                    &d_gsync, &d_retry, &d_glimbs, &d_glen})
+                    &d_gsync, &d_retry, &d_glimbs, &d_glen, &d_nqf, &d_upd})
     b->release(stream);
   if (stream) cudaStreamSynchronize(stream);
-  for (HostBuf* b : {&h_count, &h_iters, &h_status, &h_digits, &h_glimbs, &h_glen}) b->release();
+  for (HostBuf* b : {&h_count, &h_iters, &h_status, &h_digits, &h_glimbs, &h_glen, &h_nqf, &h_upd}) b->release();
   for (int i = 0; i < NSTREAMS; ++i) {
     if (bstream[i]) cudaStreamDestroy(bstream[i]);
     if (ev_b[i]) cudaEventDestroy(ev_b[i]);
@@ -128,7 +128,7 @@ size_t Plan::device_bytes() const
 {
   size_t s = 0;
   for (const DevBuf* b : {&d_limbs, &d_pairs, &d_order, &d_digits, &d_count, &d_iters, &d_status, &d_queue,
-                          &d_scratch, &d_gsync, &d_retry, &d_glimbs, &d_glen})
+                          &d_scratch, &d_gsync, &d_retry, &d_glimbs, &d_glen, &d_nqf, &d_upd})
     s += b->bytes;
   return s;
 }
@@ -322,7 +322,7 @@ int mgcd_moduli(const mgcd_context* c, uint32_t* out, size_t n)
 
 // ------------------------------------------------------------------------- batch ----
 
-static int schedule(mgcd_context* c, Plan& P, const std::vector<PairDesc>& descs, const std::vector<uint32_t>& subset,
+static int schedule(mgcd_context* c, Plan& P, std::vector<PairDesc>& descs, const std::vector<uint32_t>& subset,
                     bool plain, std::vector<Bucket>& buckets, std::vector<uint32_t>& grid_pairs, size_t& scratch,
                     bool latency = false);
 
@@ -380,11 +380,13 @@ int mgcd::plan_batch(mgcd_context* c, Plan& P, size_t np, const uint32_t* limbs,
       nq = std::min(ref_nq, std::max(256, ((int)std::ceil(scale * ref_nq) + 31) / 32 * 32));
     d.nq = (uint32_t)nq;
     d.out_off = out_off;
-    if ((uint64_t)out_off + (uint64_t)ref_nq + 1 > 0xFFFFFFFFull) return MGCD_ERR_CAPACITY;   // digit slots of one batch
-    out_off += (uint32_t)ref_nq + 1;
+    // digit slots: up to the moduli the pair may end with (a grown set: grow_cap)
+    const uint32_t slots = (!plain && c->grow_start > 0.0f) ? std::max((uint32_t)ref_nq, grow_cap(ref_nq)) : ref_nq;
+    if ((uint64_t)out_off + (uint64_t)slots + 1 > 0xFFFFFFFFull) return MGCD_ERR_CAPACITY;   // digit slots of one batch
+    out_off += slots + 1;
     d.g_off = glimbs;                 // gcd <= the smaller operand
     d.g_cap = d.v_len;
-    d.pad_ = 0;
+    d.nq_cap = 0;
     glimbs += d.g_cap;
     P.slot[i] = (int)P.descs.size();
     P.descs.push_back(d);
@@ -414,6 +416,8 @@ int mgcd::plan_batch(mgcd_context* c, Plan& P, size_t np, const uint32_t* limbs,
   CK(P.d_count.grow(std::max<size_t>(ng, 1) * sizeof(uint32_t), c->pool, s));
   CK(P.d_iters.grow(std::max<size_t>(ng, 1) * sizeof(uint32_t), c->pool, s));
   CK(P.d_status.grow(std::max<size_t>(ng, 1) * sizeof(int32_t), c->pool, s));
+  CK(P.d_nqf.grow(std::max<size_t>(ng, 1) * sizeof(uint32_t), c->pool, s));
+  CK(P.d_upd.grow(std::max<size_t>(ng, 1) * sizeof(unsigned long long), c->pool, s));
   CK(P.d_queue.grow(2 * NSTREAMS * sizeof(uint32_t), c->pool, s));
   CK(P.d_scratch.grow(std::max<size_t>(scratch, 1) * sizeof(uint32_t), c->pool, s));
   CK(P.d_gsync.grow(sizeof(GridSync), c->pool, s));
@@ -434,7 +438,7 @@ int mgcd::plan_batch(mgcd_context* c, Plan& P, size_t np, const uint32_t* limbs,
 // scratch words needed.  `latency`: the few pairs rerun after a scaled batch -- one
 // launch in which every pair has a thread-block cluster of its own (about 512 moduli per
 // CTA), so that they run side by side across the GPU instead of one CTA each.
-static int schedule(mgcd_context* c, Plan& P, const std::vector<PairDesc>& descs, const std::vector<uint32_t>& subset,
+static int schedule(mgcd_context* c, Plan& P, std::vector<PairDesc>& descs, const std::vector<uint32_t>& subset,
                     bool plain, std::vector<Bucket>& buckets, std::vector<uint32_t>& grid_pairs, size_t& scratch,
                     bool latency)
 {
@@ -513,6 +517,26 @@ static int schedule(mgcd_context* c, Plan& P, const std::vector<PairDesc>& descs
       bk.grid = (int)std::min<size_t>((v.size() + bk.k - 1) / bk.k, (size_t)nc);
       scratch += (size_t)bk.grid * 4 * bk.k * bk.nq_max;
     } else {
+      // Moduli grown on demand (K-slot kernels, k >= 2): the bucket's pairs start with the
+      // growth fraction of the reference count and may grow up to it, so shared memory and
+      // scratch are sized for the bucket's largest reference count.  Pairs of a bucket that
+      // would drop to one pair per CTA keep the class's fixed count.
+      if (!plain && c->grow_start > 0.0f) {
+        uint32_t cap_max = 0;
+        for (uint32_t k : v) cap_max = std::max(cap_max, std::max(P.ref_nq[k], grow_cap(P.ref_nq[k])));
+        int kk = bk.k;
+        while (kk > 1 && batch_smem_bytes(bk.threads, kk, cap_max) > c->smem_optin - 16384) kk /= 2;
+        if (kk >= 2 && cap_max <= CTA_MAX_NQ && cap_max <= c->moduli.size()) {
+          bk.k = kk;
+          bk.nq_max = cap_max;
+          for (uint32_t k : v) {
+            const uint32_t ref = P.ref_nq[k];
+            const uint32_t n0 = ((uint32_t)std::ceil(c->grow_start * (float)ref) + 31u) / 32u * 32u;
+            descs[k].nq = std::min(ref, std::max(64u, n0));
+            descs[k].nq_cap = std::max(ref, grow_cap(ref));
+          }
+        }
+      }
       // fewer pairs per CTA when k of the bucket's largest pairs would not fit shared memory
       // (16 KB kept for the kernel's static shared memory)
       while (bk.k > 1 && batch_smem_bytes(bk.threads, bk.k, bk.nq_max) > c->smem_optin - 16384) bk.k /= 2;
@@ -588,6 +612,9 @@ static int launch_set(mgcd_context* c, Plan& P, const std::vector<Bucket>& bucke
     a.count = P.d_count.as<uint32_t>();
     a.iters = P.d_iters.as<uint32_t>();
     a.status = P.d_status.as<int32_t>();
+    a.grow_permille = c->grow_permille;
+    a.nq_final = P.d_nqf.as<uint32_t>();
+    a.updates = P.d_upd.as<unsigned long long>();
     CK(cudaStreamWaitEvent(P.bstream[b], P.ev_start, 0));
     if (time_buckets) CK(cudaEventRecord(P.t_b0[b], P.bstream[b]));
     if (bk.csize)
@@ -711,7 +738,10 @@ int mgcd::run_plan(mgcd_context* c, Plan& P)
       // joined back into P.stream); each later run is a single graph launch.
       CK(cudaStreamBeginCapture(P.stream, cudaStreamCaptureModeThreadLocal));
       int rc = MGCD_OK;
-      if (cudaMemsetAsync(P.d_status.p, 0xFF, ng * sizeof(int32_t), P.stream) != cudaSuccess) rc = MGCD_ERR_CUDA;
+      if (cudaMemsetAsync(P.d_status.p, 0xFF, ng * sizeof(int32_t), P.stream) != cudaSuccess ||
+          cudaMemsetAsync(P.d_nqf.p, 0, ng * sizeof(uint32_t), P.stream) != cudaSuccess ||
+          cudaMemsetAsync(P.d_upd.p, 0, ng * sizeof(unsigned long long), P.stream) != cudaSuccess)
+        rc = MGCD_ERR_CUDA;
       if (rc == MGCD_OK)
         rc = launch_set(c, P, P.buckets, P.grid_pairs, P.descs, P.d_pairs.as<PairDesc>(), P.d_queue.as<uint32_t>(),
                         false);
@@ -734,6 +764,8 @@ int mgcd::run_plan(mgcd_context* c, Plan& P)
   } else {
     CK(cudaEventRecord(P.t_run0, P.stream));
     CK(cudaMemsetAsync(P.d_status.p, 0xFF, ng * sizeof(int32_t), P.stream));
+    CK(cudaMemsetAsync(P.d_nqf.p, 0, ng * sizeof(uint32_t), P.stream));
+    CK(cudaMemsetAsync(P.d_upd.p, 0, ng * sizeof(unsigned long long), P.stream));
     int rc = launch_set(c, P, P.buckets, P.grid_pairs, P.descs, P.d_pairs.as<PairDesc>(), P.d_queue.as<uint32_t>(),
                         true);
     if (rc == MGCD_OK) rc = launch_convert(c, P);
@@ -770,6 +802,7 @@ int mgcd::sync_plan(mgcd_context* c, Plan& P)
   std::vector<PairDesc> rd = P.descs;
   for (uint32_t k : redo) {
     rd[k].nq = P.ref_nq[k];
+    rd[k].nq_cap = 0;
     P.eff_nq[k] = P.ref_nq[k];
   }
   const size_t main_order = P.order.size();
@@ -822,6 +855,8 @@ int mgcd::fetch(mgcd_context* c, Plan& P)
   CK(P.h_status.grow(ng * sizeof(int32_t)));
   CK(P.h_glen.grow(ng * sizeof(uint32_t)));
   CK(P.h_glimbs.grow(std::max<size_t>(P.nglimbs, 1) * sizeof(uint32_t)));
+  CK(P.h_nqf.grow(ng * sizeof(uint32_t)));
+  CK(P.h_upd.grow(ng * sizeof(unsigned long long)));
   if (P.plain) CK(P.h_digits.grow(std::max<size_t>(P.ndig, 1) * sizeof(mgcd_pair)));
   cudaStream_t s = P.stream;
   // Results as binary limbs (converted on the device); digits only where the caller wants
@@ -831,7 +866,9 @@ int mgcd::fetch(mgcd_context* c, Plan& P)
   CK(cudaMemcpyAsync(P.h_status.p, P.d_status.p, ng * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(P.h_glen.p, P.d_glen.p, ng * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(P.h_glimbs.p, P.d_glimbs.p, P.nglimbs * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-  uint64_t d2h = ng * 4 * sizeof(uint32_t) + P.nglimbs * sizeof(uint32_t);
+  CK(cudaMemcpyAsync(P.h_nqf.p, P.d_nqf.p, ng * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(P.h_upd.p, P.d_upd.p, ng * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+  uint64_t d2h = ng * (5 * sizeof(uint32_t) + sizeof(unsigned long long)) + P.nglimbs * sizeof(uint32_t);
   if (P.plain) {
     CK(cudaMemcpyAsync(P.h_digits.p, P.d_digits.p, P.ndig * sizeof(mgcd_pair), cudaMemcpyDeviceToHost, s));
     d2h += P.ndig * sizeof(mgcd_pair);
@@ -862,14 +899,20 @@ int mgcd::fetch(mgcd_context* c, Plan& P)
   const int32_t* st = P.h_status.as<int32_t>();
   double R = 0, E = 0, M = 0, B = 0, AB = 0;
   std::vector<double> pw(4 * ng, 0.0);    // per pair: R, E, M, B
+  const uint32_t* nqf = P.h_nqf.as<uint32_t>();
+  const unsigned long long* upd = P.h_upd.as<unsigned long long>();
   for (size_t k = 0; k < ng; ++k) {
     const PairDesc& d = P.descs[k];
     double* w = &pw[4 * k];
-    w[0] = (double)d.nq * (d.u_len + d.v_len);
+    // the K-slot kernels record the final moduli count and the loop's updates (a pair's set
+    // may have grown); a rerun pair, or one of another kernel, ran with eff_nq throughout
+    const bool rec = nqf[k] != 0u && P.eff_nq[k] == d.nq;
+    const double N = rec ? (double)nqf[k] : (double)P.eff_nq[k];
+    w[0] = N * (d.u_len + d.v_len);
     w[3] = 4.0 * (d.u_len + d.v_len);
     if (st[k] == ST_OK) {
-      const double I = it[k], K = cnt[k], N = P.eff_nq[k];
-      w[1] = I * N - I * (I + 1) / 2;
+      const double I = it[k], K = cnt[k];
+      w[1] = rec ? (double)upd[k] : I * N - I * (I + 1) / 2;
       w[2] = K * (N - I) - K * (K + 1) / 2;
       AB += 12.0 * N + 8.0 * (K + 1);      // a prime and its 8-byte constant per modulus, digits
     }
@@ -956,6 +999,27 @@ int mgcd_set_nq_scale(mgcd_context* c, float scale)
   return MGCD_OK;
 }
 
+static bool valid_growth(float start, unsigned step_permille)
+{
+  return start == 0.0f || (start >= 0.1f && start <= 1.0f && step_permille >= 10u && step_permille <= 500u);
+}
+
+int mgcd_set_growth(mgcd_context* c, float start, unsigned step_permille)
+{
+  if (!c || !valid_growth(start, step_permille)) return MGCD_ERR_INVALID_ARG;
+  c->grow_start = start;
+  c->grow_permille = step_permille;
+  return MGCD_OK;
+}
+
+int mgcd_get_growth(const mgcd_context* c, float* start, unsigned* step_permille)
+{
+  if (!c) return MGCD_ERR_INVALID_ARG;
+  if (start) *start = c->grow_start;
+  if (step_permille) *step_permille = c->grow_permille;
+  return MGCD_OK;
+}
+
 // Launch configurations that exist: CTA size 256/512/1024 with k = 1, 2, 4, or k = 8 with
 // 512 threads (not in the cluster class).
 static bool valid_class_cfg(int cls, int threads, int k, float nq_scale)
@@ -1005,7 +1069,8 @@ int mgcd_get_class_cluster(const mgcd_context* c, int cls, int* ctas)
   return MGCD_OK;
 }
 
-// Tuning table: one line per size class, "class threads k nq_scale cluster_ctas" ('#' starts
+// Tuning table: one line per size class, "class threads k nq_scale cluster_ctas", and
+// optionally "grow start step_permille" (moduli grown on demand, mgcd_set_growth; '#' starts
 // a comment).  All lines are checked before any is applied.
 int mgcd_load_tuning(mgcd_context* c, const char* path)
 {
@@ -1017,10 +1082,16 @@ int mgcd_load_tuning(mgcd_context* c, const char* path)
   std::memcpy(cfg, c->cfg, sizeof(cfg));
   char line[256];
   int rc = MGCD_OK;
+  float g_start = c->grow_start;
+  unsigned g_step = c->grow_permille;
   while (rc == MGCD_OK && std::fgets(line, sizeof line, f)) {
     const char* s = line;
     while (*s == ' ' || *s == '\t') ++s;
     if (*s == '#' || *s == '\n' || *s == '\r' || *s == 0) continue;
+    if (std::strncmp(s, "grow", 4) == 0) {
+      if (std::sscanf(s + 4, "%f %u", &g_start, &g_step) != 2 || !valid_growth(g_start, g_step)) rc = MGCD_ERR_INVALID_ARG;
+      continue;
+    }
     int cls, threads, k, cs;
     float sc;
     if (std::sscanf(s, "%d %d %d %f %d", &cls, &threads, &k, &sc, &cs) != 5 || !valid_class_cfg(cls, threads, k, sc) ||
@@ -1034,7 +1105,11 @@ int mgcd_load_tuning(mgcd_context* c, const char* path)
     cfg[cls].csize = cs;
   }
   std::fclose(f);
-  if (rc == MGCD_OK) std::memcpy(c->cfg, cfg, sizeof(cfg));
+  if (rc == MGCD_OK) {
+    std::memcpy(c->cfg, cfg, sizeof(cfg));
+    c->grow_start = g_start;
+    c->grow_permille = g_step;
+  }
   return rc;
 }
 
@@ -1046,6 +1121,7 @@ int mgcd_save_tuning(const mgcd_context* c, const char* path)
   std::fprintf(f, "# modgcd tuning table (modulus width %d): class threads k nq_scale cluster_ctas\n", c->L);
   for (int i = 0; i < NSTREAMS; ++i)
     std::fprintf(f, "%d %d %d %.3f %d\n", i, c->cfg[i].threads, c->cfg[i].k, c->cfg[i].nq_scale, c->cfg[i].csize);
+  std::fprintf(f, "grow %.3f %u\n", c->grow_start, c->grow_permille);
   return std::fclose(f) == 0 ? MGCD_OK : MGCD_ERR_INVALID_ARG;
 }
 
@@ -1289,7 +1365,30 @@ int mgcd_batch_cta_trace(mgcd_context* c, mgcd_cta_record* out, size_t cap, size
     r.rounds_with_inverse = ph[PHASE_WORDS * i + 9];
     r.finite_slot_updates = ph[PHASE_WORDS * i + 10];
     r.cycles_layout = ph[PHASE_WORDS * i + 11];
+    r.cycles_grow = ph[PHASE_WORDS * i + 12];
+    r.grow_steps = ph[PHASE_WORDS * i + 13];
   }
+  return MGCD_OK;
+}
+
+int mgcd_batch_pair_digits(mgcd_context* c, size_t i, mgcd_pair* out, size_t cap, size_t* n, uint32_t* nq_final)
+{
+  if (!c || !n) return MGCD_ERR_INVALID_ARG;
+  Plan& P = c->main;
+  if (!P.synced || i >= P.np) return MGCD_ERR_INVALID_ARG;
+  const int k = P.slot[i];
+  if (k < 0 || P.h_count.p == nullptr) return MGCD_ERR_INVALID_ARG;
+  const size_t cnt = P.h_count.as<uint32_t>()[k];
+  *n = cnt;
+  if (nq_final) {
+    const uint32_t f = P.h_nqf.p ? P.h_nqf.as<uint32_t>()[k] : 0u;
+    *nq_final = (f != 0u && P.eff_nq[k] == P.descs[k].nq) ? f : P.eff_nq[k];
+  }
+  if (cnt > cap) return MGCD_ERR_CAPACITY;
+  CK(cudaSetDevice(c->device));
+  if (cnt)
+    CK(cudaMemcpy(out, P.d_digits.as<mgcd_pair>() + P.descs[k].out_off, cnt * sizeof(mgcd_pair),
+                  cudaMemcpyDeviceToHost));
   return MGCD_OK;
 }
 

@@ -228,6 +228,25 @@ __device__ __forceinline__ uint32_t inv_mod_narrow(uint32_t x, uint32_t q, uint3
   return inv_mod_slow(x, q);
 }
 
+// Register arrays indexed by a runtime slot number, without spilling them to memory.
+template <int K, class V>
+__device__ __forceinline__ V pick(const V (&a)[K], int s)
+{
+  V r = a[0];
+#pragma unroll
+  for (int t = 1; t < K; ++t)
+    if (t == s) r = a[t];
+  return r;
+}
+
+template <int K, class V>
+__device__ __forceinline__ void put(V (&a)[K], int s, V v)
+{
+#pragma unroll
+  for (int t = 0; t < K; ++t)
+    if (t == s) a[t] = v;
+}
+
 // Key of the reduction loop's pivot choice (postMinPair, GmpCudaDevice-getGcdKernel.cu:152-154):
 // high word |value| (0x80000000 for MOD_INFINITY), low word modulus - (value >= 0).
 __device__ __forceinline__ void t_key(uint32_t t, uint32_t q, uint32_t& hi, uint32_t& lo)
@@ -300,11 +319,22 @@ __device__ __forceinline__ void t_update_k(uint32_t (&t)[K], const ModConst& c, 
     need |= 1u << s;
   }
   if (!need) return;
+  // one slot needing an inverse (common where the slots' live moduli differ): no batch
+  const bool one = (need & (need - 1u)) == 0u;
+  const int s1 = __ffs((int)need) - 1;
   uint32_t P[K];
   P[0] = x[0];
+  if (!one) {
 #pragma unroll
-  for (int s = 1; s < K; ++s) P[s] = mont_mul(P[s - 1], x[s], q, qinv);
-  uint32_t Z = mont_mul(inv_mod(P[K - 1], q, qinv), c.r2, q, qinv);   // times R
+    for (int s = 1; s < K; ++s) P[s] = mont_mul(P[s - 1], x[s], q, qinv);
+  }
+  const uint32_t xin = one ? pick<K>(x, s1) : P[K - 1];
+  uint32_t Z = mont_mul(inv_mod(xin, q, qinv), c.r2, q, qinv);   // times R
+  if (one) {
+    const uint32_t ps = pick<K>(p, s1);
+    put<K>(t, s1, mont_mul(ps > q ? ps - q : ps, Z, q, qinv));
+    return;
+  }
 #pragma unroll
   for (int s = K - 1; s >= 1; --s) {
     const uint32_t y = mont_mul(Z, P[s - 1], q, qinv);
@@ -357,11 +387,21 @@ __device__ __forceinline__ void t_update_k_narrow(uint32_t (&t)[K], const ModCon
     need |= 1u << s;
   }
   if (!need) return;
+  // one slot needing an inverse (common where the slots' live moduli differ): no batch
+  const bool one = (need & (need - 1u)) == 0u;
+  const int s1 = __ffs((int)need) - 1;
   uint32_t P[K];
   P[0] = x[0];
+  if (!one) {
 #pragma unroll
-  for (int s = 1; s < K; ++s) P[s] = mont_mul_lazy(P[s - 1], x[s], q, qinv);
-  uint32_t Z = mont_mul_lazy(inv_mod_narrow(mod_canon(P[K - 1], q), q, qinv), c.r2, q, qinv);   // times R
+    for (int s = 1; s < K; ++s) P[s] = mont_mul_lazy(P[s - 1], x[s], q, qinv);
+  }
+  const uint32_t xin = one ? pick<K>(x, s1) : P[K - 1];
+  uint32_t Z = mont_mul_lazy(inv_mod_narrow(mod_canon(xin, q), q, qinv), c.r2, q, qinv);   // times R
+  if (one) {
+    put<K>(t, s1, mod_canon(mont_mul_lazy(pick<K>(p, s1), Z, q, qinv), q));
+    return;
+  }
 #pragma unroll
   for (int s = K - 1; s >= 1; --s) {
     const uint32_t y = mont_mul_lazy(Z, P[s - 1], q, qinv);

@@ -20,7 +20,8 @@ struct PairDesc {
   uint32_t out_off;  // first digit slot in the digit array; nq + 1 slots are reserved
   uint64_t g_off;    // first limb of the binary gcd in the result-limb array
   uint32_t g_cap;    // limbs reserved there (the smaller operand's length)
-  uint32_t pad_;
+  uint32_t nq_cap;   // moduli the pair may grow to during its reduction loop (the reference's
+                     // count; <= nq: no growth)
 };
 
 // Device-side mixed-radix conversion (mgcd_radix_dev.cu): pairs with up to RADIX_MAX
@@ -68,7 +69,7 @@ struct StreamRing {
   uint32_t iters[STREAM_RING];
 };
 
-constexpr int PHASE_WORDS = 12;
+constexpr int PHASE_WORDS = 14;
 
 struct BatchArgs {
   InvTab inv;
@@ -92,6 +93,9 @@ struct BatchArgs {
                               // set-up, update, pivot choice and finish, reduction iterations, moduli
                               // rounds, pairs, cycles of certification and replay; over all threads:
                               // update rounds, rounds that needed an inverse, finite slot states (null: off)
+  uint32_t grow_permille;    // moduli added per growth step, thousandths of the pair's nq_cap
+  uint32_t* nq_final;        // per pair: moduli in its set at the end (null: not recorded)
+  unsigned long long* updates; // per pair: surviving moduli summed over its iterations (null: off)
   StreamRing* ring;          // ring mode (device view of the mapped ring)
   uint32_t* ring_head;       // entries claimed (device memory)
   unsigned long long idle_ns;  // ring mode: a CTA whose slots are all empty leaves after this long idle

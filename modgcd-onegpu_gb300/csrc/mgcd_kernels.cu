@@ -166,25 +166,6 @@ __device__ __forceinline__ void block_min_keys(uint32_t (&kh)[K], uint32_t (&kl)
   parity ^= 1u;
 }
 
-// Register arrays indexed by a runtime slot number, without spilling them to memory.
-template <int K, class V>
-__device__ __forceinline__ V pick(const V (&a)[K], int s)
-{
-  V r = a[0];
-#pragma unroll
-  for (int t = 1; t < K; ++t)
-    if (t == s) r = a[t];
-  return r;
-}
-
-template <int K, class V>
-__device__ __forceinline__ void put(V (&a)[K], int s, V v)
-{
-#pragma unroll
-  for (int t = 0; t < K; ++t)
-    if (t == s) a[t] = v;
-}
-
 // Per-slot loop state of batchk_kernel in shared memory.  Warp s owns slot s's entries
 // during the pivot step; every thread reads them only after a barrier that follows the
 // writes, and the next writes come only after a barrier that follows the reads.  Keeping it
@@ -202,6 +183,7 @@ struct SlotState {
   uint32_t iters[K];
   uint32_t res[K];                   // slot_step's result for the slot's last pivot
   uint32_t seq[K];                   // ring mode: the slot's entry number
+  unsigned long long upd[K];         // surviving moduli summed over the slot's iterations (work)
   uint32_t stop;                     // set-up: slot_step's result for the first pivot
 };
 
@@ -209,19 +191,27 @@ struct SlotState {
 // of thread 0 per phase, loop iterations, moduli rounds, pairs taken, the replay's share of
 // the finish; words 8-10 are the update loop's liveness counters (every thread).
 // Word 11: cycles spent re-laying out the positions.
-enum { PH_LOAD = 0, PH_UPDATE, PH_PIVOT, PH_FINISH, PH_ITERS, PH_ROUNDS, PH_TAKEN, PH_REPLAY, PH_LAYOUT };
-constexpr int PH_WORDS_T0 = 9;          // words kept by thread 0
+// Word 12: cycles spent growing moduli sets; word 13: growth steps.
+enum { PH_LOAD = 0, PH_UPDATE, PH_PIVOT, PH_FINISH, PH_ITERS, PH_ROUNDS, PH_TAKEN, PH_REPLAY, PH_LAYOUT, PH_GROW,
+       PH_GROWS };
+constexpr int PH_WORDS_T0 = 11;         // words kept by thread 0
 
 // Iterations between two re-layouts of a K-slot CTA's positions (besides those after a pair
 // finishes or is loaded).  Each iteration retires one position per slot, so a layout stays
 // close to sorted; one re-layout moves (K + 1) x nq_max words twice.
 constexpr uint32_t RELAYOUT_EVERY = 16;
 
+// A pair that may grow its moduli set grows whenever fewer than GROW_LOW of its moduli
+// survive: near the end of a set each iteration reduces the operands by only about
+// log2(survivors) bits, so a set run down to a handful costs iterations that do little.
+constexpr int GROW_LOW = 64;
+
 // One reduction-loop step of slot s's bookkeeping for its current pivot (the reference's
 // per-iteration checks, GmpCudaDevice-getGcdKernel.cu:365-402): records (p, b) in the
-// history; returns 0 (continue), 1 (loop ended: b = INF) or 3 (ran out of moduli).  One
-// thread per slot.  The certification bounds are stepped for this pivot during the update
-// that uses it, by the last warp (below), off the path between the two barriers.
+// history; returns 0 (continue), 1 (loop ended: b = INF), 3 (ran out of moduli) or 4 (ran
+// out, or fewer than GROW_LOW moduli survive, and the pair may grow its moduli set: grow
+// before the update that applies this pivot).  One thread per slot.  The certification bounds are stepped for this pivot during
+// the update that uses it, by the last warp (below), off the path between the two barriers.
 template <int K>
 __device__ __forceinline__ uint32_t slot_step(SlotState<K>& ss, int s, int2* hist, int L)
 {
@@ -232,12 +222,23 @@ __device__ __forceinline__ uint32_t slot_step(SlotState<K>& ss, int s, int2* his
   ss.iters[s] += 1u;
   const int rem = ss.rem[s] - 1;
   ss.rem[s] = rem;
+  ss.upd[s] += (unsigned long long)rem;
   const uint32_t ab = b < 0 ? 0u - (uint32_t)b : (uint32_t)b;
   const int tbits = ss.ubits[s] - (L - 1) + __ffs((int)ab);
   const int ub = ss.vbits[s];
   ss.ubits[s] = ub;
   ss.vbits[s] = tbits;
-  return rem * (L - 2) <= ub ? 3u : 0u;
+  const bool can_grow = ss.d[s].nq_cap > ss.d[s].nq;
+  if (rem * (L - 2) <= ub) return can_grow ? 4u : 3u;
+  return can_grow && rem < GROW_LOW ? 4u : 0u;
+}
+
+// Moduli added to a pair's set by one growth step: `permille` thousandths of its cap,
+// rounded up to a warp (32).
+__device__ __forceinline__ uint32_t grow_step_for(uint32_t cap, uint32_t permille)
+{
+  const uint32_t n = (uint32_t)(((unsigned long long)cap * permille + 999ull) / 1000ull);
+  return n < 32u ? 32u : (n + 31u) & ~31u;
 }
 
 // Position layout.  The K slots share every modulus's inverse, so their states sit at common
@@ -330,7 +331,7 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
           const volatile PairDesc* e = &a.ring->desc[k % STREAM_RING];
           PairDesc d;
           d.u_off = e->u_off; d.v_off = e->v_off; d.u_len = e->u_len; d.v_len = e->v_len;
-          d.nq = e->nq; d.out_off = e->out_off; d.g_off = e->g_off; d.g_cap = e->g_cap; d.pad_ = 0u;
+          d.nq = e->nq; d.out_off = e->out_off; d.g_off = e->g_off; d.g_cap = e->g_cap; d.nq_cap = 0u;
           ss.pi[s] = k % STREAM_RING;
           ss.seq[s] = k;
           ss.d[s] = d;
@@ -375,6 +376,7 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
       ss.ubits[s] = ((int)d.u_len + 1) * 32;
       ss.vbits[s] = ((int)d.v_len + 1) * 32;
       ss.iters[s] = 0u;
+      ss.upd[s] = 0ull;
       ss.lu[s] = bound_init(a.limbs + d.u_off, d.u_len);
       ss.lv[s] = bound_init(a.limbs + d.v_off, d.v_len);
       ss.stop = 16u | slot_step<K>(ss, s, hist_of(s), L);
@@ -385,6 +387,8 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
     return r;
   };
   uint32_t npos = 0, fresh = 0, since = 0;             // positions visited; slots in modulus order
+  uint32_t grow = 0, failed = 0;                      // slots to grow before the next update; slots
+                                                      // whose growth could not stage its operands
   auto take_slot = [&](int s, bool wait) {
     ph_mark(PH_FINISH);
     const uint32_t r = load(s, wait);
@@ -394,7 +398,99 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
       fresh |= 1u << s;
       if (!(r & 1u)) active |= 1u << s;
       if ((r & 3u) == 3u) redux |= 1u << s;
+      if (r & 4u) grow |= 1u << s;
     }
+  };
+  // Slot s's states back into modulus order (ts[m] for the modulus of table index m < nq).
+  auto to_modulus_order = [&](int s) {
+    if ((fresh >> s) & 1u) return;
+    const uint32_t nq = ss.d[s].nq;
+    uint32_t* ts = tS + (size_t)s * NQS;
+    for (uint32_t pos = threadIdx.x; pos < NQS; pos += T) {
+      const uint32_t m = pmod[pos];
+      if (m < nq) acc2[m] = ts[pos];
+    }
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < nq; j += T) ts[j] = acc2[j];
+    __syncthreads();
+  };
+
+  // ---- moduli grown on demand (batches; not in ring mode).  A pair starts with fewer moduli
+  // than the reference's count and takes the next table entries, up to its nq_cap, when its
+  // loop runs out of moduli (the reference's check) or ends without a certified result.  A
+  // new modulus q joins in the state it would have had from the start: the operands'
+  // residues, then the first nrep pivots of the history replayed projectively,
+  // (U, V) <- (p V, U - b V) (the ratio U/V is all a state holds; the replay reaches the
+  // same INF, degenerate and zero states as the loop's updates), then t = U/V.  The slot is
+  // put into modulus order and the next re-layout takes the new states in (`fresh`).  Its
+  // moduli count, survivors and the operands' residues (u0, v0, for the final replay) grow
+  // with it.  Every thread calls it; returns this thread's minimum key over the new states
+  // in (h0, l0), or false (nothing added) if an operand tile could not be staged.
+  auto grow_slot = [&](int s, uint32_t nrep, uint32_t& h0, uint32_t& l0) -> bool {
+    const PairDesc& d = ss.d[s];
+    const uint32_t n0 = d.nq;
+    const uint32_t n1 = min(d.nq_cap, n0 + grow_step_for(d.nq_cap, a.grow_permille));
+    const uint32_t dn = n1 - n0;
+    uint32_t* ts = tS + (size_t)s * NQS;
+    uint32_t* u0 = scr + (size_t)s * 4 * NQS;
+    to_modulus_order(s);
+    const Stage stg = stage();
+    bool ok = residues<T>(a.limbs + d.u_off, d.u_len, a.mods + n0, dn, acc2, stg, NARROW);
+    for (uint32_t j = threadIdx.x; j < dn; j += T) u0[n0 + j] = acc2[j];
+    ok = residues<T>(a.limbs + d.v_off, d.v_len, a.mods + n0, dn, acc2, stg, NARROW) && ok;
+    for (uint32_t j = threadIdx.x; j < dn; j += T) u0[NQS + n0 + j] = acc2[j];
+    if (!ok) return false;
+    const int2* hist = hist_of(s);
+    int2* const hb = reinterpret_cast<int2*>(smem);   // the staging buffers (free again)
+    for (uint32_t base = 0; base < dn; base += T) {
+      const bool have = base + threadIdx.x < dn;
+      const uint32_t j = n0 + base + threadIdx.x;
+      const ModConst c = a.mods[have ? j : n0];
+      const uint32_t q = c.q, qi = c.qinv;
+      uint32_t U = have ? u0[j] : 0u, V = have ? u0[NQS + j] : 0u;
+      for (uint32_t c0 = 0; c0 < nrep; c0 += REPLAY_CHUNK) {
+        const uint32_t n = nrep - c0 < REPLAY_CHUNK ? nrep - c0 : REPLAY_CHUNK;
+        __syncthreads();                              // the previous chunk is consumed
+        for (uint32_t e = threadIdx.x; e < n; e += T) hb[e] = hist[c0 + e];
+        __syncthreads();
+        if (!have) continue;
+#pragma unroll 4
+        for (uint32_t e = 0; e < n; ++e) {
+          const int2 h = hb[e];
+          const uint32_t pp = (uint32_t)h.x;
+          const uint32_t pm = pp > q ? pp - q : pp;
+          const uint32_t bn = from_signed(-h.y, q);   // -b mod q
+          if constexpr (NARROW) {                    // lazily in [0, 2q), as the final replay
+            const uint64_t T2 = (uint64_t)bn * V + U;
+            const uint32_t U2 = mont_mul_lazy(V, pm, q, qi);
+            const uint32_t lo = (uint32_t)T2, hi = (uint32_t)(T2 >> 32);
+            V = hi + __umulhi(lo * qi, q) + (lo != 0u);
+            U = U2;
+          } else {
+            const uint32_t U2 = mont_mul(V, pm, q, qi);
+            V = redc((uint64_t)bn * V + U, q, qi);
+            U = U2;
+          }
+        }
+      }
+      if (have) {
+        if constexpr (NARROW) { U = mod_canon(U, q); V = mod_canon(V, q); }
+        const uint32_t t = t_init(U, V, q, qi);
+        ts[j] = t;
+        uint32_t h, l;
+        t_key(t, q, h, l);
+        if (key_less(h, l, h0, l0)) { h0 = h; l0 = l; }
+      }
+    }
+    __syncthreads();                                  // hb, the new states
+    if (threadIdx.x == 0) {
+      ss.d[s].nq = n1;
+      ss.rem[s] += (int)dn;
+      if (prof) phs[PH_GROWS] += 1u;
+    }
+    __syncthreads();
+    fresh |= 1u << s;
+    return true;
   };
 
   // ---- position layout
@@ -480,23 +576,54 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
 #pragma unroll 1
     for (int s = 0; s < K; ++s) {
       if (!((done >> s) & 1u)) continue;
-      const uint32_t pi = ss.pi[s];
-      const uint32_t it = ss.iters[s];
-      if (threadIdx.x == 0) a.iters[pi] = it;
-      if ((redux >> s) & 1u) {
-        if (threadIdx.x == 0) { a.status[pi] = ST_REDUX; a.count[pi] = 0; }
-      } else {
-        if (!((fresh >> s) & 1u)) {                  // back to modulus order
-          const uint32_t nq = ss.d[s].nq;
-          uint32_t* ts = tS + (size_t)s * NQS;
-          for (uint32_t pos = threadIdx.x; pos < NQS; pos += T) {
-            const uint32_t m = pmod[pos];
-            if (m < nq) acc2[m] = ts[pos];
+      if constexpr (!RING) {
+        // the loop ended: a result that the surviving moduli cannot certify grows the set
+        // (replayed through the whole history) and goes on with the pivot chosen over it
+        while (!((redux | failed) >> s & 1u) && ss.d[s].nq_cap > ss.d[s].nq) {
+          // one modulus to spare: the recovery stops at the first all-zero round, so it
+          // needs one survivor more than it has digits
+          if (threadIdx.x == 0) ss.stop = bound_certified(ss.rem[s] - 1, L, ss.lu[s], ss.lv[s]) ? 1u : 0u;
+          __syncthreads();
+          const bool cert = ss.stop != 0u;
+          __syncthreads();
+          if (cert) break;
+          ph_mark(PH_FINISH);
+          uint32_t h0 = 0xFFFFFFFFu, l0 = 0xFFFFFFFFu;
+          const bool ok = grow_slot(s, ss.iters[s], h0, l0);
+          if (!ok) {
+            failed |= 1u << s;
+            ph_mark(PH_GROW);
+            break;
+          }
+          block_min_key<T>(h0, l0, rs, rparity);
+          if (threadIdx.x == 0) {
+            if (h0 == 0xFFFFFFFFu) { h0 = KEY_INF_HI; l0 = 0xFFFFFFFFu; }
+            key_pair(h0, l0, ss.p[s], ss.b[s]);
+            ss.stop = slot_step<K>(ss, s, hist_of(s), L);
           }
           __syncthreads();
-          for (uint32_t j = threadIdx.x; j < nq; j += T) ts[j] = acc2[j];
+          const uint32_t r = ss.stop;
           __syncthreads();
+          ph_mark(PH_GROW);
+          if (r & 2u) redux |= 1u << s;
+          if (r & 4u) grow |= 1u << s;
+          if (!(r & 1u)) { active |= 1u << s; break; }
         }
+        if ((active >> s) & 1u) { changed = true; continue; }   // back in the loop
+      }
+      const uint32_t pi = ss.pi[s];
+      const uint32_t it = ss.iters[s];
+      if (threadIdx.x == 0) {
+        a.iters[pi] = it;
+        if (a.nq_final) a.nq_final[pi] = ss.d[s].nq;
+        if (a.updates) a.updates[pi] = ss.upd[s];
+      }
+      if ((failed >> s) & 1u) {
+        if (threadIdx.x == 0) { a.status[pi] = ST_TIMEOUT; a.count[pi] = 0; }
+      } else if ((redux >> s) & 1u) {
+        if (threadIdx.x == 0) { a.status[pi] = ST_REDUX; a.count[pi] = 0; }
+      } else {
+        to_modulus_order(s);
         uint32_t* u0 = scr + (size_t)s * 4 * NQS;
         finish_pair<T, SYNC_CTA>(a.mods, ss.d[s], L, 0u, ss.d[s].nq, tS + (size_t)s * NQS, rs, rparity, repoch, nullptr,
                               u0, u0 + NQS, reinterpret_cast<const int2*>(u0 + 2 * (size_t)NQS), it, ss.rem[s],
@@ -508,6 +635,8 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
       valid &= ~(1u << s);
       redux &= ~(1u << s);
       fresh &= ~(1u << s);
+      grow &= ~(1u << s);
+      failed &= ~(1u << s);
       changed = true;
       if (!RING) take_slot(s, false);
     }
@@ -524,6 +653,22 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
     }
     if (!valid) break;
     ph_mark(PH_FINISH);
+    if constexpr (!RING) {
+      // slots that ran out of moduli at their current pivot: the set grows before the update
+      // that applies it (the new moduli replay the history without it)
+#pragma unroll 1
+      for (int s = 0; s < K; ++s) {
+        if (!((grow >> s) & 1u)) continue;
+        grow &= ~(1u << s);
+        uint32_t h0 = 0xFFFFFFFFu, l0 = 0xFFFFFFFFu;
+        if (!grow_slot(s, ss.iters[s] - 1u, h0, l0)) {   // the pair ends: a failed staging
+          failed |= 1u << s;
+          active &= ~(1u << s);
+        }
+        changed = true;
+      }
+      ph_mark(PH_GROW);
+    }
     if (changed || since >= RELAYOUT_EVERY) {
       relayout();
       since = 0;
@@ -608,6 +753,7 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
       const uint32_t r = ss.res[s];
       if (r & 1u) active &= ~(1u << s);
       if (r & 2u) redux |= 1u << s;
+      if (r & 4u) grow |= 1u << s;
     }
     ph_mark(PH_PIVOT);
   }
@@ -619,6 +765,8 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
     o[PH_TAKEN] = taken;
     o[8] = lvs[0]; o[9] = lvs[1]; o[10] = lvs[2];      // every warp's sums are in (barriers since)
     o[11] = phs[PH_LAYOUT];
+    o[12] = phs[PH_GROW];
+    o[13] = phs[PH_GROWS];
   }
   trace_end(a.trace, taken);
 }

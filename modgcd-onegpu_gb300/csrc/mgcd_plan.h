@@ -5,6 +5,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <vector>
 
@@ -55,6 +56,12 @@ constexpr size_t INVTAB_N = 16384;        // moduli covered by the pairwise inve
 
 inline int size_class(uint32_t nq) { return nq <= 1024 ? 0 : nq <= 4096 ? 1 : nq <= CTA_MAX_NQ ? 2 : CLUSTER_CLASS; }
 
+// Moduli a batched pair may grow to (mgcd_set_growth): an eighth more than the reference's
+// count, so that a pair whose smaller sets took more iterations still ends in its own loop
+// (with the growth policy's defaults no pair of the mixed 1k-64k-bit batches went past the
+// reference's count in the oracle's runs), rounded up to a warp.
+inline uint32_t grow_cap(uint32_t ref) { return std::min<uint32_t>(CTA_MAX_NQ, (ref + ref / 8 + 31u) / 32u * 32u); }
+
 struct Plan {
   cudaStream_t stream = nullptr;
   cudaStream_t bstream[NSTREAMS] = {};
@@ -81,11 +88,12 @@ struct Plan {
   int cluster_k = 0;                   // pairs per cluster of size class 3 (0: the context's setting)
 
   DevBuf d_limbs, d_pairs, d_order, d_digits, d_count, d_iters, d_status, d_queue, d_scratch, d_gsync, d_retry;
+  DevBuf d_nqf, d_upd;                 // per pair (K-slot kernels): final moduli count, loop updates
   DevBuf d_glimbs, d_glen;             // binary gcds converted on the device
   DevBuf d_trace;                      // per-CTA occupancy trace of the bucket kernels (4 words each)
   DevBuf d_phases;                     // per-CTA phase accounting of the K-slot kernels (8 words each)
   std::vector<int> trace_cls;          // size class of each traced CTA (launch order)
-  HostBuf h_count, h_iters, h_status, h_digits, h_glimbs, h_glen;
+  HostBuf h_count, h_iters, h_status, h_digits, h_glimbs, h_glen, h_nqf, h_upd;
   int launches = 0, retried = 0;
   bool ran = false, synced = false, bucket_timed = false;
   double work[4] = {0, 0, 0, 0};       // residue steps, loop updates, recovery updates, operand bytes
@@ -127,6 +135,11 @@ struct mgcd_context {
   uint32_t stage_fail_cta = 0xFFFFFFFFu;                // test hook (mgcd_test_fail_staging)
   uint32_t force_nq = 0;                                // test hook (mgcd_test_force_moduli)
   bool trace = false;                                   // record per-CTA occupancy (mgcd_set_cta_trace)
+  // Moduli grown on demand in the K-slot kernels (mgcd_set_growth): batched pairs start with
+  // this fraction of the reference count (0: off) and grow by grow_permille thousandths of it
+  // at a time, up to the reference count.
+  float grow_start = 0.4f;
+  uint32_t grow_permille = 50;
 };
 
 namespace mgcd {

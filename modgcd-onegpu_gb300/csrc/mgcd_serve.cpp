@@ -323,7 +323,7 @@ bool lane_publish(mgcd_server* S, StreamLane& L, Request* r)
   d.out_off = slot * (L.nq_cap + 1);
   d.g_off = 0;
   d.g_cap = 0;
-  d.pad_ = 0;
+  d.nq_cap = 0;
   L.ring_h->desc[slot] = d;
   L.ring_h->done[slot] = 0u;
   r->seq = L.tail;

@@ -359,3 +359,215 @@ long orc_mixed_radix_to_limbs(const orc_pair_t *d, size_t n, uint32_t *out, size
   }
   return (long)len;
 }
+
+/* ------------------------------------------------ moduli grown on demand (batches) ---- */
+
+/*  The reduction loop with moduli grown on demand, as this project's batched K-slot kernel
+    runs it (a policy of this project; the reference's count is fixed per call,
+    GmpCudaDevice-gcd.cu:49-55).  The steps of the loop and of the recovery are the
+    reference's (orc_modgcd above); what differs:
+
+      - the pair starts with the first nq0 moduli and may take the next ones, up to nq_cap,
+        step = ceil(nq_cap * step_permille / 1000) rounded up to a multiple of 32 (>= 32)
+        at a time;
+      - when a pivot's bookkeeping finds the loop out of moduli (the reference's check,
+        GmpCudaDevice-getGcdKernel.cu:393-399), or fewer than GROW_LOW surviving moduli,
+        and nq < nq_cap, the set grows before that pivot is applied; out of moduli with
+        nq = nq_cap, the run fails with ORC_ERR_REDUX;
+      - when the loop ends (every value infinite) with a result the surviving moduli less
+        one cannot certify (their product, each modulus counted as 2^(L-1), must exceed
+        2|u| and |v| by the size bounds below; the one to spare lets the recovery reach its
+        all-zero round), the set grows and the next pivot is chosen over it; a result the
+        survivors cannot certify at nq = nq_cap is ORC_ERR_UNCERTIFIED (the host reruns
+        such a pair with the reference's count, orc_modgcd);
+      - a modulus that joins takes the exact residues (u_i, v_i) mod q of the current pair:
+        the operands' residues with every applied pivot replayed, (u, v) <- (v, (u - b v)/p).
+
+    Size bounds (the kernel's certification): lu >= log2|u_i|, lv >= log2|v_i| in fixed point
+    with 24 fraction bits, from the operands' bit lengths, stepped per pivot by
+    |v'| <= (|u| + |b||v|)/p with log2f/exp2f rounded outward by 2^-17 bits.
+
+    *nq_final receives the moduli count at the end; other outputs as orc_modgcd's. */
+enum { ORC_ERR_UNCERTIFIED = 6 };
+#define GROW_LOW 64
+
+#define BOUND_FRAC 24
+#define BOUND_ONE (1ll << BOUND_FRAC)
+#define BOUND_SLACK (1ll << (BOUND_FRAC - 17))
+
+static long long bound_log2(float x) { return (long long)(log2f(x) * (float)BOUND_ONE); }
+
+static long long bound_init(const uint32_t *limbs, size_t len)
+{
+  return (long long)((long long)(len - 1) * 32 + (32 - __builtin_clz(limbs[len - 1]))) << BOUND_FRAC;
+}
+
+static void bound_step(long long *lu, long long *lv, uint32_t p, int32_t b)
+{
+  uint32_t ab = b < 0 ? 0u - (uint32_t)b : (uint32_t)b;
+  long long s = *lu;
+  if (ab != 0u) {
+    long long y = *lv + bound_log2((float)ab) + BOUND_SLACK;
+    long long m = y > *lu ? y : *lu, d = y > *lu ? y - *lu : *lu - y;
+    s = m + BOUND_SLACK;
+    if (d < 40 * BOUND_ONE) s += bound_log2(1.0f + exp2f(-(float)d * (1.0f / (float)BOUND_ONE)));
+  }
+  *lu = *lv;
+  *lv = s - bound_log2((float)p) + BOUND_SLACK;
+}
+
+static int bound_certified(long remaining, int L, long long lu, long long lv)
+{
+  long long cap = (long long)remaining * (L - 1) * BOUND_ONE;
+  return cap > lu + 2 * BOUND_ONE && cap > lv + BOUND_ONE;
+}
+
+static uint32_t grow_step(size_t cap, unsigned permille)
+{
+  uint64_t n = ((uint64_t)cap * permille + 999) / 1000;
+  return n < 32 ? 32u : (uint32_t)((n + 31) & ~(uint64_t)31);
+}
+
+int orc_modgcd_grow(const uint32_t *u, size_t uSz, const uint32_t *v, size_t vSz, int L,
+                    const uint32_t *moduli, size_t nq0, size_t nq_cap, unsigned step_permille,
+                    orc_pair_t *digits, size_t digits_cap, size_t *ndigits,
+                    orc_pair_t *trace, size_t trace_cap, size_t *ntrace, size_t *iters, size_t *nq_final)
+{
+  if (!moduli || nq0 == 0 || nq_cap < nq0 || !digits || !ndigits) return ORC_ERR_ARG;
+  uint32_t *uq = malloc(nq_cap * 4), *vq = malloc(nq_cap * 4);
+  int32_t *val = malloc(nq_cap * 4);
+  char *active = malloc(nq_cap);
+  orc_pair_t *hist = malloc(sizeof(orc_pair_t) * (nq_cap + 1));
+  if (!uq || !vq || !val || !active || !hist) {
+    free(uq); free(vq); free(val); free(active); free(hist);
+    return ORC_ERR_NOMEM;
+  }
+  int status = ORC_OK;
+  size_t nq = nq0, nt = 0, nd = 0, it = 0;
+  long remaining = (long)nq;
+  long ubits = (long)(uSz + 1) * 32, vbits = (long)(vSz + 1) * 32;
+  long long lu = bound_init(u, uSz), lv = bound_init(v, vSz);
+
+  /* residues of moduli [from, to), with the first nrep pivots of hist applied */
+#define JOIN(from, to, nrep)                                                              \
+  do {                                                                                  \
+    for (size_t j = (from); j < (to); j++) {                                            \
+      uint32_t q = moduli[j];                                                           \
+      uint32_t a = orc_residue(u, uSz, q), c = orc_residue(v, vSz, q);                  \
+      for (size_t h = 0; h < (nrep); h++) {                                             \
+        uint32_t p = hist[h].modulus;                                                   \
+        if (p > q) p -= q;                                                              \
+        uint32_t t = mulmod(submod(a, mulmod(from_signed(hist[h].value, q), c, q), q), invmod(p, q), q); \
+        a = c; c = t;                                                                   \
+      }                                                                                 \
+      uq[j] = a; vq[j] = c; active[j] = 1;                                              \
+      val[j] = (c == 0) ? ORC_MOD_INFINITY : to_signed(mulmod(a, invmod(c, q), q), q);  \
+    }                                                                                   \
+  } while (0)
+#define COLLECT_MIN(pairvar)                                                              \
+  do {                                                                                  \
+    uint64_t best = UINT64_MAX;                                                         \
+    for (size_t j = 0; j < nq; j++) {                                                   \
+      uint64_t k = min_key(val[j], moduli[j]);                                          \
+      if (k < best) best = k;                                                           \
+    }                                                                                   \
+    pairvar = key_pair(best);                                                           \
+  } while (0)
+
+  JOIN(0, nq, 0);
+  orc_pair_t pair;
+  COLLECT_MIN(pair);
+  for (;;) {
+    if (pair.value == ORC_MOD_INFINITY) {               /* the loop ended */
+      if (trace && nt < trace_cap) trace[nt] = pair;
+      nt++;
+      if (nq < nq_cap && !bound_certified(remaining - 1, L, lu, lv)) {
+        size_t n1 = nq + grow_step(nq_cap, step_permille);
+        if (n1 > nq_cap) n1 = nq_cap;
+        JOIN(nq, n1, it);
+        remaining += (long)(n1 - nq);
+        nq = n1;
+        COLLECT_MIN(pair);
+        continue;
+      }
+      break;
+    }
+    /* the pivot's bookkeeping (GmpCudaDevice-getGcdKernel.cu:389-399) */
+    if (trace && nt < trace_cap) trace[nt] = pair;
+    nt++;
+    hist[it] = pair;
+    remaining -= 1;
+    {
+      uint32_t absb = (pair.value < 0) ? 0u - (uint32_t)pair.value : (uint32_t)pair.value;
+      long tbits = ubits - (L - 1) + __builtin_ffs((int)absb);
+      ubits = vbits;
+      vbits = tbits;
+    }
+    if (remaining * (L - 2) <= ubits || (nq < nq_cap && remaining < GROW_LOW)) {
+      if (nq >= nq_cap) { status = ORC_ERR_REDUX; it++; goto done; }
+      size_t n1 = nq + grow_step(nq_cap, step_permille);
+      if (n1 > nq_cap) n1 = nq_cap;
+      JOIN(nq, n1, it);                                 /* before this pivot is applied */
+      remaining += (long)(n1 - nq);
+      nq = n1;
+    }
+    /* the update (GmpCudaDevice-getGcdKernel.cu:373-386) */
+    for (size_t j = 0; j < nq; j++) {
+      uint32_t q = moduli[j];
+      if (pair.modulus == q) { active[j] = 0; val[j] = ORC_MOD_INFINITY; }
+      if (active[j]) {
+        uint32_t p = pair.modulus;
+        if (p > q) p -= q;
+        uint32_t d = submod(uq[j], mulmod(from_signed(pair.value, q), vq[j], q), q);
+        uint32_t tq = mulmod(d, invmod(p, q), q);
+        val[j] = (tq == 0) ? ORC_MOD_INFINITY : to_signed(mulmod(vq[j], invmod(tq, q), q), q);
+        uq[j] = vq[j];
+        vq[j] = tq;
+      }
+    }
+    bound_step(&lu, &lv, pair.modulus, pair.value);
+    it++;
+    COLLECT_MIN(pair);
+  }
+  if (!bound_certified(remaining, L, lu, lv)) { status = ORC_ERR_UNCERTIFIED; goto done; }
+
+  /* MGCD4, as orc_modgcd */
+#define COLLECT_ANY(pairvar)                                                              \
+  do {                                                                                  \
+    size_t w = 0;                                                                       \
+    for (size_t j = 0; j < nq; j++) if (val[j] != 0) { w = j; break; }                  \
+    pairvar.modulus = moduli[w];                                                        \
+    pairvar.value = val[w];                                                             \
+  } while (0)
+  for (size_t j = 0; j < nq; j++) val[j] = active[j] ? to_signed(uq[j], moduli[j]) : 0;
+  COLLECT_ANY(pair);
+  do {
+    for (size_t j = 0; j < nq; j++) {
+      uint32_t q = moduli[j];
+      if (pair.modulus == q) { active[j] = 0; val[j] = 0; }
+      if (active[j]) {
+        uint32_t p = pair.modulus;
+        if (p > q) p -= q;
+        uq[j] = mulmod(submod(uq[j], from_signed(pair.value, q), q), invmod(p, q), q);
+        val[j] = to_signed(uq[j], q);
+      }
+    }
+    if (nd < digits_cap) digits[nd] = pair; else status = ORC_ERR_CAPACITY;
+    nd++;
+    remaining -= 1;
+    if (remaining <= 0) break;
+    COLLECT_ANY(pair);
+  } while (pair.value != 0);
+  if (status == ORC_OK && pair.value != 0) status = ORC_ERR_RECOVERY;
+
+done:
+  *ndigits = nd;
+  if (ntrace) *ntrace = nt;
+  if (iters) *iters = it;
+  if (nq_final) *nq_final = nq;
+  free(uq); free(vq); free(val); free(active); free(hist);
+  return status;
+#undef JOIN
+#undef COLLECT_MIN
+#undef COLLECT_ANY
+}

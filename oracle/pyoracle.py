@@ -52,6 +52,12 @@ def _load():
                                    ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t),
                                    ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t),
                                    ctypes.POINTER(ctypes.c_size_t)]
+        lib.orc_modgcd_grow.restype = ctypes.c_int
+        lib.orc_modgcd_grow.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int,
+                                        ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_uint,
+                                        ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t),
+                                        ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t),
+                                        ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]
         lib.orc_mixed_radix_to_limbs.restype = ctypes.c_long
         lib.orc_mixed_radix_to_limbs.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t]
         _lib = lib
@@ -127,6 +133,38 @@ def modgcd(u: int, v: int, L: int, moduli: np.ndarray, nq: int):
     digits = [(dig[i].modulus, dig[i].value) for i in range(min(nd.value, cap))]
     trace = [(tr[i].modulus, tr[i].value) for i in range(min(nt.value, nq + 2))]
     return st, digits, trace, it.value
+
+
+ORC_ERR_UNCERTIFIED = 6
+
+
+def grow_start_count(ref: int, start: float) -> int:
+    """A batched pair's first moduli count under growth (the plan's rounding: a multiple of
+    32, at least 64, at most the reference count)."""
+    n0 = (int(np.ceil(np.float32(start) * np.float32(ref))) + 31) // 32 * 32
+    return min(ref, max(64, n0))
+
+
+def grow_cap(ref: int) -> int:
+    """The moduli a batched pair may grow to: the reference count plus an eighth, rounded up
+    to 32, at most 16,384 (the K-slot kernels' limit)."""
+    return max(ref, min(16384, (ref + ref // 8 + 31) // 32 * 32))
+
+
+def modgcd_grow(u: int, v: int, L: int, moduli: np.ndarray, nq0: int, nq_cap: int, step_permille: int):
+    """The restated loop with moduli grown on demand (orc_modgcd_grow) on u >= v > 0.
+
+    Returns (status, digits, iters, nq_final)."""
+    ul, vl = to_limbs(u), to_limbs(v)
+    m = np.ascontiguousarray(moduli[:nq_cap], dtype=np.uint32)
+    cap = nq_cap + 2
+    dig = (Pair * cap)()
+    nd, nt, it, nf = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_size_t()
+    st = _load().orc_modgcd_grow(ul.ctypes.data, len(ul), vl.ctypes.data, len(vl), L, m.ctypes.data, nq0, nq_cap,
+                                 step_permille, dig, cap, ctypes.byref(nd), None, 0, ctypes.byref(nt),
+                                 ctypes.byref(it), ctypes.byref(nf))
+    digits = [(dig[i].modulus, dig[i].value) for i in range(min(nd.value, cap))]
+    return st, digits, it.value, nf.value
 
 
 def mixed_radix_to_int(digits) -> int:

@@ -107,6 +107,7 @@ def test_graph_replay_with_fewer_moduli_and_retries(mgcd):
         vs.append(v)
     exp = [math.gcd(u, v) for u, v in zip(us, vs)]
     with mgcd.Device(0, 32) as dev:
+        dev.set_growth(0)            # fixed counts: the rerun path
         dev.set_nq_scale(0.5)
         dev.batch_use_graph(True)
         dev.batch_upload(*mgcd.pack_pairs(us, vs))

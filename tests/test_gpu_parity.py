@@ -72,6 +72,7 @@ def test_batch_fewer_moduli_certified(mgcd, scale):
     wl = __import__("importlib").import_module("modgcd-onegpu_gb300.workloads")
     us, vs, _ = wl.mixed_batch(200, seed=9, hi_bits=20000)
     with mgcd.Device(0, 32) as dev:
+        dev.set_growth(0)            # fixed counts: the rerun path
         dev.set_nq_scale(scale)
         res = dev.gcd_batch(us, vs)
         retried = dev.batch_retried()

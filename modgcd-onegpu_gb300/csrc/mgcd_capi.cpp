@@ -8,7 +8,8 @@
 //             :49-55) and reject pairs that need more moduli than the table holds (:76-78);
 //             pairs with a zero operand are answered on the host (gcd(x, 0) = x);
 //             group the rest by size into size-class buckets, largest first; copy the batch.
-//   run       one persistent kernel per bucket, each on its own stream so buckets overlap;
+//   run       one persistent kernel per bucket, chained on one stream by programmatic
+//             dependent launches so that the buckets overlap, largest class placed first;
 //             single pairs too large for one CTA run on a cluster or a cooperative grid.
 //   download  copy digits back and convert each pair's digits to binary.
 #include <cuda_runtime.h>
@@ -80,13 +81,7 @@ void HostBuf::release()
 
 cudaError_t Plan::create(int priority)
 {
-  if (cudaStreamCreateWithPriority(&stream, cudaStreamNonBlocking, priority) != cudaSuccess) return cudaErrorUnknown;
-  for (int i = 0; i < NSTREAMS; ++i)
-    if (cudaStreamCreateWithPriority(&bstream[i], cudaStreamNonBlocking, priority) != cudaSuccess ||
-        cudaEventCreateWithFlags(&ev_b[i], cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreate(&t_b0[i]) != cudaSuccess || cudaEventCreate(&t_b1[i]) != cudaSuccess)
-      return cudaErrorUnknown;
-  if (cudaEventCreateWithFlags(&ev_start, cudaEventDisableTiming) != cudaSuccess ||
+  if (cudaStreamCreateWithPriority(&stream, cudaStreamNonBlocking, priority) != cudaSuccess ||
       cudaEventCreate(&t_run0) != cudaSuccess || cudaEventCreate(&t_run1) != cudaSuccess)
     return cudaErrorUnknown;
   return cudaSuccess;
@@ -104,23 +99,14 @@ void Plan::destroy(cudaMemPool_t)
   if (stream) cudaStreamSynchronize(stream);
   drop_graph();
   for (DevBuf* b : {&d_limbs, &d_pairs, &d_order, &d_digits, &d_count, &d_iters, &d_status, &d_queue, &d_scratch,
-                    &d_gsync, &d_retry, &d_glimbs, &d_glen, &d_nqf, &d_upd})
+                    &d_gsync, &d_retry, &d_glimbs, &d_glen, &d_nqf, &d_upd, &d_span})
     b->release(stream);
   if (stream) cudaStreamSynchronize(stream);
   for (HostBuf* b : {&h_count, &h_iters, &h_status, &h_digits, &h_glimbs, &h_glen, &h_nqf, &h_upd}) b->release();
-  for (int i = 0; i < NSTREAMS; ++i) {
-    if (bstream[i]) cudaStreamDestroy(bstream[i]);
-    if (ev_b[i]) cudaEventDestroy(ev_b[i]);
-    if (t_b0[i]) cudaEventDestroy(t_b0[i]);
-    if (t_b1[i]) cudaEventDestroy(t_b1[i]);
-    bstream[i] = nullptr;
-    ev_b[i] = t_b0[i] = t_b1[i] = nullptr;
-  }
   if (t_run0) cudaEventDestroy(t_run0);
   if (t_run1) cudaEventDestroy(t_run1);
-  if (ev_start) cudaEventDestroy(ev_start);
   if (stream) cudaStreamDestroy(stream);
-  t_run0 = t_run1 = ev_start = nullptr;
+  t_run0 = t_run1 = nullptr;
   stream = nullptr;
 }
 
@@ -128,7 +114,7 @@ size_t Plan::device_bytes() const
 {
   size_t s = 0;
   for (const DevBuf* b : {&d_limbs, &d_pairs, &d_order, &d_digits, &d_count, &d_iters, &d_status, &d_queue,
-                          &d_scratch, &d_gsync, &d_retry, &d_glimbs, &d_glen, &d_nqf, &d_upd})
+                          &d_scratch, &d_gsync, &d_retry, &d_glimbs, &d_glen, &d_nqf, &d_upd, &d_span})
     s += b->bytes;
   return s;
 }
@@ -417,6 +403,7 @@ int mgcd::plan_batch(mgcd_context* c, Plan& P, size_t np, const uint32_t* limbs,
   CK(P.d_iters.grow(std::max<size_t>(ng, 1) * sizeof(uint32_t), c->pool, s));
   CK(P.d_status.grow(std::max<size_t>(ng, 1) * sizeof(int32_t), c->pool, s));
   CK(P.d_nqf.grow(std::max<size_t>(ng, 1) * sizeof(uint32_t), c->pool, s));
+  CK(P.d_span.grow(2 * NSTREAMS * sizeof(unsigned long long), c->pool, s));
   CK(P.d_upd.grow(std::max<size_t>(ng, 1) * sizeof(unsigned long long), c->pool, s));
   CK(P.d_queue.grow(2 * NSTREAMS * sizeof(uint32_t), c->pool, s));
   CK(P.d_scratch.grow(std::max<size_t>(scratch, 1) * sizeof(uint32_t), c->pool, s));
@@ -584,12 +571,17 @@ static int launch_set(mgcd_context* c, Plan& P, const std::vector<Bucket>& bucke
     phases = P.d_phases.as<unsigned long long>();
     P.trace_cls.clear();
   }
-  CK(cudaEventRecord(P.ev_start, P.stream));
+  // every bucket kernel on P.stream, largest class first, each after the first a
+  // programmatic dependent of the one before (it starts once all CTAs of that one have
+  // started, cta_begin): the kernels run side by side, the larger classes' persistent CTAs
+  // placed first.  The span of each (earliest CTA start, latest CTA end) is its time.
+  if (time_buckets) CK(cudaMemsetAsync(P.d_span.p, 0xFF, 2 * NSTREAMS * sizeof(unsigned long long), P.stream));
   for (size_t b = 0; b < buckets.size(); ++b) {
     const Bucket& bk = buckets[b];
     BatchArgs a{};
     a.trace = trace;
     a.phases = phases;
+    a.span = time_buckets ? P.d_span.as<unsigned long long>() + 2 * b : nullptr;
     if (trace) {
       const int n = bk.grid * (bk.csize ? bk.csize : 1);
       trace += 4 * (size_t)n;
@@ -615,17 +607,12 @@ static int launch_set(mgcd_context* c, Plan& P, const std::vector<Bucket>& bucke
     a.grow_permille = c->grow_permille;
     a.nq_final = P.d_nqf.as<uint32_t>();
     a.updates = P.d_upd.as<unsigned long long>();
-    CK(cudaStreamWaitEvent(P.bstream[b], P.ev_start, 0));
-    if (time_buckets) CK(cudaEventRecord(P.t_b0[b], P.bstream[b]));
     if (bk.csize)
-      CK(launch_cluster_batch(a, bk.threads, bk.k, bk.csize, bk.grid, bk.smem, P.bstream[b]));
+      CK(launch_cluster_batch(a, bk.threads, bk.k, bk.csize, bk.grid, bk.smem, P.stream, b > 0));
     else
-      CK(launch_batch(a, bk.threads, bk.k, bk.grid, bk.smem, P.bstream[b]));
-    if (time_buckets) CK(cudaEventRecord(P.t_b1[b], P.bstream[b]));
-    CK(cudaEventRecord(P.ev_b[b], P.bstream[b]));
+      CK(launch_batch(a, bk.threads, bk.k, bk.grid, bk.smem, P.stream, b > 0));
     ++P.launches;
   }
-  for (size_t b = 0; b < buckets.size(); ++b) CK(cudaStreamWaitEvent(P.stream, P.ev_b[b], 0));
 
   for (uint32_t k : grid_pairs) {
     const PairDesc& d = descs[k];
@@ -734,8 +721,8 @@ int mgcd::run_plan(mgcd_context* c, Plan& P)
   for (size_t k = 0; k < ng; ++k) P.eff_nq[k] = P.descs[k].nq;
   if (c->use_graph && P.graphable && !P.plain) {
     if (!P.graph) {
-      // Record the run once (status reset, queue reset, every bucket kernel on its stream,
-      // joined back into P.stream); each later run is a single graph launch.
+      // Record the run once (status reset, queue reset, the chained bucket kernels, the
+      // conversion); each later run is a single graph launch.
       CK(cudaStreamBeginCapture(P.stream, cudaStreamCaptureModeThreadLocal));
       int rc = MGCD_OK;
       if (cudaMemsetAsync(P.d_status.p, 0xFF, ng * sizeof(int32_t), P.stream) != cudaSuccess ||
@@ -744,7 +731,7 @@ int mgcd::run_plan(mgcd_context* c, Plan& P)
         rc = MGCD_ERR_CUDA;
       if (rc == MGCD_OK)
         rc = launch_set(c, P, P.buckets, P.grid_pairs, P.descs, P.d_pairs.as<PairDesc>(), P.d_queue.as<uint32_t>(),
-                        false);
+                        true);
       if (rc == MGCD_OK) rc = launch_convert(c, P);
       cudaGraph_t g = nullptr;
       const cudaError_t e = cudaStreamEndCapture(P.stream, &g);
@@ -760,7 +747,7 @@ int mgcd::run_plan(mgcd_context* c, Plan& P)
     CK(cudaEventRecord(P.t_run0, P.stream));
     CK(cudaGraphLaunch(P.graph, P.stream));
     P.launches = P.graph_kernels;
-    P.bucket_timed = false;
+    P.bucket_timed = true;
   } else {
     CK(cudaEventRecord(P.t_run0, P.stream));
     CK(cudaMemsetAsync(P.d_status.p, 0xFF, ng * sizeof(int32_t), P.stream));
@@ -1189,13 +1176,26 @@ int mgcd_get_size_class(const mgcd_context* c, int cls, int* threads, int* k, fl
   return MGCD_OK;
 }
 
+// Bucket kernel i's time in the last run: its CTAs' earliest start to latest end (the span
+// the kernels record with the global timer).
+static int bucket_span_ms(const mgcd_context* c, int i, float* ms)
+{
+  unsigned long long sp[2] = {0, 0};
+  CK(cudaSetDevice(c->device));
+  CK(cudaMemcpy(sp, c->main.d_span.as<unsigned long long>() + 2 * i, sizeof sp, cudaMemcpyDeviceToHost));
+  const unsigned long long t0 = sp[0], t1 = ~sp[1];
+  *ms = (sp[0] != ~0ull && sp[1] != ~0ull && t1 >= t0) ? (float)((double)(t1 - t0) * 1e-6) : 0.f;
+  return MGCD_OK;
+}
+
 int mgcd_batch_kernel_stats(const mgcd_context* c, int i, int* cls, int* pairs, float* ms)
 {
   if (!c) return MGCD_ERR_INVALID_ARG;
   const Plan& P = c->main;
   if (!P.ran || !P.bucket_timed || i < 0 || i >= (int)P.buckets.size()) return MGCD_ERR_INVALID_ARG;
   float t = 0.f;
-  CK(cudaEventElapsedTime(&t, P.t_b0[i], P.t_b1[i]));
+  int rc = bucket_span_ms(c, i, &t);
+  if (rc != MGCD_OK) return rc;
   if (cls) *cls = P.buckets[i].cls;
   if (pairs) *pairs = (int)P.buckets[i].n;
   if (ms) *ms = t;
@@ -1228,7 +1228,8 @@ int mgcd_batch_elapsed_ms(const mgcd_context* c, float* run_ms, float* dominant_
     if (P.bucket_timed)
       for (size_t b = 0; b < P.buckets.size(); ++b) {
         float t = 0.f;
-        CK(cudaEventElapsedTime(&t, P.t_b0[b], P.t_b1[b]));
+        const int rc = bucket_span_ms(c, (int)b, &t);
+        if (rc != MGCD_OK) return rc;
         if (t > best) { best = t; bt = P.buckets[b].threads; }
       }
   }

@@ -93,6 +93,8 @@ struct BatchArgs {
                               // set-up, update, pivot choice and finish, reduction iterations, moduli
                               // rounds, pairs, cycles of certification and replay; over all threads:
                               // update rounds, rounds that needed an inverse, finite slot states (null: off)
+  unsigned long long* span;  // the kernel's earliest CTA start and ~(latest CTA end), globaltimer ns,
+                             // each lowered by atomicMin (null: off)
   uint32_t grow_permille;    // moduli added per growth step, thousandths of the pair's nq_cap
   uint32_t* nq_final;        // per pair: moduli in its set at the end (null: not recorded)
   unsigned long long* updates; // per pair: surviving moduli summed over its iterations (null: off)
@@ -144,7 +146,10 @@ struct GridArgs {
 // query) select the kernels with lazily reduced Montgomery products.
 size_t batch_smem_bytes(int threads, int k, uint32_t nq_max);
 cudaError_t batch_max_blocks_per_sm(int threads, int k, bool narrow, size_t smem, int* blocks);
-cudaError_t launch_batch(const BatchArgs& a, int threads, int k, int grid, size_t smem, cudaStream_t s);
+// after: a programmatic dependent launch -- the kernel may start once every CTA of the
+// stream's previous kernel has started (the batch kernels trigger at their start).
+cudaError_t launch_batch(const BatchArgs& a, int threads, int k, int grid, size_t smem, cudaStream_t s,
+                         bool after = false);
 // The same K-slot kernel in ring mode (continuous serving, a.ring set): threads 512 or 1024,
 // k 2 or 4.
 cudaError_t launch_ring(const BatchArgs& a, int threads, int k, int grid, size_t smem, cudaStream_t s);
@@ -159,7 +164,7 @@ cudaError_t launch_cluster(const GridArgs& a, int threads, int ctas, size_t smem
 size_t cluster_batch_smem_bytes(int csize, uint32_t nq_max, int k);
 cudaError_t cluster_batch_max_clusters(int threads, int k, int csize, size_t smem, int* clusters);
 cudaError_t launch_cluster_batch(const BatchArgs& a, int threads, int k, int csize, int clusters, size_t smem,
-                                 cudaStream_t s);
+                                 cudaStream_t s, bool after = false);
 
 // One pair on a cooperative grid of `clusters` clusters of `csize` CTAs (hierarchical
 // exchange; a.sync is the global state, a.per_cta the moduli per CTA).

@@ -29,23 +29,38 @@
 
 namespace mgcd {
 
-// Occupancy trace of the persistent kernels (BatchArgs::trace): when and where each CTA
-// ran and how many pairs it took, for the step's SM-busy accounting.
-__device__ __forceinline__ void trace_begin(unsigned long long* t)
+// Start and end of every CTA of a batch kernel: the occupancy trace (BatchArgs::trace: when
+// and where each CTA ran and how many pairs it took), the kernel's span (BatchArgs::span:
+// the earliest start and, as its complement, the latest end, globaltimer ns) and the launch
+// of the batch's next bucket kernel.  The bucket kernels of a batch are launched largest
+// class first on one stream, each a programmatic dependent of the one before: it may start
+// once every CTA of that one has started (griddepcontrol.launch_dependents) and does not
+// wait for its results, so the kernels still run side by side, but every persistent CTA of
+// a larger class is placed before a smaller class's CTAs can fill the SMs.
+__device__ __forceinline__ void cta_begin(const BatchArgs& a)
 {
-  if (t && threadIdx.x == 0) {
-    uint32_t sm;
-    asm volatile("mov.u32 %0, %%smid;" : "=r"(sm));
-    t[4 * blockIdx.x] = globaltimer_ns();
-    t[4 * blockIdx.x + 2] = sm;
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  if (threadIdx.x == 0 && (a.trace || a.span)) {
+    const unsigned long long t = globaltimer_ns();
+    if (a.trace) {
+      uint32_t sm;
+      asm volatile("mov.u32 %0, %%smid;" : "=r"(sm));
+      a.trace[4 * blockIdx.x] = t;
+      a.trace[4 * blockIdx.x + 2] = sm;
+    }
+    if (a.span) atomicMin(a.span, t);
   }
 }
 
-__device__ __forceinline__ void trace_end(unsigned long long* t, uint32_t pairs)
+__device__ __forceinline__ void cta_end(const BatchArgs& a, uint32_t pairs)
 {
-  if (t && threadIdx.x == 0) {
-    t[4 * blockIdx.x + 1] = globaltimer_ns();
-    t[4 * blockIdx.x + 3] = pairs;
+  if (threadIdx.x == 0 && (a.trace || a.span)) {
+    const unsigned long long t = globaltimer_ns();
+    if (a.trace) {
+      a.trace[4 * blockIdx.x + 1] = t;
+      a.trace[4 * blockIdx.x + 3] = pairs;
+    }
+    if (a.span) atomicMin(a.span + 1, ~t);
   }
 }
 
@@ -108,7 +123,7 @@ __global__ void __launch_bounds__(T) batch_kernel(const BatchArgs a)
   uint32_t* u0 = scr;
   uint32_t* v0 = scr + a.nq_max;
   int2* hist = reinterpret_cast<int2*>(scr + 2 * (size_t)a.nq_max);
-  trace_begin(a.trace);
+  cta_begin(a);
   uint32_t taken = 0;
   for (;;) {
     if (threadIdx.x == 0) next = atomicAdd(a.queue, 1u);
@@ -123,7 +138,7 @@ __global__ void __launch_bounds__(T) batch_kernel(const BatchArgs a)
                        a.digits, a.count + pi, a.iters + pi, a.status + pi, a.inv);
     __syncthreads();
   }
-  trace_end(a.trace, taken);
+  cta_end(a, taken);
 }
 
 // ------------------------------------------------------- K pairs per CTA, lockstep ----
@@ -288,7 +303,7 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   uint32_t rparity = 0, repoch = 0;
   uint32_t valid = 0, active = 0, redux = 0;          // slots holding a pair / in the loop / ran out (uniform)
-  trace_begin(a.trace);
+  cta_begin(a);
   uint32_t taken = 0;
   auto hist_of = [&](int s) { return reinterpret_cast<int2*>(scr + (size_t)s * 4 * NQS + 2 * (size_t)NQS); };
   // phase accounting (a.phases): thread 0's clock in each phase; the phases end at barriers,
@@ -768,7 +783,7 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
     o[12] = phs[PH_GROW];
     o[13] = phs[PH_GROWS];
   }
-  trace_end(a.trace, taken);
+  cta_end(a, taken);
 }
 
 // ------------------------------------------- K pairs per thread-block cluster, lockstep ----
@@ -839,7 +854,7 @@ __global__ void __launch_bounds__(T) cluster_batchk_kernel(const BatchArgs a)
   int rem[K], ubits[K], vbits[K];
   uint32_t iters[K], p[K], kh[K], kl[K];
   int32_t b[K];
-  trace_begin(a.trace);
+  cta_begin(a);
   uint32_t taken = 0;
 
   cluster_sync_all();
@@ -997,7 +1012,7 @@ __global__ void __launch_bounds__(T) cluster_batchk_kernel(const BatchArgs a)
       if ((active >> s) & 1u) key_pair(kh[s], kl[s], p[s], b[s]);
   }
   cluster_sync_all();   // no CTA leaves while others may still address its shared memory
-  trace_end(a.trace, taken);
+  cta_end(a, taken);
 }
 
 // One pair over a cooperative grid of GRID_THREADS-thread CTAs; CTA c owns moduli
@@ -1101,7 +1116,7 @@ __global__ void __launch_bounds__(T) cluster_batch_kernel(const BatchArgs a)
   uint32_t* st = smem + STAGE_SMEM_WORDS;
   uint32_t* acc2 = st + per_max;
   uint32_t* scr = a.scratch + (size_t)(blockIdx.x / C) * a.scratch_words;
-  trace_begin(a.trace);
+  cta_begin(a);
   uint32_t taken = 0;
   cluster_sync_all();
   for (;;) {
@@ -1127,7 +1142,7 @@ __global__ void __launch_bounds__(T) cluster_batch_kernel(const BatchArgs a)
     cluster_sync_all();   // every CTA is done with `next` and with the pair's scratch
   }
   cluster_sync_all();     // no CTA leaves while others may still address its shared memory
-  trace_end(a.trace, taken);
+  cta_end(a, taken);
 }
 
 // Integer-pipe microbenchmark: eight independent IMAD chains per thread.
@@ -1279,14 +1294,24 @@ cudaError_t launch_ring(const BatchArgs& a, int threads, int k, int grid, size_t
   return cudaLaunchKernel(fn, dim3(grid), dim3(threads), args, smem, s);
 }
 
-cudaError_t launch_batch(const BatchArgs& a, int threads, int k, int grid, size_t smem, cudaStream_t s)
+cudaError_t launch_batch(const BatchArgs& a, int threads, int k, int grid, size_t smem, cudaStream_t s, bool after)
 {
   const void* fn = batch_fn_for(threads, k, a.L <= 30);
   if (!fn) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   void* args[] = {const_cast<BatchArgs*>(&a)};
-  return cudaLaunchKernel(fn, dim3(grid), dim3(threads), args, smem, s);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = after ? 1 : 0;
+  return cudaLaunchKernelExC(&cfg, fn, args);
 }
 
 static const void* cluster_fn(int threads)
@@ -1384,13 +1409,18 @@ cudaError_t launch_cluster(const GridArgs& a, int threads, int ctas, size_t smem
 }
 
 cudaError_t launch_cluster_batch(const BatchArgs& a, int threads, int k, int csize, int clusters, size_t smem,
-                                 cudaStream_t s)
+                                 cudaStream_t s, bool after)
 {
   const void* fn = cluster_batch_fn_k(threads, k);
   cudaError_t e = prepare_cluster_fn(fn, csize, smem);
   if (e != cudaSuccess) return e;
-  cudaLaunchAttribute attr[1];
-  const cudaLaunchConfig_t cfg = cluster_config(clusters * csize, threads, csize, smem, s, attr);
+  cudaLaunchAttribute attr[2];
+  cudaLaunchConfig_t cfg = cluster_config(clusters * csize, threads, csize, smem, s, attr);
+  if (after) {
+    attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[1].val.programmaticStreamSerializationAllowed = 1;
+    cfg.numAttrs = 2;
+  }
   void* args[] = {const_cast<BatchArgs*>(&a)};
   return cudaLaunchKernelExC(&cfg, fn, args);
 }

@@ -46,7 +46,7 @@ struct Bucket {
   size_t scratch_off;  // words
 };
 
-// Size classes of the batched path, one persistent kernel (and stream) each: pairs with at
+// Size classes of the batched path, one persistent kernel each: pairs with at
 // most 1,024 / 4,096 / 16,384 moduli run K per CTA (or K per small cluster, when the class
 // or a serving lane asks for one); larger pairs K per thread-block cluster.
 constexpr int NSTREAMS = MGCD_NUM_SIZE_CLASSES;
@@ -63,11 +63,8 @@ inline int size_class(uint32_t nq) { return nq <= 1024 ? 0 : nq <= 4096 ? 1 : nq
 inline uint32_t grow_cap(uint32_t ref) { return std::min<uint32_t>(CTA_MAX_NQ, (ref + ref / 8 + 31u) / 32u * 32u); }
 
 struct Plan {
-  cudaStream_t stream = nullptr;
-  cudaStream_t bstream[NSTREAMS] = {};
-  cudaEvent_t ev_start = nullptr, ev_b[NSTREAMS] = {};
-  // timing: the whole run on `stream`, and each bucket launch on its stream
-  cudaEvent_t t_run0 = nullptr, t_run1 = nullptr, t_b0[NSTREAMS] = {}, t_b1[NSTREAMS] = {};
+  cudaStream_t stream = nullptr;       // every launch of the plan
+  cudaEvent_t t_run0 = nullptr, t_run1 = nullptr;   // timing of the whole run
 
   size_t np = 0;                       // pairs in the plan
   std::vector<int32_t> status;         // per pair: MGCD_OK / error code / -1 = computed on the GPU
@@ -89,6 +86,7 @@ struct Plan {
 
   DevBuf d_limbs, d_pairs, d_order, d_digits, d_count, d_iters, d_status, d_queue, d_scratch, d_gsync, d_retry;
   DevBuf d_nqf, d_upd;                 // per pair (K-slot kernels): final moduli count, loop updates
+  DevBuf d_span;                       // per bucket kernel: earliest CTA start, ~(latest CTA end), ns
   DevBuf d_glimbs, d_glen;             // binary gcds converted on the device
   DevBuf d_trace;                      // per-CTA occupancy trace of the bucket kernels (4 words each)
   DevBuf d_phases;                     // per-CTA phase accounting of the K-slot kernels (8 words each)
@@ -105,7 +103,7 @@ struct Plan {
   cudaGraphExec_t graph = nullptr;
   int graph_kernels = 0;
 
-  cudaError_t create(int priority = 0);   // streams at this priority (lower = more urgent)
+  cudaError_t create(int priority = 0);   // the stream at this priority (lower = more urgent)
   void destroy(cudaMemPool_t pool);
   void drop_graph();
   size_t device_bytes() const;

@@ -111,13 +111,19 @@ def test_reference_testmodgcd_compiles_against_dropin(mgcd, tmp_path):
 
 def test_tuning_tables_width_choice_and_traffic_record(mgcd):
     """The committed tuning artifacts the benchmark reads: one table per modulus width in the
-    loader's format (class threads k nq_scale cluster_ctas, '#' comments), the width choice,
-    and an ncu traffic figure for every width the batched benchmark can run."""
+    loader's format (class threads k nq_scale cluster_ctas, an optional 'grow start permille'
+    line, '#' comments), the width choice, and an ncu traffic figure for every width the
+    batched benchmark can run."""
     import json
     tdir = os.path.join(os.path.dirname(mgcd.__file__), "tuning")
     for L in (22, 27, 32):
         rows = [ln.split() for ln in open(os.path.join(tdir, "gb300_L%d.txt" % L))
                 if ln.strip() and not ln.lstrip().startswith("#")]
+        grow = [r for r in rows if r[0] == "grow"]
+        rows = [r for r in rows if r[0] != "grow"]
+        assert len(grow) <= 1
+        for _, start, permille in grow:
+            assert 0.1 <= float(start) <= 1.0 and 10 <= int(permille) <= 500
         assert sorted(int(r[0]) for r in rows) == [0, 1, 2, 3]
         for cls, threads, k, scale, cs in rows:
             assert int(threads) in (256, 512, 1024) and int(k) in (1, 2, 4, 8)

@@ -81,3 +81,8 @@ def test_growth_settings_validated(mgcd, tmp_path):
         assert dev.growth()[0] == 0
         dev.load_tuning(path)
         assert dev.growth() == (pytest.approx(0.4), 80)
+        bad = tmp_path / "bad.txt"
+        bad.write_text("0 256 4 1.0 0\ngrow 0.05 50\n")
+        with pytest.raises(mgcd.GcdError):
+            dev.load_tuning(str(bad))
+        assert dev.growth() == (pytest.approx(0.4), 80)       # nothing applied

@@ -172,8 +172,9 @@ def occupancy(rec, sms):
     of its CTAs' intervals, over the span from the first CTA start to the last CTA end; per
     size class the CTAs, their start and end spread, the longest CTA and, for the K-slot
     CTAs, where thread 0's clock went (set-up, update, pivot step incl. the wait for the
-    slowest warp, finish, layout: re-sorting the positions by live slots; finish_replay: the
-    certification and replay part of finish)."""
+    slowest warp, finish, layout: re-sorting the positions by live slots; grow: moduli added
+    to a pair's set, residues and history replay; finish_replay: the certification and
+    replay part of finish) and the growth steps per pair."""
     rec = rec[rec["ran"] != 0]
     if not len(rec):
         return None
@@ -198,11 +199,12 @@ def occupancy(rec, sms):
                            "start_ms_max": float(r["t_start_ms"].max()), "end_ms_min": float(r["t_end_ms"].min()),
                            "end_ms_max": float(r["t_end_ms"].max()), "cta_ms_median": float(statistics.median(d)),
                            "cta_ms_max": float(d.max())}
-        cyc = {k: float(r["cycles_" + k].sum()) for k in ("setup", "update", "pivot", "finish", "layout")}
+        cyc = {k: float(r["cycles_" + k].sum()) for k in ("setup", "update", "pivot", "finish", "layout", "grow")}
         tot = sum(cyc.values())
         if tot > 0:
             classes[str(c)]["phases"] = {k: v / tot for k, v in cyc.items()}
             classes[str(c)]["phases"]["finish_replay"] = float(r["cycles_replay"].sum()) / tot
+            classes[str(c)]["grow_steps_per_pair"] = float(r["grow_steps"].sum()) / max(1.0, float(r["pairs"].sum()))
             classes[str(c)]["iterations"] = int(r["iterations"].sum())
             classes[str(c)]["cycles_per_round"] = cyc["update"] / max(1.0, float(r["rounds"].sum()))
             classes[str(c)]["pivot_cycles_per_iteration"] = cyc["pivot"] / max(1.0, float(r["iterations"].sum()))

@@ -237,8 +237,12 @@ int lane_init(mgcd_server* S, StreamLane& L, int l, int priority)
 {
   mgcd_context* c = S->c;
   L.lane = l;
-  L.threads = c->cfg[l].threads >= 512 ? c->cfg[l].threads : 512;
-  L.k = c->cfg[l].k >= 4 ? 4 : 2;
+  // 1,024-thread CTAs with K = 4 slots, whatever the batch table says: a lane's CTAs are
+  // capped (STREAM_MAX_CTAS) and share the GPU with the other lanes, so its concurrency is
+  // its CTAs x K; the batch table's two-per-SM 512 x 2 shape for class 1 halved it (the
+  // saturation replay served 21.1k instead of 25.0k GCDs/s)
+  L.threads = 1024;
+  L.k = 4;
   L.nq_cap = STREAM_NQ_CAP[l];
   while (L.k > 2 && batch_smem_bytes(L.threads, L.k, L.nq_cap) > c->smem_optin - 16384) L.k /= 2;
   L.smem = batch_smem_bytes(L.threads, L.k, L.nq_cap);

@@ -282,7 +282,9 @@ __device__ __forceinline__ void warp_min_key(uint32_t& hi, uint32_t& lo)
 //   t' = p / (t - b)  (mod q)   since t' = u'/v' = v / ((u - b v)/p)
 // with t = INF -> 0 (v was 0: u' = 0, v' = u/p), t == b -> INF (v' = 0), degenerate and
 // retired states fixed; the pivot's own modulus retires.
-__device__ __forceinline__ uint32_t t_update(uint32_t t, uint32_t q, uint32_t qinv, uint32_t p, int32_t b)
+// narrow: q < 2^30 (the shorter inverse, inv_mod_narrow).
+__device__ __forceinline__ uint32_t t_update(uint32_t t, uint32_t q, uint32_t qinv, uint32_t p, int32_t b,
+                                             bool narrow)
 {
   if (t >= T_MARK) return (t == T_INF) ? 0u : t;
   if (q == p) return T_RETIRED;
@@ -290,7 +292,8 @@ __device__ __forceinline__ uint32_t t_update(uint32_t t, uint32_t q, uint32_t qi
   const uint32_t d = mod_sub(t, from_signed(b, q), q);
   if (d == 0u) return T_INF;
   // redc(d) = d/R, inv = R/d, mont_mul(pm, R/d) = pm/d
-  return mont_mul(pm, inv_mod(redc((uint64_t)d, q, qinv), q, qinv), q, qinv);
+  const uint32_t x = redc((uint64_t)d, q, qinv);
+  return mont_mul(pm, narrow ? inv_mod_narrow(x, q, qinv) : inv_mod(x, q, qinv), q, qinv);
 }
 
 // The same update for K pairs that share the modulus q (slot s uses pivot (p[s], b[s]);

@@ -479,16 +479,18 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
 #pragma unroll 4
         for (uint32_t e = 0; e < n; ++e) {
           const int2 h = hb[e];
-          const uint32_t pp = (uint32_t)h.x;
-          const uint32_t pm = pp > q ? pp - q : pp;
-          const uint32_t bn = from_signed(-h.y, q);   // -b mod q
-          if constexpr (NARROW) {                    // lazily in [0, 2q), as the final replay
+          if constexpr (NARROW) {                    // lazily in [0, 2q), as the final replay:
+            const uint32_t pm = (uint32_t)h.x;       // p < 2^L <= 2q as it is, and q - b in
+            const uint32_t bn = q - (uint32_t)h.y;   // (0, 2q) since |b| <= p/2 < q
             const uint64_t T2 = (uint64_t)bn * V + U;
             const uint32_t U2 = mont_mul_lazy(V, pm, q, qi);
             const uint32_t lo = (uint32_t)T2, hi = (uint32_t)(T2 >> 32);
             V = hi + __umulhi(lo * qi, q) + (lo != 0u);
             U = U2;
           } else {
+            const uint32_t pp = (uint32_t)h.x;
+            const uint32_t pm = pp > q ? pp - q : pp;
+            const uint32_t bn = from_signed(-h.y, q);   // -b mod q
             const uint32_t U2 = mont_mul(V, pm, q, qi);
             V = redc((uint64_t)bn * V + U, q, qi);
             U = U2;

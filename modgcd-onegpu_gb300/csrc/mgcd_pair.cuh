@@ -602,7 +602,7 @@ __device__ void run_pair(const uint32_t* __restrict__ limbs, const PairDesc& d, 
     kl = 0xFFFFFFFFu;
     for (uint32_t j = threadIdx.x; j < nloc; j += T) {
       const ModConst c = my[j];
-      const uint32_t t = t_update(st[j], c.q, c.qinv, p, b);
+      const uint32_t t = t_update(st[j], c.q, c.qinv, p, b, L <= 30);
       st[j] = t;
       uint32_t h, l;
       t_key(t, c.q, h, l);
@@ -882,10 +882,10 @@ __device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d
         if (narrow) {
 #pragma unroll 4
           for (uint32_t e = 0; e < n; ++e) {
+            // lazy operands: p < 2^L <= 2q as it is, and |b| <= p/2 < q puts q - b in (0, 2q)
             const int2 h = hb[e];
-            const uint32_t pp = (uint32_t)h.x;
-            const uint32_t pm = pp > q ? pp - q : pp;
-            const uint32_t bn = from_signed(-h.y, q);
+            const uint32_t pm = (uint32_t)h.x;
+            const uint32_t bn = q - (uint32_t)h.y;
             const uint64_t T2 = (uint64_t)bn * V + U;
             const uint32_t U2 = mont_mul_lazy(V, pm, q, qi);
             const uint32_t lo = (uint32_t)T2, hi = (uint32_t)(T2 >> 32);

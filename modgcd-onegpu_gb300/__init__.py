@@ -300,12 +300,17 @@ class Device:
             raise GcdError(int(st[bad[0]]), status_string(int(st[bad[0]])))
         return res
 
-    def gcd_batch_packed(self, limbs, u_off, u_len, v_off, v_len):
+    def gcd_batch_packed(self, limbs, u_off, u_len, v_off, v_len, out=None):
+        """mgcd_gcd_batch on packed pairs; `out` = (g, g_off, g_cap, g_len, status) arrays to
+        reuse (sized by result_layout), else new ones."""
         n = len(u_off)
-        g_off, g_cap, tot = result_layout(u_len, v_len)
-        g = np.zeros(max(tot, 1), dtype=np.uint32)
-        g_len = np.zeros(n, dtype=np.uint32)
-        st = np.zeros(n, dtype=np.int32)
+        if out is None:
+            g_off, g_cap, tot = result_layout(u_len, v_len)
+            g = np.zeros(max(tot, 1), dtype=np.uint32)
+            g_len = np.zeros(n, dtype=np.uint32)
+            st = np.zeros(n, dtype=np.int32)
+        else:
+            g, g_off, g_cap, g_len, st = out
         self._lib.mgcd_gcd_batch(self._h, n, _ptr(limbs), _ptr(u_off), _ptr(u_len), _ptr(v_off), _ptr(v_len),
                                  g.ctypes.data, _ptr(g_off), _ptr(g_cap), _ptr(g_len), _ptr(st))
         return g, g_off, g_len, st

@@ -117,3 +117,38 @@ def test_gmp_batch_baseline(oracle):
     secs, g, goff, glen = oracle.cpu_gmp_gcd_batch(np.concatenate(parts), uo, ul, vo, vl, 2)
     for i, (u, v) in enumerate(zip(us, vs)):
         assert oracle.from_limbs(g[int(goff[i]): int(goff[i]) + int(glen[i])]) == math.gcd(u, v)
+
+
+def test_oracle_growth_restatement(oracle, golden):
+    """The oracle's restatement of the batches' moduli growth (orc_modgcd_grow): without room
+    to grow it is the reference loop (same digits as orc_modgcd at the same count); with
+    growth every result is the exact gcd, sets stay within their caps, and the set grows."""
+    for L in (32, 27):
+        mods = oracle.gen_moduli(L, 20000)
+        grown = 0
+        pairs = []
+        for case in golden["cases"]:
+            if case["bits"] <= 20000:
+                pairs += golden_pairs(case)[:3]
+        rng = random.Random(L)
+        for _ in range(6):
+            a = rng.getrandbits(rng.randint(200, 9000)) | 1
+            pairs.append((a * (rng.getrandbits(64) | 1), a))                    # v | u
+            pairs.append((rng.getrandbits(5000) | 1, rng.getrandbits(4000) | 1))  # near-coprime
+        pairs.append((12345678901234567890123, 12345678901234567890123))       # u = v
+        for u, v in pairs:
+            uu, vv = (u, v) if u >= v else (v, u)
+            ref = oracle.num_moduli_needed(uu.bit_length(), L)
+            st, dig, _, nf = oracle.modgcd_grow(uu, vv, L, mods, ref, ref, 50)
+            st0, dig0, _, _ = oracle.modgcd(uu, vv, L, mods, ref)
+            if st == 0 and st0 == 0:
+                assert dig == dig0 and nf == ref
+            cap = oracle.grow_cap(ref)
+            for start, permille in ((0.4, 50), (0.2, 20)):
+                n0 = oracle.grow_start_count(ref, start)
+                st, dig, _, nf = oracle.modgcd_grow(uu, vv, L, mods, n0, cap, permille)
+                assert st == 0, (L, uu.bit_length(), st)
+                assert oracle.mixed_radix_to_int(dig) == math.gcd(u, v)
+                assert n0 <= nf <= cap
+                grown += nf > n0
+        assert grown > 0

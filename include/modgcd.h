@@ -132,7 +132,7 @@ int mgcd_set_nq_scale(mgcd_context *ctx, float scale);
    reference's check, GmpCudaDevice-getGcdKernel.cu:393-399), has fewer than 64 surviving
    moduli, or ends with a result that the surviving moduli less one cannot certify, takes
    the next step_permille / 1000 of its cap from the table, up to the cap (the reference's
-   count plus an eighth, rounded up to 32, at most 16,384).  A new modulus joins in the
+   count plus a sixteenth, rounded up to 32, at most 16,384).  A new modulus joins in the
    state it would have had from the start (residues of the operands, then the pivots so far
    replayed on it), so the result is the pair's gcd as before; the pivots after a growth may
    differ from a run with the larger set from the start.  A pair that still fails is rerun

@@ -146,9 +146,9 @@ def grow_start_count(ref: int, start: float) -> int:
 
 
 def grow_cap(ref: int) -> int:
-    """The moduli a batched pair may grow to: the reference count plus an eighth, rounded up
-    to 32, at most 16,384 (the K-slot kernels' limit)."""
-    return max(ref, min(16384, (ref + ref // 8 + 31) // 32 * 32))
+    """The moduli a batched pair may grow to: the reference count plus a sixteenth, rounded
+    up to 32, at most 16,384 (the K-slot kernels' limit)."""
+    return max(ref, min(16384, (ref + ref // 16 + 31) // 32 * 32))
 
 
 def modgcd_grow(u: int, v: int, L: int, moduli: np.ndarray, nq0: int, nq_cap: int, step_permille: int):

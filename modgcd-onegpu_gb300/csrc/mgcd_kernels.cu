@@ -223,6 +223,9 @@ constexpr uint32_t RELAYOUT_EVERY = MGCD_RELAYOUT_EVERY;
 // A pair that may grow its moduli set grows whenever fewer than GROW_LOW of its moduli
 // survive: near the end of a set each iteration reduces the operands by only about
 // log2(survivors) bits, so a set run down to a handful costs iterations that do little.
+#ifndef MGCD_PREFETCH_MAX_K
+#define MGCD_PREFETCH_MAX_K 2
+#endif
 #ifndef MGCD_GROW_LOW
 #define MGCD_GROW_LOW 64
 #endif
@@ -714,7 +717,21 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
     // size bounds for this update's pivots (log2f/exp2f on one lane per slot): the last warp
     // has the fewest moduli rounds whenever npos is not a multiple of T
     if (w == NW - 1 && lane < K && ((active >> lane) & 1u)) bound_step(ss.lu[lane], ss.lv[lane], ss.p[lane], ss.b[lane]);
+    // with K <= MGCD_PREFETCH_MAX_K, each position's constants are loaded one round ahead (a
+    // global load from a table that the shared memory leaves little L1 for: its latency
+    // overlaps a round's update); the K = 4 loop has no registers to spare for them (mixed
+    // batch: none 72.6 ms, K <= 2 72.1, every K 75.6: the K = 4 loop's spills double)
+    constexpr bool PREFETCH = K <= MGCD_PREFETCH_MAX_K;
+    ModConst cn{};
+    if constexpr (PREFETCH) cn = a.mods[pmod[threadIdx.x < npos ? threadIdx.x : 0u]];
     for (uint32_t j = threadIdx.x; j < npos; j += T) {
+      ModConst c;
+      if constexpr (PREFETCH) {
+        c = cn;
+        if (j + T < npos) cn = a.mods[pmod[j + T]];
+      } else {
+        c = a.mods[pmod[j]];
+      }
       uint32_t m = 0, tv[K];
 #pragma unroll
       for (int s = 0; s < K; ++s) {                   // (states beyond a pair's moduli are retired)
@@ -730,7 +747,6 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
         lv_fin += fin;
       }
       if (!m) continue;
-      const ModConst c = a.mods[pmod[j]];
       if constexpr (NARROW) t_update_k_narrow<K>(tv, c, p, b, m);
       else t_update_k<K>(tv, c, p, b, m);
 #pragma unroll

@@ -858,6 +858,7 @@ __device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d
   // whole CTA stages into shared memory (hbuf), so every step reads a broadcast from shared
   // memory instead of waiting on a global load.
   const bool narrow = L <= 30;
+  uint32_t ns;                                         // survivors, listed in ibuf
   {
     __shared__ uint32_t nsurv;
     if (threadIdx.x == 0) nsurv = 0u;
@@ -865,7 +866,7 @@ __device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d
     for (uint32_t j = threadIdx.x; j < nloc; j += T)
       if (st[j] != T_RETIRED) ibuf[atomicAdd(&nsurv, 1u)] = j;
     __syncthreads();
-    const uint32_t ns = nsurv;
+    ns = nsurv;
     int2* const hb = reinterpret_cast<int2*>(hbuf);
     for (uint32_t base = 0; base < ns; base += T) {
       const bool have = base + threadIdx.x < ns;
@@ -930,12 +931,13 @@ __device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d
     return;
   }
 
-  // ---- MGCD4: recovery (GmpCudaDevice-getGcdKernel.cu:404-443)
+  // ---- MGCD4: recovery (GmpCudaDevice-getGcdKernel.cu:404-443), over the survivors listed
+  // in ibuf (in no particular order: each thread keeps the lowest index among its own)
   kh = 0xFFFFFFFFu;
   kl = 0u;
-  for (uint32_t j = threadIdx.x; j < nloc; j += T) {
-    const uint32_t u = st[j];
-    if (u != U_RETIRED && u != 0u) { kh = j0 + j; kl = (uint32_t)to_signed(u, my[j].q); break; }
+  for (uint32_t i = threadIdx.x; i < ns; i += T) {
+    const uint32_t j = ibuf[i], u = st[j];
+    if (u != 0u && j0 + j < kh) { kh = j0 + j; kl = (uint32_t)to_signed(u, my[j].q); }
   }
   if (!reduce_min<T, MODE>(kh, kl, rs, parity, gs, epoch)) {
     if (writer) *status = ST_TIMEOUT;
@@ -948,7 +950,8 @@ __device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d
   do {
     kh = 0xFFFFFFFFu;
     kl = 0u;
-    for (uint32_t j = threadIdx.x; j < nloc; j += T) {
+    for (uint32_t i = threadIdx.x; i < ns; i += T) {
+      const uint32_t j = ibuf[i];
       uint32_t u = st[j];
       if (u == U_RETIRED) continue;
       const ModConst c = my[j];
@@ -960,7 +963,7 @@ __device__ void finish_pair(const ModConst* __restrict__ mods, const PairDesc& d
                                 : inv_mod(redc((uint64_t)(p > q ? p - q : p), q, qi), q, qi);
       u = mont_mul(mod_sub(u, from_signed(g, q), q), dinv, q, qi);
       st[j] = u;
-      if (u != 0u && kh == 0xFFFFFFFFu) { kh = j0 + j; kl = (uint32_t)to_signed(u, q); }
+      if (u != 0u && jj < kh) { kh = jj; kl = (uint32_t)to_signed(u, q); }
     }
     if (writer) digits[d.out_off + ndig] = mgcd_pair{p, g};
     ++ndig;

@@ -532,12 +532,15 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
   // Counting sort of the positions by live set (full sets first, the empty set last);
   // warp-aggregated shared-memory atomics give the ranks.  Every thread calls it.
   auto relayout = [&]() {
+    // without a fresh slot only [0, npos) needs sorting: positions past it are dead in every
+    // active slot, and dead states stay dead (a slot becomes active again only as a fresh one)
+    const uint32_t lim = fresh ? NQS : npos;
     if (threadIdx.x < (1u << K)) bucket[threadIdx.x] = 0u;
     __syncthreads();
     const uint32_t below = (1u << lane) - 1u;
-    for (uint32_t base = 0; base < NQS; base += T) {
+    for (uint32_t base = 0; base < lim; base += T) {
       const uint32_t pos = base + threadIdx.x;
-      const bool in = pos < NQS;
+      const bool in = pos < lim;
       uint32_t set = 0xFFFFu;
       if (in) {
         const uint32_t m = pmod[pos];
@@ -561,9 +564,9 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
       bucket[0] = off;
     }
     __syncthreads();
-    for (uint32_t base = 0; base < NQS; base += T) {
+    for (uint32_t base = 0; base < lim; base += T) {
       const uint32_t pos = base + threadIdx.x;
-      const bool in = pos < NQS;
+      const bool in = pos < lim;
       const uint32_t set = in ? aux[pos] : 0xFFFFu;
       const uint32_t grp = __match_any_sync(0xFFFFFFFFu, set);
       const int lead = __ffs((int)grp) - 1;
@@ -576,15 +579,15 @@ __global__ void __launch_bounds__(T) batchk_kernel(const BatchArgs a)
 #pragma unroll 1
     for (int s = 0; s < K; ++s) {
       if (!((valid >> s) & 1u)) continue;
-      for (uint32_t pos = threadIdx.x; pos < NQS; pos += T) acc2[aux[pos]] = state_at(s, pos, pmod[pos]);
+      for (uint32_t pos = threadIdx.x; pos < lim; pos += T) acc2[aux[pos]] = state_at(s, pos, pmod[pos]);
       __syncthreads();
       uint32_t* ts = tS + (size_t)s * NQS;
-      for (uint32_t pos = threadIdx.x; pos < NQS; pos += T) ts[pos] = acc2[pos];
+      for (uint32_t pos = threadIdx.x; pos < lim; pos += T) ts[pos] = acc2[pos];
       __syncthreads();
     }
-    for (uint32_t pos = threadIdx.x; pos < NQS; pos += T) acc2[aux[pos]] = pmod[pos];
+    for (uint32_t pos = threadIdx.x; pos < lim; pos += T) acc2[aux[pos]] = pmod[pos];
     __syncthreads();
-    for (uint32_t pos = threadIdx.x; pos < NQS; pos += T) pmod[pos] = (uint16_t)acc2[pos];
+    for (uint32_t pos = threadIdx.x; pos < lim; pos += T) pmod[pos] = (uint16_t)acc2[pos];
     __syncthreads();
     npos = live_pos;
     fresh = 0u;

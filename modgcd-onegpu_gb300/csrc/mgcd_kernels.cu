@@ -220,12 +220,15 @@ constexpr int PH_WORDS_T0 = 11;         // words kept by thread 0
 #endif
 constexpr uint32_t RELAYOUT_EVERY = MGCD_RELAYOUT_EVERY;
 
-// A pair that may grow its moduli set grows whenever fewer than GROW_LOW of its moduli
-// survive: near the end of a set each iteration reduces the operands by only about
-// log2(survivors) bits, so a set run down to a handful costs iterations that do little.
+// Largest K whose update loop loads each position's modulus constants a round ahead
+// (batchk_kernel's update loop).
 #ifndef MGCD_PREFETCH_MAX_K
 #define MGCD_PREFETCH_MAX_K 2
 #endif
+
+// A pair that may grow its moduli set grows whenever fewer than GROW_LOW of its moduli
+// survive: near the end of a set each iteration reduces the operands by only about
+// log2(survivors) bits, so a set run down to a handful costs iterations that do little.
 #ifndef MGCD_GROW_LOW
 #define MGCD_GROW_LOW 64
 #endif
@@ -235,8 +238,9 @@ constexpr int GROW_LOW = MGCD_GROW_LOW;
 // per-iteration checks, GmpCudaDevice-getGcdKernel.cu:365-402): records (p, b) in the
 // history; returns 0 (continue), 1 (loop ended: b = INF), 3 (ran out of moduli) or 4 (ran
 // out, or fewer than GROW_LOW moduli survive, and the pair may grow its moduli set: grow
-// before the update that applies this pivot).  One thread per slot.  The certification bounds are stepped for this pivot during
-// the update that uses it, by the last warp (below), off the path between the two barriers.
+// before the update that applies this pivot).  One thread per slot.  The certification
+// bounds are stepped for this pivot during the update that uses it, by the last warp
+// (below), off the path between the two barriers.
 template <int K>
 __device__ __forceinline__ uint32_t slot_step(SlotState<K>& ss, int s, int2* hist, int L)
 {

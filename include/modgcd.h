@@ -99,7 +99,9 @@ int mgcd_gcd(mgcd_context *ctx, const uint32_t *u, size_t uSz, const uint32_t *v
    u_off[i]+u_len[i]) and v at limbs[v_off[i] .. +v_len[i]).  Results: g of pair i at
    g[g_off[i] ..] with capacity g_cap[i] limbs, length in g_len[i], per-pair status in
    status[i] (MGCD_OK or an error code).  The call returns MGCD_OK when every pair
-   succeeded, else the first failing pair's code. */
+   succeeded, else the first failing pair's code.  When the result slots are contiguous
+   (g_off[i+1] = g_off[i] + g_cap[i]), mgcd_gcd_batch writes them straight from the device:
+   the limbs of a slot past g_len[i] are then unspecified, as are a failed pair's. */
 int mgcd_gcd_batch(mgcd_context *ctx, size_t npairs, const uint32_t *limbs,
                    const uint64_t *u_off, const uint32_t *u_len,
                    const uint64_t *v_off, const uint32_t *v_len,

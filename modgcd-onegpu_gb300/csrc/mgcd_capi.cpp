@@ -313,7 +313,8 @@ static int schedule(mgcd_context* c, Plan& P, std::vector<PairDesc>& descs, cons
                     bool latency = false);
 
 int mgcd::plan_batch(mgcd_context* c, Plan& P, size_t np, const uint32_t* limbs, const uint64_t* u_off,
-                     const uint32_t* u_len, const uint64_t* v_off, const uint32_t* v_len, bool plain)
+                     const uint32_t* u_len, const uint64_t* v_off, const uint32_t* v_len, bool plain,
+                     const uint64_t* g_off, const uint32_t* g_cap)
 {
   if (!c || (np && (!limbs || !u_off || !u_len || !v_off || !v_len))) return MGCD_ERR_INVALID_ARG;
   CK(cudaSetDevice(c->device));
@@ -380,6 +381,29 @@ int mgcd::plan_batch(mgcd_context* c, Plan& P, size_t np, const uint32_t* limbs,
   }
   P.ndig = out_off;
   P.nglimbs = glimbs;
+  P.direct = false;
+  P.in_place = false;
+  P.direct_base = 0;
+  if (g_off && g_cap && np) {
+    // The caller's result slots in place of the compact layout when they are contiguous
+    // (g_off[i + 1] = g_off[i] + g_cap[i]) and not much larger than it: the device writes
+    // each gcd where the caller wants it and one copy brings back the whole span.  A slot
+    // smaller than the gcd is left to the host conversion, which reports it as before.
+    bool tiled = true;
+    for (size_t i = 0; i + 1 < np && tiled; ++i) tiled = g_off[i + 1] == g_off[i] + g_cap[i];
+    const uint64_t span = tiled ? g_off[np - 1] + g_cap[np - 1] - g_off[0] : 0;
+    if (tiled && span <= 2 * glimbs + 4096) {
+      P.direct = true;
+      P.direct_base = g_off[0];
+      P.nglimbs = span;
+      for (size_t i = 0; i < np; ++i) {
+        if (P.slot[i] < 0) continue;
+        PairDesc& d = P.descs[P.slot[i]];
+        d.g_off = g_off[i] - g_off[0];
+        d.g_cap = std::min(d.v_len, g_cap[i]);
+      }
+    }
+  }
   const size_t ng = P.descs.size();
   P.order.clear();
   std::vector<uint32_t> all(ng);
@@ -841,7 +865,7 @@ int mgcd::sync_plan(mgcd_context* c, Plan& P)
 }
 
 // Copies the GPU results of the plan to pinned host memory.
-int mgcd::fetch(mgcd_context* c, Plan& P)
+int mgcd::fetch(mgcd_context* c, Plan& P, uint32_t* direct_g)
 {
   const size_t ng = P.descs.size();
   CK(cudaSetDevice(c->device));
@@ -850,7 +874,8 @@ int mgcd::fetch(mgcd_context* c, Plan& P)
   CK(P.h_iters.grow(ng * sizeof(uint32_t)));
   CK(P.h_status.grow(ng * sizeof(int32_t)));
   CK(P.h_glen.grow(ng * sizeof(uint32_t)));
-  CK(P.h_glimbs.grow(std::max<size_t>(P.nglimbs, 1) * sizeof(uint32_t)));
+  P.in_place = P.direct && direct_g != nullptr;
+  if (!P.in_place) CK(P.h_glimbs.grow(std::max<size_t>(P.nglimbs, 1) * sizeof(uint32_t)));
   CK(P.h_nqf.grow(ng * sizeof(uint32_t)));
   CK(P.h_upd.grow(ng * sizeof(unsigned long long)));
   if (P.plain) CK(P.h_digits.grow(std::max<size_t>(P.ndig, 1) * sizeof(mgcd_pair)));
@@ -861,7 +886,8 @@ int mgcd::fetch(mgcd_context* c, Plan& P)
   CK(cudaMemcpyAsync(P.h_iters.p, P.d_iters.p, ng * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(P.h_status.p, P.d_status.p, ng * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(P.h_glen.p, P.d_glen.p, ng * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(P.h_glimbs.p, P.d_glimbs.p, P.nglimbs * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(P.in_place ? (void*)(direct_g + P.direct_base) : P.h_glimbs.p, P.d_glimbs.p,
+                     P.nglimbs * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(P.h_nqf.p, P.d_nqf.p, ng * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(P.h_upd.p, P.d_upd.p, ng * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
   uint64_t d2h = ng * (5 * sizeof(uint32_t) + sizeof(unsigned long long)) + P.nglimbs * sizeof(uint32_t);
@@ -949,7 +975,7 @@ int mgcd::convert_all(mgcd_context* c, Plan& P, uint32_t* g, const uint64_t* g_o
         } else if (gl[k] != RADIX_HOST) {           // converted on the device
           len = gl[k];
           if (len > g_cap[i]) { s = MGCD_ERR_CAPACITY; len = 0; }
-          else if (len) std::memcpy(g + g_off[i], gv + P.descs[k].g_off, len * sizeof(uint32_t));
+          else if (len && !P.in_place) std::memcpy(g + g_off[i], gv + P.descs[k].g_off, len * sizeof(uint32_t));
         } else if (mixed_radix_to_limbs(dig + P.descs[k].out_off, cnt[k], g + g_off[i], g_cap[i], &len)) {
           s = MGCD_ERR_CAPACITY;
         }
@@ -971,7 +997,7 @@ int mgcd::convert_all(mgcd_context* c, Plan& P, uint32_t* g, const uint64_t* g_o
   for (size_t k = 0; k < P.descs.size(); ++k) {
     if (st[k] != ST_OK) continue;
     if (gl[k] == RADIX_HOST) host_radix = true;
-    else copy_bytes += (size_t)gl[k] * sizeof(uint32_t);
+    else if (!P.in_place) copy_bytes += (size_t)gl[k] * sizeof(uint32_t);
   }
   const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
   const size_t want = host_radix ? (np + 15) / 16 : 1 + copy_bytes / (32u << 20);
@@ -1431,13 +1457,20 @@ int mgcd_gcd_batch(mgcd_context* c, size_t np, const uint32_t* limbs, const uint
                    const uint32_t* u_len, const uint64_t* v_off, const uint32_t* v_len, uint32_t* g,
                    const uint64_t* g_off, const uint32_t* g_cap, uint32_t* g_len, int32_t* status)
 {
-  if (!c) return MGCD_ERR_INVALID_ARG;
+  if (!c || (np && (!g || !g_off || !g_cap || !g_len || !status))) return MGCD_ERR_INVALID_ARG;
   if (busy(c)) return MGCD_ERR_BUSY;
-  int rc = plan_batch(c, c->main, np, limbs, u_off, u_len, v_off, v_len, false);
+  Plan& P = c->main;
+  // results planned in the caller's layout where it allows: one device-to-host copy puts them
+  // in place, with no pass over them on the host
+  int rc = plan_batch(c, P, np, limbs, u_off, u_len, v_off, v_len, false, g_off, g_cap);
   if (rc != MGCD_OK) return rc;
-  rc = run_plan(c, c->main);
+  rc = run_plan(c, P);
   if (rc != MGCD_OK) return rc;
-  return mgcd_batch_download(c, g, g_off, g_cap, g_len, status);
+  rc = sync_plan(c, P);
+  if (rc != MGCD_OK) return rc;
+  rc = fetch(c, P, g);
+  if (rc != MGCD_OK) return rc;
+  return convert_all(c, P, g, g_off, g_cap, g_len, status, true);
 }
 
 // ------------------------------------------------------------------ single pair ----

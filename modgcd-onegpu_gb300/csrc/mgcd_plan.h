@@ -78,6 +78,10 @@ struct Plan {
   std::vector<uint32_t> ref_nq, eff_nq; // per GPU pair: reference count, count of the final run
   size_t ndig = 0, scratch_words = 0, grid_scratch_off = 0;
   size_t nglimbs = 0;                  // result limbs reserved (sum of g_cap)
+  // results planned in the caller's layout (mgcd_gcd_batch, slots contiguous): d_glimbs[x]
+  // is the caller's g[direct_base + x], copied there in one piece; in_place: fetch did so
+  bool direct = false, in_place = false;
+  uint64_t direct_base = 0;
   bool plain = false;                  // single-pair latency policy
   bool graphable = true;               // may be recorded into a CUDA graph (context setting)
   int cluster_ctas = 0;                // CTAs per cluster of size class 3 (0: the context's setting)
@@ -145,16 +149,20 @@ namespace mgcd {
 
 // Plan operations (mgcd_capi.cpp).  All return MGCD_* codes.
 //   plan_batch   validate, order and size the pairs on the host, copy the batch to the
-//                device on P.stream (asynchronous when `limbs` is pinned);
+//                device on P.stream (asynchronous when `limbs` is pinned); given the
+//                caller's result layout (g_off, g_cap), results are planned in it when its
+//                slots are contiguous (Plan::direct);
 //   run_plan     launch the GPU work (asynchronous);
 //   sync_plan    wait; rerun uncertified pairs of a scaled run with the reference count;
-//   fetch        copy the digits back (pinned) and account the work;
+//   fetch        copy the results back (pinned; a direct plan's binary results straight
+//                into `direct_g`, the caller's array) and account the work;
 //   convert_all  digits -> binary gcds for every pair of the plan.
 int plan_batch(mgcd_context* c, Plan& P, size_t np, const uint32_t* limbs, const uint64_t* u_off,
-               const uint32_t* u_len, const uint64_t* v_off, const uint32_t* v_len, bool plain);
+               const uint32_t* u_len, const uint64_t* v_off, const uint32_t* v_len, bool plain,
+               const uint64_t* g_off = nullptr, const uint32_t* g_cap = nullptr);
 int run_plan(mgcd_context* c, Plan& P);
 int sync_plan(mgcd_context* c, Plan& P);
-int fetch(mgcd_context* c, Plan& P);
+int fetch(mgcd_context* c, Plan& P, uint32_t* direct_g = nullptr);
 int convert_all(mgcd_context* c, Plan& P, uint32_t* g, const uint64_t* g_off, const uint32_t* g_cap,
                 uint32_t* g_len, int32_t* status, bool threaded);
 int to_status(int32_t st);

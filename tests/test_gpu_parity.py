@@ -111,6 +111,57 @@ def test_order_and_leading_zero_limbs(device, mgcd):
         assert mgcd.from_limbs(g[int(g_off[i]): int(g_off[i]) + int(g_len[i])]) == math.gcd(u, v)
 
 
+def test_batch_result_layouts(device, mgcd):
+    """mgcd_gcd_batch with the caller's result slots: contiguous slots after a 3-limb margin
+    (results copied back in place; nothing outside the slots touched), slots with 5-limb
+    gaps (the compact layout; the gaps keep their contents), and contiguous slots of which
+    one is a limb short of its gcd (that pair alone fails with the capacity error)."""
+    rng = random.Random(29)
+    us, vs = [], []
+    for nbits, gbits in [(100, 40), (3000, 700), (20000, 5000), (64, 1), (9000, 2000), (40000, 9000)]:
+        u, v = rand_pair(rng, nbits, gbits)
+        us.append(u)
+        vs.append(v)
+    us.append(0)
+    vs.append(123456789)                       # decided on the host
+    exp = [math.gcd(u, v) for u, v in zip(us, vs)]
+    n = len(us)
+    limbs, uo, ul, vo, vl = mgcd.pack_pairs(us, vs)
+    off, cap, tot = mgcd.result_layout(ul, vl)
+    SENT = 0xA5A5A5A5
+
+    def run(off, cap, size):
+        g = np.full(size, SENT, dtype=np.uint32)
+        gl = np.zeros(n, dtype=np.uint32)
+        st = np.zeros(n, dtype=np.int32)
+        device.gcd_batch_packed(limbs, uo, ul, vo, vl, out=(g, off, cap, gl, st))
+        res = [mgcd.from_limbs(g[int(o): int(o) + int(k)]) for o, k in zip(off, gl)]
+        return g, gl, st, res
+
+    off1 = off + np.uint64(3)
+    g, gl, st, res = run(off1, cap, tot + 7)
+    assert list(st) == [0] * n and res == exp
+    assert (g[:3] == SENT).all() and (g[tot + 3:] == SENT).all()
+
+    off2 = off + np.uint64(5) * np.arange(n, dtype=np.uint64)
+    g, gl, st, res = run(off2, cap, tot + 5 * n)
+    assert list(st) == [0] * n and res == exp
+    for i in range(n):
+        end = int(off2[i]) + int(cap[i])
+        assert (g[end: end + 5] == SENT).all()
+
+    k = 2
+    need = (exp[k].bit_length() + 31) // 32
+    cap3 = cap.copy()
+    cap3[k] = need - 1
+    off3 = np.zeros(n, dtype=np.uint64)
+    off3[1:] = np.cumsum(cap3[:-1], dtype=np.uint64)
+    g, gl, st, res = run(off3, cap3, int(cap3.sum(dtype=np.uint64)))
+    assert st[k] == mgcd.MGCD_ERR_CAPACITY and gl[k] == 0
+    assert [int(s) for i, s in enumerate(st) if i != k] == [0] * (n - 1)
+    assert [r for i, r in enumerate(res) if i != k] == [e for i, e in enumerate(exp) if i != k]
+
+
 @pytest.mark.parametrize("L", [22, 27])
 def test_other_modulus_widths(mgcd, oracle, L):
     rng = random.Random(15 + L)
